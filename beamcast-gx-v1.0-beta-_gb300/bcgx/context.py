@@ -1,0 +1,186 @@
+"""GPU context: the Python face of the C-ABI in include/bc_gx.h.
+
+`render_cuda` mirrors renderOpenCL (windows_portable/gpu_opencl_windows.go:565):
+scene, camera and settings in; linear HDR rows, compact guides, the extension
+ray count and the device name out, with the same chunked row loop and
+`on_chunk(y0, rows, data, progress)` callback. A GPU error raises; there is no
+CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib, ptr
+from .scene import Scene, SceneArrays
+from .settings import Camera, RenderSettings
+
+
+def gpu_available() -> tuple[bool, str]:
+    """openCLGPUAvailable (gpu_opencl_windows.go:172) for the CUDA backend."""
+    buf = C.create_string_buffer(512)
+    ok = lib().bc_gpu_available(buf, len(buf))
+    return bool(ok), buf.value.decode(errors="replace")
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().bc_create(int(device), C.byref(h)))
+        self._h = h
+        self._desc_keep = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().bc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def device_name(self) -> str:
+        buf = C.create_string_buffer(256)
+        check(lib().bc_device_name(self._h, buf, len(buf)), self._h)
+        return buf.value.decode()
+
+    # -- scene --
+    def upload(self, scene, scene_id: int | None = None, topology_rev: int | None = None,
+               geometry_rev: int | None = None):
+        """ensureSceneLocked (gpu_opencl_windows.go:484-495) by revision."""
+        if isinstance(scene, Scene):
+            d = scene.desc()
+            t, g = scene.revisions()
+            sid = scene.scene_id
+        elif isinstance(scene, SceneArrays):
+            d = scene.desc()
+            sid, t, g = id(scene), 1, 1
+        else:
+            raise TypeError("scene must be a Scene or SceneArrays")
+        sid = sid if scene_id is None else scene_id
+        t = t if topology_rev is None else topology_rev
+        g = g if geometry_rev is None else geometry_rev
+        check(lib().bc_scene_upload(self._h, C.byref(d), sid, t, g), self._h)
+        self._desc_keep = scene
+
+    def scene_stats(self) -> dict:
+        out = (C.c_int64 * 6)()
+        check(lib().bc_scene_stats(self._h, out, 6), self._h)
+        keys = ("nodes8", "slots", "binary_nodes", "depth8", "stack_need", "device_bytes")
+        return dict(zip(keys, list(out)))
+
+    # -- ray casting --
+    def raycast(self, rays: np.ndarray):
+        """rays: (n, 8) float32 (ox, oy, oz, tmin, dx, dy, dz, tmax) -> (t float32, prim int32)."""
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = len(r)
+        t = np.empty(n, dtype=np.float32)
+        p = np.empty(n, dtype=np.int32)
+        check(lib().bc_raycast(self._h, ptr(r, C.c_float), n, ptr(t, C.c_float), ptr(p, C.c_int32)), self._h)
+        return t, p
+
+    def occluded(self, rays: np.ndarray) -> np.ndarray:
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        out = np.empty(len(r), dtype=np.uint8)
+        check(lib().bc_occluded(self._h, ptr(r, C.c_float), len(r), ptr(out, C.c_uint8)), self._h)
+        return out.astype(bool)
+
+    def raycast_device(self, d_rays: int, n: int, d_t: int, d_prim: int, stream: int = 0):
+        """Device-pointer variant (asynchronous on `stream`)."""
+        check(lib().bc_raycast_device(self._h, C.c_void_p(d_rays), int(n), C.c_void_p(d_t), C.c_void_p(d_prim),
+                                      C.c_void_p(stream) if stream else None), self._h)
+
+    def occluded_device(self, d_rays: int, n: int, d_out: int, stream: int = 0):
+        check(lib().bc_occluded_device(self._h, C.c_void_p(d_rays), int(n), C.c_void_p(d_out),
+                                       C.c_void_p(stream) if stream else None), self._h)
+
+    # -- rendering --
+    def render_rows(self, cam: Camera, settings: RenderSettings, y0: int, rows: int, guides: bool = False):
+        W = settings.width
+        lin = np.empty((rows, W, 3), dtype=np.float32)
+        g = np.empty((rows, W, 3), dtype=np.uint32) if guides else None
+        rays = C.c_int64(0)
+        cc, sc = cam.c(), settings.c()
+        check(lib().bc_render_rows(self._h, C.byref(cc), C.byref(sc), int(y0), int(rows), ptr(lin, C.c_float),
+                                   ptr(g, C.c_uint32), C.byref(rays)), self._h)
+        return lin, g, rays.value
+
+    def render_frame(self, cam: Camera, settings: RenderSettings, want_guides: bool = True, want_rgba: bool = True):
+        W, H = settings.width, settings.height
+        lin = np.empty((H, W, 3), dtype=np.float32)
+        g = np.empty((H, W, 3), dtype=np.uint32) if want_guides else None
+        rgba = np.empty((H, W), dtype=np.uint32) if want_rgba else None
+        rays = C.c_int64(0)
+        cc, sc = cam.c(), settings.c()
+        check(lib().bc_render_frame(self._h, C.byref(cc), C.byref(sc), ptr(lin, C.c_float), ptr(g, C.c_uint32),
+                                    ptr(rgba, C.c_uint32), C.byref(rays)), self._h)
+        return {"linear": lin, "guides": g, "rgba": rgba, "rays": rays.value}
+
+    def cancel(self):
+        lib().bc_cancel(self._h)
+
+    def reset_cancel(self):
+        lib().bc_reset_cancel(self._h)
+
+
+_persistent: Context | None = None
+
+
+def persistent_context() -> Context:
+    """One context per process, like persistentCL (gpu_opencl_windows.go:132)."""
+    global _persistent
+    if _persistent is None:
+        _persistent = Context(0)
+    return _persistent
+
+
+def internal_size(settings: RenderSettings):
+    return settings.width, settings.height
+
+
+def render_cuda(scene: Scene, cam: Camera, settings: RenderSettings, cancel=None, on_chunk=None):
+    """renderOpenCL's contract on the CUDA backend.
+
+    Returns (linear (H, W, 3) float32, compact guides (H, W, 3) uint32 or None,
+    extension rays, device name). Raises on any GPU error.
+    """
+    if scene is None or scene.counts()["prims"] == 0 or scene.counts()["nodes"] == 0:
+        raise ValueError("CUDA backend requires a non-empty built scene")
+    ctx = persistent_context()
+    ctx.upload(scene)
+    w, h = internal_size(settings)
+    need_guides = (settings.denoise or settings.hbao > 0 or settings.hbao_plus > 0 or settings.taa > 0
+                   or settings.tsaa > 0 or settings.txaa > 0)
+    chunk = 64
+    if not settings.progressive_updates:
+        chunk = h
+    elif settings.publish_hz <= 15:
+        chunk = 128
+    elif settings.publish_hz >= 60:
+        chunk = 32
+    linear = np.empty((h, w, 3), dtype=np.float32)
+    guides = np.empty((h, w, 3), dtype=np.uint32) if need_guides else None
+    rays = 0
+    for y0 in range(0, h, chunk):
+        if cancel is not None and cancel():
+            raise RuntimeError("render cancelled")
+        rows = min(chunk, h - y0)
+        lin, g, r = ctx.render_rows(cam, settings, y0, rows, guides=need_guides)
+        linear[y0:y0 + rows] = lin
+        if need_guides:
+            guides[y0:y0 + rows] = g
+        rays += r
+        if on_chunk is not None:
+            on_chunk(y0, rows, lin, (y0 + rows) / h)
+    return linear, guides, rays, ctx.device_name()

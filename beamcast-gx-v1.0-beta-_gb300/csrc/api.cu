@@ -1,0 +1,293 @@
+// C-ABI: context lifetime, scene upload and the ray-cast entry points.
+// Mirrors the call sequence of renderOpenCL (gpu_opencl_windows.go:565-720):
+// init once, ensure the scene by revision, then launch and read back.
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "context.h"
+
+namespace bcgx {
+
+static thread_local std::string g_tls_error;
+
+bc_status set_error(bc_context* ctx, bc_status st, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  g_tls_error = msg;
+  return st;
+}
+
+bc_status cuda_status(bc_context* ctx, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return BC_OK;
+  std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  cudaGetLastError();  // clear a non-sticky error
+  return set_error(ctx, e == cudaErrorMemoryAllocation ? BC_ERR_OOM : BC_ERR_DEVICE, m);
+}
+
+// Reads and clears the kernel status word after the stream has drained.
+bc_status check_kernel_status(bc_context* ctx) {
+  unsigned h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_status(ctx, e, "reading kernel status");
+  if (h == 0) return BC_OK;
+  cudaMemsetAsync(ctx->d_status, 0, sizeof(unsigned), ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  if (h & kStatusStackOverflow)
+    return set_error(ctx, BC_ERR_CAPACITY, "traversal stack overflow (scene deeper than the compiled stack)");
+  if (h & kStatusTimeout) return set_error(ctx, BC_ERR_TIMEOUT, "a bounded device wait gave up");
+  if (h & kStatusCapacity) return set_error(ctx, BC_ERR_CAPACITY, "a device queue exceeded its capacity");
+  return set_error(ctx, BC_ERR_DEVICE, "unknown kernel status");
+}
+
+static bc_status upload(bc_context* ctx, DevBuf& b, const void* src, size_t bytes, const char* what) {
+  cudaError_t e = b.ensure(bytes ? bytes : 16);
+  if (e != cudaSuccess) return cuda_status(ctx, e, what);
+  if (bytes) {
+    e = cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_status(ctx, e, what);
+  }
+  return BC_OK;
+}
+
+}  // namespace bcgx
+
+using namespace bcgx;
+
+extern "C" {
+
+int bc_gpu_available(char* reason, size_t reason_len) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  std::string msg;
+  int ok = 0;
+  if (e != cudaSuccess) {
+    msg = std::string("CUDA unavailable: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+  } else if (n == 0) {
+    msg = "no CUDA device";
+  } else {
+    cudaDeviceProp p;
+    cudaGetDeviceProperties(&p, 0);
+    if (p.major == 10 && p.minor == 3) {
+      ok = 1;
+      msg = std::string("CUDA GPU: ") + p.name;
+    } else {
+      msg = std::string("device 0 (") + p.name + ") is sm_" + std::to_string(p.major) + std::to_string(p.minor) +
+            "; this build targets sm_103a";
+    }
+  }
+  if (reason && reason_len) {
+    std::snprintf(reason, reason_len, "%s", msg.c_str());
+  }
+  return ok;
+}
+
+bc_status bc_create(int device_ordinal, bc_context** out) {
+  if (!out) return set_error(nullptr, BC_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0 || device_ordinal < 0 || device_ordinal >= n) {
+    cudaGetLastError();
+    return set_error(nullptr, BC_ERR_NO_DEVICE, "no usable CUDA device at that ordinal");
+  }
+  cudaDeviceProp p;
+  e = cudaGetDeviceProperties(&p, device_ordinal);
+  if (e != cudaSuccess) return set_error(nullptr, BC_ERR_NO_DEVICE, cudaGetErrorString(e));
+  if (!(p.major == 10 && p.minor == 3))
+    return set_error(nullptr, BC_ERR_NO_DEVICE, std::string("device is not sm_103: ") + p.name);
+  bc_context* ctx = new (std::nothrow) bc_context();
+  if (!ctx) return set_error(nullptr, BC_ERR_OOM, "host allocation failed");
+  ctx->device = device_ordinal;
+  ctx->name = p.name;
+  e = cudaSetDevice(device_ordinal);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_status, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaHostAlloc((void**)&ctx->h_cancel, sizeof(int), cudaHostAllocMapped);
+  if (e == cudaSuccess) {
+    *ctx->h_cancel = 0;
+    e = cudaHostGetDevicePointer((void**)&ctx->d_cancel, ctx->h_cancel, 0);
+  }
+  if (e != cudaSuccess) {
+    bc_status st = cuda_status(nullptr, e, "context creation");
+    bc_destroy(ctx);
+    return st;
+  }
+  *out = ctx;
+  return BC_OK;
+}
+
+void bc_destroy(bc_context* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  destroy_render_buffers(ctx);
+  for (DevBuf* b : {&ctx->d_nodes, &ctx->d_tri, &ctx->d_slot64, &ctx->d_snorm, &ctx->d_slot_prim, &ctx->d_mats,
+                    &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ})
+    b->release();
+  if (ctx->d_status) cudaFree(ctx->d_status);
+  if (ctx->h_cancel) cudaFreeHost(ctx->h_cancel);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+bc_status bc_last_error(const bc_context* ctx, char* buf, size_t len) {
+  if (!buf || !len) return BC_ERR_INVALID_ARG;
+  const std::string& m = ctx ? ctx->err : g_tls_error;
+  std::snprintf(buf, len, "%s", m.c_str());
+  return BC_OK;
+}
+
+bc_status bc_device_name(const bc_context* ctx, char* buf, size_t len) {
+  if (!ctx || !buf || !len) return BC_ERR_INVALID_ARG;
+  std::snprintf(buf, len, "%s", ctx->name.c_str());
+  return BC_OK;
+}
+
+bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t scene_id, uint64_t topology_rev,
+                          uint64_t geometry_rev) {
+  if (!ctx || !scene) return set_error(ctx, BC_ERR_INVALID_ARG, "NULL context or scene");
+  if (ctx->has_scene && ctx->scene_id == scene_id && ctx->topo_rev == topology_rev && ctx->geom_rev == geometry_rev)
+    return BC_OK;
+  cudaSetDevice(ctx->device);
+  PackedScene ps;
+  std::string err;
+  bc_status st = pack_scene(*scene, &ps, &err);
+  if (st != BC_OK) return set_error(ctx, st, err);
+  if (stack_variant(ps.stack_need) == 0)
+    return set_error(ctx, BC_ERR_BAD_SCENE,
+                     "BVH too deep for the compiled traversal stack (needs " + std::to_string(ps.stack_need) + ")");
+  // The stream may still be reading the previous scene.
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_status(ctx, e, "scene upload");
+  ctx->has_scene = false;
+  const size_t slots = (size_t)ps.n_prims;
+  if ((st = upload(ctx, ctx->d_nodes, ps.nodes.data(), ps.nodes.size() * sizeof(Node8), "BVH8 upload")) ||
+      (st = upload(ctx, ctx->d_tri, ps.tri.data(), ps.tri.size() * sizeof(F4), "primitive upload")) ||
+      (st = upload(ctx, ctx->d_slot64, ps.slot64.data(), ps.slot64.size() * sizeof(double), "fp64 upload")) ||
+      (st = upload(ctx, ctx->d_snorm, ps.snorm.data(), ps.snorm.size() * sizeof(F4), "normal upload")) ||
+      (st = upload(ctx, ctx->d_slot_prim, ps.slot_prim.data(), slots * sizeof(int32_t), "order upload")) ||
+      (st = upload(ctx, ctx->d_mats, ps.mats.data(), ps.mats.size() * sizeof(MatGPU), "material upload")) ||
+      (st = upload(ctx, ctx->d_lights, ps.lights.data(), ps.lights.size() * sizeof(LightGPU), "light upload")) ||
+      (st = upload(ctx, ctx->d_lpdf, ps.light_pdf_by_prim.data(), ps.light_pdf_by_prim.size() * sizeof(float),
+                   "light pdf upload")))
+    return st;
+  // The host arrays of `ps` die at return: drain the copies first.
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_status(ctx, e, "scene upload");
+  DeviceScene& ds = ctx->ds;
+  ds.nodes = ctx->d_nodes.as<Node8>();
+  ds.tri = ctx->d_tri.as<float4>();
+  ds.slot64 = ctx->d_slot64.as<double>();
+  ds.snorm = ctx->d_snorm.as<float4>();
+  ds.slot_prim = ctx->d_slot_prim.as<int32_t>();
+  ds.mats = ctx->d_mats.as<MatGPU>();
+  ds.lights = ctx->d_lights.as<LightGPU>();
+  ds.light_pdf_by_prim = ctx->d_lpdf.as<float>();
+  ds.n_mats = (int32_t)ps.mats.size();
+  ds.n_lights = (int32_t)ps.lights.size();
+  ds.n_prims = ps.n_prims;
+  ds.stack_need = ps.stack_need;
+  ds.has_spheres = ps.has_spheres;
+  ctx->stats[0] = (int64_t)ps.nodes.size();
+  ctx->stats[1] = ps.n_prims;
+  ctx->stats[2] = ps.n_binary;
+  ctx->stats[3] = ps.depth;
+  ctx->stats[4] = ps.stack_need;
+  ctx->stats[5] = (int64_t)(ps.nodes.size() * sizeof(Node8) + ps.tri.size() * sizeof(F4) +
+                            ps.slot64.size() * sizeof(double) + ps.snorm.size() * sizeof(F4) +
+                            slots * sizeof(int32_t) + ps.mats.size() * sizeof(MatGPU) +
+                            ps.lights.size() * sizeof(LightGPU) + ps.light_pdf_by_prim.size() * sizeof(float));
+  ctx->has_scene = true;
+  ctx->scene_id = scene_id;
+  ctx->topo_rev = topology_rev;
+  ctx->geom_rev = geometry_rev;
+  return BC_OK;
+}
+
+bc_status bc_scene_stats(const bc_context* ctx, int64_t* out, int n_out) {
+  if (!ctx || !out || n_out < 0) return BC_ERR_INVALID_ARG;
+  if (!ctx->has_scene) return BC_ERR_NO_SCENE;
+  for (int i = 0; i < n_out && i < 6; i++) out[i] = ctx->stats[i];
+  return BC_OK;
+}
+
+bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, float* d_t_out, int32_t* d_prim_out,
+                            void* stream) {
+  if (!ctx) return set_error(nullptr, BC_ERR_INVALID_ARG, "NULL context");
+  if (n < 0 || (n > 0 && (!d_rays || !d_t_out || !d_prim_out)))
+    return set_error(ctx, BC_ERR_INVALID_ARG, "bad ray-cast arguments");
+  if (((uintptr_t)d_rays & 15u) != 0) return set_error(ctx, BC_ERR_INVALID_ARG, "rays must be 16-byte aligned");
+  if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  cudaError_t e = launch_raycast_closest(ctx->ds, (const float4*)d_rays, n, d_t_out, d_prim_out, ctx->d_status, 128, st);
+  return cuda_status(ctx, e, "ray-cast launch");
+}
+
+bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out, int32_t* prim_out) {
+  if (!ctx) return set_error(nullptr, BC_ERR_INVALID_ARG, "NULL context");
+  if (n < 0 || (n > 0 && (!rays || !t_out || !prim_out))) return set_error(ctx, BC_ERR_INVALID_ARG, "bad ray-cast arguments");
+  if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
+  if (n == 0) return BC_OK;
+  cudaSetDevice(ctx->device);
+  cudaError_t e;
+  if ((e = ctx->d_rays.ensure((size_t)n * 32)) || (e = ctx->d_t.ensure((size_t)n * 4)) ||
+      (e = ctx->d_prim.ensure((size_t)n * 4)))
+    return cuda_status(ctx, e, "ray-cast buffers");
+  e = cudaMemcpyAsync(ctx->d_rays.p, rays, (size_t)n * 32, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_raycast_closest(ctx->ds, ctx->d_rays.as<float4>(), n, ctx->d_t.as<float>(), ctx->d_prim.as<int32_t>(),
+                               ctx->d_status, 128, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(t_out, ctx->d_t.p, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(prim_out, ctx->d_prim.p, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_status(ctx, e, "ray cast");
+  return check_kernel_status(ctx);
+}
+
+bc_status bc_occluded_device(bc_context* ctx, const float* d_rays, int64_t n, uint8_t* d_out, void* stream) {
+  if (!ctx) return set_error(nullptr, BC_ERR_INVALID_ARG, "NULL context");
+  if (n < 0 || (n > 0 && (!d_rays || !d_out))) return set_error(ctx, BC_ERR_INVALID_ARG, "bad any-hit arguments");
+  if (((uintptr_t)d_rays & 15u) != 0) return set_error(ctx, BC_ERR_INVALID_ARG, "rays must be 16-byte aligned");
+  if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  cudaError_t e = launch_raycast_any(ctx->ds, (const float4*)d_rays, n, d_out, ctx->d_status, 128, st);
+  return cuda_status(ctx, e, "any-hit launch");
+}
+
+bc_status bc_occluded(bc_context* ctx, const float* rays, int64_t n, uint8_t* out) {
+  if (!ctx) return set_error(nullptr, BC_ERR_INVALID_ARG, "NULL context");
+  if (n < 0 || (n > 0 && (!rays || !out))) return set_error(ctx, BC_ERR_INVALID_ARG, "bad any-hit arguments");
+  if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
+  if (n == 0) return BC_OK;
+  cudaSetDevice(ctx->device);
+  cudaError_t e;
+  if ((e = ctx->d_rays.ensure((size_t)n * 32)) || (e = ctx->d_occ.ensure((size_t)n)))
+    return cuda_status(ctx, e, "any-hit buffers");
+  e = cudaMemcpyAsync(ctx->d_rays.p, rays, (size_t)n * 32, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_raycast_any(ctx->ds, ctx->d_rays.as<float4>(), n, ctx->d_occ.as<uint8_t>(), ctx->d_status, 128,
+                           ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, ctx->d_occ.p, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_status(ctx, e, "any hit");
+  return check_kernel_status(ctx);
+}
+
+bc_status bc_cancel(bc_context* ctx) {
+  if (!ctx) return BC_ERR_INVALID_ARG;
+  ctx->cancel.store(1);
+  if (ctx->h_cancel) *(volatile int*)ctx->h_cancel = 1;
+  return BC_OK;
+}
+
+bc_status bc_reset_cancel(bc_context* ctx) {
+  if (!ctx) return BC_ERR_INVALID_ARG;
+  ctx->cancel.store(0);
+  if (ctx->h_cancel) *(volatile int*)ctx->h_cancel = 0;
+  return BC_OK;
+}
+
+}  // extern "C"

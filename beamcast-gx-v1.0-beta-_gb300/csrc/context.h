@@ -1,0 +1,84 @@
+// bc_context internals shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <string>
+
+#include "../../include/bc_gx.h"
+#include "kernels.h"
+#include "pack.h"
+
+namespace bcgx {
+
+// Growable device buffer owned by a context.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+// Growable pinned host buffer.
+struct HostBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaHostAlloc(&p, bytes, cudaHostAllocDefault);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+}  // namespace bcgx
+
+struct bc_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::string name;
+  // resident scene
+  bool has_scene = false;
+  uint64_t scene_id = 0, topo_rev = 0, geom_rev = 0;
+  bcgx::DeviceScene ds;
+  bcgx::DevBuf d_nodes, d_tri, d_slot64, d_snorm, d_slot_prim, d_mats, d_lights, d_lpdf;
+  int64_t stats[6] = {0, 0, 0, 0, 0, 0};
+  // ray-cast staging
+  bcgx::DevBuf d_rays, d_t, d_prim, d_occ;
+  unsigned* d_status = nullptr;
+  // rendering state (render.cu)
+  struct RenderBuffers* rb = nullptr;
+  std::atomic<int> cancel{0};
+  int* h_cancel = nullptr;  // host-mapped cancel flag read by device loops
+  int* d_cancel = nullptr;
+};
+
+namespace bcgx {
+bc_status set_error(bc_context* ctx, bc_status st, const std::string& msg);
+bc_status cuda_status(bc_context* ctx, cudaError_t e, const char* what);
+bc_status check_kernel_status(bc_context* ctx);
+void destroy_render_buffers(bc_context* ctx);
+}  // namespace bcgx

@@ -1,0 +1,34 @@
+// Host-side launchers of the CUDA kernels (one declaration per kernel family).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "layout.h"
+
+namespace bcgx {
+
+struct DeviceScene {
+  const Node8* nodes = nullptr;
+  const float4* tri = nullptr;
+  const double* slot64 = nullptr;
+  const float4* snorm = nullptr;
+  const int32_t* slot_prim = nullptr;
+  const MatGPU* mats = nullptr;
+  const LightGPU* lights = nullptr;
+  const float* light_pdf_by_prim = nullptr;
+  int32_t n_mats = 0, n_lights = 0, n_prims = 0;
+  int32_t stack_need = 0;
+  bool has_spheres = false;
+};
+
+// Picks the smallest compiled stack size >= need; 0 if none fits.
+int stack_variant(int need);
+
+// Exact closest hit over n rays (8 floats each); see bc_raycast in bc_gx.h.
+cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int64_t n, float* t_out,
+                                   int32_t* prim_out, unsigned* status, int block, cudaStream_t st);
+// Exact any hit.
+cudaError_t launch_raycast_any(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
+                               int block, cudaStream_t st);
+
+}  // namespace bcgx

@@ -1,0 +1,289 @@
+// Host packer (see pack.h). Validation mirrors validateGPUSceneEncoding
+// (gpu_opencl_windows.go:470-482) and adds the structural checks a device
+// kernel needs to stay in bounds: child indices, leaf ranges, the Order
+// permutation and material indices are all checked here, once, on the host.
+#include "pack.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace bcgx {
+
+float round_down_f32(double x) {
+  float f = (float)x;
+  if ((double)f > x) f = std::nextafterf(f, -INFINITY);
+  return f;
+}
+float round_up_f32(double x) {
+  float f = (float)x;
+  if ((double)f < x) f = std::nextafterf(f, INFINITY);
+  return f;
+}
+
+namespace {
+
+double box_area(const double* b) {
+  double ex = b[3] - b[0], ey = b[4] - b[1], ez = b[5] - b[2];
+  if (ex < 0 || ey < 0 || ez < 0) return 0;
+  return 2 * (ex * ey + ey * ez + ez * ex);
+}
+
+bc_status fail(std::string* err, const std::string& m) {
+  if (err) *err = m;
+  return BC_ERR_BAD_SCENE;
+}
+
+bc_status validate(const bc_scene_desc& d, std::string* err) {
+  if (d.n_prims <= 0 || d.n_nodes <= 0)
+    return fail(err, "scene requires a non-empty built scene (primitives and BVH nodes)");
+  if (d.n_nodes >= kMaxIndex || d.n_prims >= kMaxIndex)
+    return fail(err, "compact BVH supports fewer than 134217728 nodes/primitives");
+  if (!d.prim_kind || !d.prim_material || !d.node_box || !d.node_left || !d.node_right || !d.node_start ||
+      !d.node_count || !d.order)
+    return fail(err, "scene descriptor is missing primitive or node arrays");
+  if (d.n_materials < 1 || !d.mat_kind || !d.mat_color || !d.mat_emission)
+    return fail(err, "scene requires at least one material");
+  bool any_sphere = false, any_tri = false;
+  for (int32_t i = 0; i < d.n_prims; i++) {
+    if (d.prim_kind[i] == BC_PRIM_SPHERE) any_sphere = true;
+    else if (d.prim_kind[i] == BC_PRIM_TRIANGLE) any_tri = true;
+    else return fail(err, "primitive " + std::to_string(i) + " has an unknown kind");
+  }
+  if (any_sphere && (!d.prim_center || !d.prim_radius)) return fail(err, "sphere arrays missing");
+  if (any_tri && (!d.prim_a || !d.prim_e1 || !d.prim_e2 || !d.prim_normal)) return fail(err, "triangle arrays missing");
+  for (int32_t i = 0; i < d.n_nodes; i++) {
+    int32_t c = d.node_count[i];
+    if (c < 0 || c > 16)
+      return fail(err, "compact BVH leaf " + std::to_string(i) + " has unsupported count " + std::to_string(c));
+    if (c > 0) {
+      if (d.node_start[i] < 0 || (int64_t)d.node_start[i] + c > d.n_prims)
+        return fail(err, "leaf " + std::to_string(i) + " range outside Order");
+    } else {
+      int32_t l = d.node_left[i], r = d.node_right[i];
+      if (l <= i || r <= i || l >= d.n_nodes || r >= d.n_nodes || l == r)
+        return fail(err, "inner node " + std::to_string(i) + " has invalid children");
+    }
+  }
+  // Each node reachable exactly once from the root (children always follow
+  // their parent, so the walk terminates).
+  std::vector<uint8_t> seen(d.n_nodes, 0);
+  std::vector<int32_t> st{0};
+  while (!st.empty()) {
+    int32_t i = st.back();
+    st.pop_back();
+    if (seen[i]) return fail(err, "node " + std::to_string(i) + " is shared by two parents");
+    seen[i] = 1;
+    if (d.node_count[i] == 0) {
+      st.push_back(d.node_left[i]);
+      st.push_back(d.node_right[i]);
+    }
+  }
+  std::vector<uint8_t> used(d.n_prims, 0);
+  for (int32_t i = 0; i < d.n_prims; i++) {
+    int32_t p = d.order[i];
+    if (p < 0 || p >= d.n_prims || used[p]) return fail(err, "Order is not a permutation of the primitives");
+    used[p] = 1;
+  }
+  if (d.n_lights < 0 || (d.n_lights > 0 && (!d.light_spheres || !d.light_cdf)))
+    return fail(err, "light arrays missing");
+  for (int32_t i = 0; i < d.n_lights; i++) {
+    int32_t p = d.light_spheres[i];
+    if (p < 0 || p >= d.n_prims || d.prim_kind[p] != BC_PRIM_SPHERE)
+      return fail(err, "light " + std::to_string(i) + " is not a sphere primitive");
+  }
+  return BC_OK;
+}
+
+void pack_slots(const bc_scene_desc& d, PackedScene* ps) {
+  const int32_t n = d.n_prims;
+  ps->tri.resize(3 * (size_t)n);
+  ps->slot64.assign(9 * (size_t)n, 0.0);
+  ps->snorm.resize(n);
+  ps->slot_prim.resize(n);
+  ps->has_spheres = false;
+  for (int32_t s = 0; s < n; s++) {
+    const int32_t p = d.order[s];
+    ps->slot_prim[s] = p;
+    F4* r = &ps->tri[3 * (size_t)s];
+    double* q = &ps->slot64[9 * (size_t)s];
+    int32_t mat = d.prim_material[p];
+    float matbits;
+    std::memcpy(&matbits, &mat, 4);
+    if (d.prim_kind[p] == BC_PRIM_SPHERE) {
+      ps->has_spheres = true;
+      const double* c = d.prim_center + 3 * (size_t)p;
+      double rad = d.prim_radius[p];
+      r[0] = F4{(float)c[0], (float)c[1], (float)c[2], (float)rad};
+      r[1] = F4{(float)(rad * rad), rad > 0 ? (float)(1.0 / rad) : 0.0f, 0.0f, 0.0f};
+      r[2] = F4{0.0f, 0.0f, 0.0f, -1.0f};
+      q[0] = c[0]; q[1] = c[1]; q[2] = c[2]; q[3] = rad;
+      ps->snorm[s] = F4{0.0f, 0.0f, 0.0f, matbits};
+    } else {
+      const double* a = d.prim_a + 3 * (size_t)p;
+      const double* e1 = d.prim_e1 + 3 * (size_t)p;
+      const double* e2 = d.prim_e2 + 3 * (size_t)p;
+      const double* nn = d.prim_normal + 3 * (size_t)p;
+      auto amax = [](const double* v) {
+        return round_up_f32(std::max(std::fabs(v[0]), std::max(std::fabs(v[1]), std::fabs(v[2]))));
+      };
+      r[0] = F4{(float)a[0], (float)a[1], (float)a[2], amax(a)};
+      r[1] = F4{(float)e1[0], (float)e1[1], (float)e1[2], amax(e1)};
+      r[2] = F4{(float)e2[0], (float)e2[1], (float)e2[2], amax(e2)};
+      for (int k = 0; k < 3; k++) { q[k] = a[k]; q[3 + k] = e1[k]; q[6 + k] = e2[k]; }
+      ps->snorm[s] = F4{(float)nn[0], (float)nn[1], (float)nn[2], matbits};
+    }
+  }
+}
+
+// Outward-rounded fp32 box with one extra ulp of slack, so that a ray origin
+// lying exactly on an fp64 face is strictly inside the fp32 box.
+void store_child_box(Node8& n, int slot, const double* b) {
+  n.lox[slot] = std::nextafterf(round_down_f32(b[0]), -INFINITY);
+  n.loy[slot] = std::nextafterf(round_down_f32(b[1]), -INFINITY);
+  n.loz[slot] = std::nextafterf(round_down_f32(b[2]), -INFINITY);
+  n.hix[slot] = std::nextafterf(round_up_f32(b[3]), INFINITY);
+  n.hiy[slot] = std::nextafterf(round_up_f32(b[4]), INFINITY);
+  n.hiz[slot] = std::nextafterf(round_up_f32(b[5]), INFINITY);
+}
+
+uint32_t leaf_ref(const bc_scene_desc& d, int32_t i) {
+  return kLeafBit | ((uint32_t)(d.node_count[i] - 1) & 0xfu) << 27 | ((uint32_t)d.node_start[i] & kSlotMask);
+}
+
+// Wide collapse: repeatedly open the inner child of largest surface area
+// until a node has 8 children or only leaves. Leaves (and their primitive
+// ranges) are carried over unchanged, so the leaf sets match the binary tree.
+void collapse(const bc_scene_desc& d, PackedScene* ps) {
+  ps->nodes.clear();
+  struct Job { int32_t bin, parent, slot, depth, acc; };
+  std::vector<Job> jobs{Job{0, -1, 0, 1, 0}};
+  ps->depth = 0;
+  ps->stack_need = 1;
+  while (!jobs.empty()) {
+    Job j = jobs.back();
+    jobs.pop_back();
+    const int32_t idx = (int32_t)ps->nodes.size();
+    ps->nodes.emplace_back();
+    if (j.parent >= 0) ps->nodes[j.parent].child[j.slot] = (uint32_t)idx;
+    int32_t kids[8];
+    int nk = 0;
+    if (d.node_count[j.bin] > 0) {
+      kids[nk++] = j.bin;  // single-leaf scene: the root holds one leaf child
+    } else {
+      kids[nk++] = d.node_left[j.bin];
+      kids[nk++] = d.node_right[j.bin];
+      while (nk < 8) {
+        int best = -1;
+        double best_area = -1;
+        for (int k = 0; k < nk; k++) {
+          if (d.node_count[kids[k]] > 0) continue;
+          double a = box_area(d.node_box + 6 * (size_t)kids[k]);
+          if (a > best_area) { best_area = a; best = k; }
+        }
+        if (best < 0) break;
+        int32_t b = kids[best];
+        kids[best] = d.node_left[b];
+        for (int k = nk; k > best + 1; k--) kids[k] = kids[k - 1];
+        kids[best + 1] = d.node_right[b];
+        nk++;
+      }
+    }
+    Node8& n = ps->nodes[idx];
+    std::memset(&n, 0, sizeof(n));
+    n.nchild = nk;
+    for (int k = nk; k < 8; k++) {  // unused slots: empty boxes, never read
+      n.lox[k] = n.loy[k] = n.loz[k] = INFINITY;
+      n.hix[k] = n.hiy[k] = n.hiz[k] = -INFINITY;
+      n.child[k] = 0;
+    }
+    ps->depth = std::max(ps->depth, j.depth);
+    ps->stack_need = std::max(ps->stack_need, j.acc + nk + 1);
+    for (int k = nk - 1; k >= 0; k--) {
+      store_child_box(ps->nodes[idx], k, d.node_box + 6 * (size_t)kids[k]);
+      if (d.node_count[kids[k]] > 0) {
+        ps->nodes[idx].child[k] = leaf_ref(d, kids[k]);
+      } else {
+        jobs.push_back(Job{kids[k], idx, k, j.depth + 1, j.acc + nk - 1});
+      }
+    }
+  }
+}
+
+void pack_materials(const bc_scene_desc& d, PackedScene* ps) {
+  ps->mats.resize(d.n_materials);
+  for (int32_t i = 0; i < d.n_materials; i++) {
+    const double* c = d.mat_color + 3 * (size_t)i;
+    const double* e = d.mat_emission + 3 * (size_t)i;
+    MatGPU& m = ps->mats[i];
+    m.cr = (float)c[0]; m.cg = (float)c[1]; m.cb = (float)c[2];
+    m.rough = d.mat_roughness ? (float)d.mat_roughness[i] : 0.0f;
+    m.er = (float)e[0]; m.eg = (float)e[1]; m.eb = (float)e[2];
+    m.kind = (float)d.mat_kind[i];
+    m.ior = d.mat_ior ? (float)d.mat_ior[i] : 0.0f;
+    // materialPreviewColor (renderer.go:1467-1475)
+    if (d.mat_kind[i] == BC_MAT_EMISSIVE) {
+      auto cl = [](double x) { return (float)std::min(1.0, std::max(0.0, x / 8)); };
+      m.preview_r = cl(e[0]); m.preview_g = cl(e[1]); m.preview_b = cl(e[2]);
+    } else if (c[0] * c[0] + c[1] * c[1] + c[2] * c[2] > 0) {
+      m.preview_r = (float)c[0]; m.preview_g = (float)c[1]; m.preview_b = (float)c[2];
+    } else {
+      m.preview_r = m.preview_g = m.preview_b = 0.8f;
+    }
+  }
+}
+
+void pack_lights(const bc_scene_desc& d, PackedScene* ps) {
+  ps->lights.resize(d.n_lights);
+  ps->light_pdf_by_prim.assign(d.n_prims, 0.0f);
+  if (d.light_pdf_by_prim)
+    for (int32_t i = 0; i < d.n_prims; i++) ps->light_pdf_by_prim[i] = (float)d.light_pdf_by_prim[i];
+  for (int32_t i = 0; i < d.n_lights; i++) {
+    int32_t p = d.light_spheres[i];
+    LightGPU& L = ps->lights[i];
+    const double* c = d.prim_center + 3 * (size_t)p;
+    L.cx = (float)c[0]; L.cy = (float)c[1]; L.cz = (float)c[2];
+    L.r = (float)d.prim_radius[p];
+    int32_t m = d.prim_material[p];
+    const double* e = (m >= 0 && m < d.n_materials) ? d.mat_emission + 3 * (size_t)m : nullptr;
+    L.er = e ? (float)e[0] : 0.0f; L.eg = e ? (float)e[1] : 0.0f; L.eb = e ? (float)e[2] : 0.0f;
+    double pdf = d.light_pdf_by_prim ? d.light_pdf_by_prim[p] : 0.0;
+    if (pdf <= 0) pdf = 1.0 / (double)d.n_lights;  // chooseLight fallback, renderer.go:1389-1391
+    L.select_pdf = (float)pdf;
+    L.cdf = (float)d.light_cdf[i];
+    L.prim = p;
+  }
+}
+
+}  // namespace
+
+bc_status pack_scene(const bc_scene_desc& d, PackedScene* out, std::string* err) {
+  bc_status st = validate(d, err);
+  if (st != BC_OK) return st;
+  try {
+    out->n_prims = d.n_prims;
+    out->n_binary = d.n_nodes;
+    pack_slots(d, out);
+    collapse(d, out);
+    pack_materials(d, out);
+    pack_lights(d, out);
+    for (int k = 0; k < 3; k++) {
+      out->scene_lo[k] = round_down_f32(d.node_box[k]);
+      out->scene_hi[k] = round_up_f32(d.node_box[3 + k]);
+    }
+  } catch (const std::bad_alloc&) {
+    if (err) *err = "host allocation failed while packing the scene";
+    return BC_ERR_OOM;
+  }
+  return BC_OK;
+}
+
+bc_status repack_geometry(const bc_scene_desc& d, PackedScene* io, std::string* err) {
+  if (d.n_prims != io->n_prims || d.n_nodes != io->n_binary) {
+    if (err) *err = "geometry update changes the topology; a full upload is required";
+    return BC_ERR_BAD_SCENE;
+  }
+  return pack_scene(d, io, err);
+}
+
+}  // namespace bcgx

@@ -1,0 +1,36 @@
+// Host packer: validates a bc_scene_desc and converts the reference's binary
+// BVH into the device layout of layout.h (BVH8 collapse, outward-rounded fp32
+// boxes, Order-sorted primitive slots).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/bc_gx.h"
+#include "layout.h"
+
+namespace bcgx {
+
+struct PackedScene {
+  std::vector<Node8> nodes;
+  std::vector<F4> tri;           // 3 per slot
+  std::vector<double> slot64;    // 9 per slot
+  std::vector<F4> snorm;         // 1 per slot
+  std::vector<int32_t> slot_prim;
+  std::vector<MatGPU> mats;
+  std::vector<LightGPU> lights;
+  std::vector<float> light_pdf_by_prim;
+  int32_t n_prims = 0, n_binary = 0;
+  int32_t depth = 0, stack_need = 0;
+  bool has_spheres = false;
+  float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
+};
+
+// Fills `out`; returns BC_OK or BC_ERR_BAD_SCENE / BC_ERR_INVALID_ARG with a message.
+bc_status pack_scene(const bc_scene_desc& d, PackedScene* out, std::string* err);
+// Re-packs only geometry (boxes and primitive records) for an unchanged topology.
+bc_status repack_geometry(const bc_scene_desc& d, PackedScene* io, std::string* err);
+
+float round_down_f32(double x);
+float round_up_f32(double x);
+
+}  // namespace bcgx

@@ -1,0 +1,106 @@
+// Ray-cast kernels: exact closest hit and any hit over the BVH8, one thread
+// per ray. Rays are 32-byte records (ox, oy, oz, tmin, dx, dy, dz, tmax) read
+// with two 128-bit loads; results are written as coalesced 4-byte streams.
+#include "kernels.h"
+#include "trace_core.cuh"
+
+namespace bcgx {
+
+int stack_variant(int need) {
+  if (need <= 64) return 64;
+  if (need <= 128) return 128;
+  if (need <= 256) return 256;
+  return 0;
+}
+
+namespace {
+
+template <int STACK, bool SPHERES>
+__global__ void __launch_bounds__(128) k_closest_exact(SceneView sv, const float4* __restrict__ rays, int64_t n,
+                                                       float* __restrict__ t_out, int32_t* __restrict__ prim_out,
+                                                       unsigned* status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 a = __ldg(rays + 2 * i);
+  const float4 b = __ldg(rays + 2 * i + 1);
+  const Ray32 r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
+  const HitResult h = closest_hit<STACK, true, SPHERES>(sv, r, b.w, (double)b.w, status);
+  if (h.slot >= 0) {
+    t_out[i] = __double2float_rn(h.t64);
+    prim_out[i] = __ldg(sv.slot_prim + h.slot);
+  } else {
+    t_out[i] = -1.0f;
+    prim_out[i] = -1;
+  }
+}
+
+template <int STACK, bool SPHERES>
+__global__ void __launch_bounds__(128) k_any_exact(SceneView sv, const float4* __restrict__ rays, int64_t n,
+                                                   uint8_t* __restrict__ out, unsigned* status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 a = __ldg(rays + 2 * i);
+  const float4 b = __ldg(rays + 2 * i + 1);
+  const Ray32 r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
+  out[i] = any_hit<STACK, true, SPHERES>(sv, r, b.w, (double)b.w, status) ? 1 : 0;
+}
+
+SceneView view_of(const DeviceScene& s) {
+  SceneView v;
+  v.nodes = s.nodes;
+  v.tri = s.tri;
+  v.slot64 = s.slot64;
+  v.snorm = s.snorm;
+  v.slot_prim = s.slot_prim;
+  return v;
+}
+
+template <int STACK>
+cudaError_t closest_stack(const DeviceScene& s, const float4* rays, int64_t n, float* t, int32_t* p, unsigned* status,
+                          int block, cudaStream_t st) {
+  const int64_t grid = (n + 127) / 128;
+  (void)block;
+  if (s.has_spheres)
+    k_closest_exact<STACK, true><<<(unsigned)grid, 128, 0, st>>>(view_of(s), rays, n, t, p, status);
+  else
+    k_closest_exact<STACK, false><<<(unsigned)grid, 128, 0, st>>>(view_of(s), rays, n, t, p, status);
+  return cudaGetLastError();
+}
+
+template <int STACK>
+cudaError_t any_stack(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status, int block,
+                      cudaStream_t st) {
+  const int64_t grid = (n + 127) / 128;
+  (void)block;
+  if (s.has_spheres)
+    k_any_exact<STACK, true><<<(unsigned)grid, 128, 0, st>>>(view_of(s), rays, n, out, status);
+  else
+    k_any_exact<STACK, false><<<(unsigned)grid, 128, 0, st>>>(view_of(s), rays, n, out, status);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int64_t n, float* t_out,
+                                   int32_t* prim_out, unsigned* status, int block, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  switch (stack_variant(s.stack_need)) {
+    case 64: return closest_stack<64>(s, rays, n, t_out, prim_out, status, block, st);
+    case 128: return closest_stack<128>(s, rays, n, t_out, prim_out, status, block, st);
+    case 256: return closest_stack<256>(s, rays, n, t_out, prim_out, status, block, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_raycast_any(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
+                               int block, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  switch (stack_variant(s.stack_need)) {
+    case 64: return any_stack<64>(s, rays, n, out, status, block, st);
+    case 128: return any_stack<128>(s, rays, n, out, status, block, st);
+    case 256: return any_stack<256>(s, rays, n, out, status, block, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace bcgx

@@ -1,0 +1,300 @@
+"""Benchmark of the GB300 hot path (one JSON line on rank 0).
+
+Workload (the ray-cast configuration of the measurement plan): 1,000,000
+seeded random triangles (centroids U[0,1]^3, edge lengths LogNormal(-5, 0.5)),
+32-bin SAH BVH collapsed to BVH8, 4,194,304 seeded rays (origins U[0,1]^3,
+directions uniform on the sphere), exact closest hit. A step is one ray cast
+of all 4M rays; a path segment is one closest-hit query (the unit the
+reference counts as Rays, renderer.go:1491).
+
+  value  : Mpath-segments/s over all ranks, rays resident in HBM, device time
+           from CUDA events on the launching stream; L2 flushed between steps.
+  e2e    : the same through the host-buffer C-ABI call bc_raycast (host->device
+           copy of the rays, the kernel, device->host copy of t and prim).
+  roofline: algorithmic bytes per ray from the oracle's binary-BVH traversal
+           counters on the CPU-baseline sample, 32*boxes + 40*tris + 24 + 8,
+           times the rays of one launch, over the average kernel time.
+
+Multi-GPU: every rank casts its own 4M rays (weak scaling, no collective on
+the data path); rank 0 reports max-over-ranks time.
+`--impl reference` times the CPU restatement of the reference renderer
+(the oracle port) on the host cores instead, with the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "beamcast-gx-v1.0-beta-_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+N_TRIS = 1_000_000
+N_RAYS = 4_194_304
+METRIC = "Mpath-segments/s"
+WORKLOAD = "raycast: 1M random tris (32-bin SAH -> BVH8), 4M random rays, exact closest hit"
+DATA = "synthetic, seeded (tris seed 0xBEAC0002, rays seed 0xBEAC0003)"
+
+
+def _dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _make_workload():
+    from bcgx import scenes
+    spec = scenes.random_triangles(N_TRIS, seed=scenes.SEED_C2)
+    rays = scenes.random_rays(N_RAYS, seed=scenes.SEED_C3)
+    return spec, rays
+
+
+def cpu_baseline(spec, rays, seconds_target=15.0, threads=0):
+    """The oracle (fp64 restatement of Scene.Hit) on a bounded sample of rays.
+    Returns (Mpath-segments/s, cores, sample description, algorithmic bytes per ray)."""
+    import numpy as np
+    import oracle
+    ref = oracle.OracleScene.from_spec(spec)
+    cores = threads or os.cpu_count() or 1
+    n = 65_536
+    t0 = time.perf_counter()
+    _, _, cnt = ref.hit_f32(rays[:n], threads=cores)
+    dt = time.perf_counter() - t0
+    # grow the sample to roughly seconds_target of CPU work
+    m = int(min(len(rays), max(n, n * seconds_target / max(dt, 1e-3))))
+    rng = np.random.default_rng(1234)
+    idx = np.sort(rng.choice(len(rays), m, replace=False))
+    sample = np.ascontiguousarray(rays[idx])
+    t0 = time.perf_counter()
+    _, _, cnt = ref.hit_f32(sample, threads=cores)
+    dt = time.perf_counter() - t0
+    boxes, tris, sph = (int(x) for x in cnt)
+    bytes_per_ray = (32 * boxes + 40 * tris + 32 * sph) / m + 24 + 8
+    return m / dt / 1e6, cores, f"{m} of {len(rays)} rays (seeded subset), {dt:.1f} s", bytes_per_ray, \
+        {"box_tests_per_ray": boxes / m, "tri_tests_per_ray": tris / m}
+
+
+def run_reference(args):
+    ws, rank, _ = _dist_env()
+    if rank != 0:
+        return 0
+    spec, rays = _make_workload()
+    import numpy as np
+    import oracle
+    ref = oracle.OracleScene.from_spec(spec)
+    cores = os.cpu_count() or 1
+    per_step = 262_144
+    rng = np.random.default_rng(99)
+    for _ in range(args.warmup):
+        idx = rng.choice(len(rays), per_step, replace=False)
+        ref.hit_f32(np.ascontiguousarray(rays[np.sort(idx)]), threads=cores)
+    times = []
+    for _ in range(args.steps):
+        idx = rng.choice(len(rays), per_step, replace=False)
+        sample = np.ascontiguousarray(rays[np.sort(idx)])
+        t0 = time.perf_counter()
+        ref.hit_f32(sample, threads=cores)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = per_step * args.steps / total / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+            "config": {"workload": WORKLOAD, "rays_per_step": per_step, "triangles": N_TRIS},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                             "sample": f"{per_step} seeded rays of the 4M-ray set per step"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    import bcgx
+
+    ws, rank, local = _dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from bcgx import scenes
+    spec, rays = _make_workload()
+    scene = scenes.to_scene(spec)
+    ctx = bcgx.Context(local)
+    ctx.upload(scene)
+    stats = ctx.scene_stats()
+
+    stream = torch.cuda.Stream(device=dev)
+    d_rays = torch.from_numpy(rays).to(dev)
+    d_t = torch.empty(N_RAYS, dtype=torch.float32, device=dev)
+    d_p = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+
+    def step():
+        ctx.raycast_device(d_rays.data_ptr(), N_RAYS, d_t.data_ptr(), d_p.data_ptr(), stream.cuda_stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()  # L2 flush between steps, outside the events
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    kernel_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(kernel_ms)
+
+    # e2e: the host-buffer entry point, pinned host rays, copies inside the region
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_np = h_rays.numpy()
+    e2e_steps = max(1, min(args.steps, 5))
+    ctx.raycast(h_np)  # warm the staging buffers
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        t_h, p_h = ctx.raycast(h_np)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    clk = clocks.stop()
+
+    if dist:
+        tt = torch.tensor([total_ms, e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms, e2e_s = float(tt[0]), float(tt[1])
+        dist.barrier()
+    if rank != 0:
+        ctx.close()
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    value = ws * N_RAYS * args.steps / (total_ms / 1e3) / 1e6
+    e2e_value = ws * N_RAYS / e2e_s / 1e6
+    peak, peak_kind = _peaks()
+    cpu_v, cores, sample, bytes_per_ray, counters = cpu_baseline(spec, rays)
+    avg_ms = total_ms / args.steps
+    achieved = bytes_per_ray * N_RAYS / (avg_ms / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "raycast_c2_traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": avg_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 traversal + f64 re-test", "data": DATA,
+        "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays_per_gpu": N_RAYS,
+                   "l2": "flushed between steps (256 MiB write)", "bvh8_nodes": stats["nodes8"],
+                   "bvh8_depth": stats["depth8"], "scene_bytes": stats["device_bytes"]},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": N_RAYS * 32,
+                "d2h_bytes_per_step": N_RAYS * 8},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_ray": bytes_per_ray, **counters},
+        "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+        "kernel_ms": [round(x, 4) for x in kernel_ms],
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,202 @@
+/*
+ * bc_gx.h - C ABI of the GB300-native Beamcast GX path-tracing hot path.
+ *
+ * This library replaces the explicit-GPU OpenCL slot of the portable Go
+ * renderer (windows_portable/gpu_opencl_windows.go, stub gpu_opencl_stub.go).
+ * Every entry point takes plain pointers and sizes, returns a bc_status, and
+ * never aborts or traps: a failure is reported through the status and
+ * bc_last_error(). There is no CPU fallback: without a usable GPU the calls
+ * fail with BC_ERR_NO_DEVICE.
+ *
+ * Threading: a bc_context is not thread-safe (the Go glue holds a mutex, as
+ * persistentCL.mu does at gpu_opencl_windows.go:94-131). bc_cancel() alone may
+ * be called from any thread.
+ *
+ * Memory: host buffers are caller-owned and are not retained after a call
+ * returns; device memory and pinned staging are owned by the context and
+ * released by bc_destroy().
+ */
+#ifndef BC_GX_H
+#define BC_GX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bc_status {
+  BC_OK = 0,
+  BC_ERR_NO_DEVICE = 1,     /* no CUDA device / driver, or not sm_103 */
+  BC_ERR_OOM = 2,           /* device or pinned allocation failed */
+  BC_ERR_BAD_SCENE = 3,     /* scene encoding rejected (gpu_opencl_windows.go:470-482) */
+  BC_ERR_CANCELLED = 4,     /* bc_cancel() observed ("render cancelled", gpu_opencl_windows.go:645) */
+  BC_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up */
+  BC_ERR_DEVICE = 6,        /* any other CUDA error; the context may need bc_destroy() */
+  BC_ERR_INVALID_ARG = 7,   /* null pointer, bad size, bad setting */
+  BC_ERR_NO_SCENE = 8,      /* render or ray cast before bc_scene_upload() */
+  BC_ERR_CAPACITY = 9       /* a queue or buffer limit of the context was exceeded */
+} bc_status;
+
+typedef struct bc_context bc_context;
+
+/* Material kinds (renderer.go:85-92) and primitive kinds (renderer.go:102-107). */
+enum { BC_MAT_DIFFUSE = 0, BC_MAT_METAL = 1, BC_MAT_GLASS = 2, BC_MAT_EMISSIVE = 3 };
+enum { BC_PRIM_SPHERE = 0, BC_PRIM_TRIANGLE = 1 };
+/* Samplers (renderer.go:1019-1025). */
+enum { BC_SAMPLER_RANDOM = 0, BC_SAMPLER_HALTON = 1, BC_SAMPLER_R2 = 2 };
+
+/*
+ * Scene hand-off. Mirrors the fields of Go's Scene (renderer.go:225-240) after
+ * Scene.Build(): primitives as the reference stores them (fp64), the binary
+ * BVH produced by the reference's own builder (Nodes + Order), and the light
+ * distribution (LightSpheres, LightCDF, LightPDFByPrim). The library copies
+ * what it needs; nothing is retained after bc_scene_upload() returns.
+ * Arrays marked 3n/6n are row-major (x, y, z) triples / (min xyz, max xyz).
+ */
+typedef struct bc_scene_desc {
+  int32_t n_materials;
+  const int32_t* mat_kind;        /* n_materials */
+  const double* mat_color;        /* 3n */
+  const double* mat_roughness;    /* n */
+  const double* mat_ior;          /* n */
+  const double* mat_emission;     /* 3n */
+
+  int32_t n_prims;
+  const int32_t* prim_kind;       /* BC_PRIM_* */
+  const int32_t* prim_material;
+  const double* prim_center;      /* 3n, spheres */
+  const double* prim_radius;      /* n, spheres */
+  const double* prim_a;           /* 3n, triangle vertex A */
+  const double* prim_e1;          /* 3n, B - A */
+  const double* prim_e2;          /* 3n, C - A */
+  const double* prim_normal;      /* 3n, unit(E1 x E2) */
+
+  int32_t n_nodes;
+  const double* node_box;         /* 6n */
+  const int32_t* node_left;       /* -1 for leaves */
+  const int32_t* node_right;
+  const int32_t* node_start;      /* leaves: first index into order */
+  const int32_t* node_count;      /* leaves: 1..16 primitives; 0 for internal nodes */
+  const int32_t* order;           /* n_prims permutation (Scene.Order) */
+
+  int32_t n_lights;
+  const int32_t* light_spheres;   /* prim indices of emissive spheres */
+  const double* light_cdf;        /* n_lights */
+  const double* light_pdf_by_prim;/* n_prims */
+} bc_scene_desc;
+
+/* Pinhole camera (renderer.go:941-960). */
+typedef struct bc_camera {
+  double position[3], target[3], up[3];
+  double fov_deg;
+} bc_camera;
+
+/*
+ * The subset of RenderSettings (renderer.go:1027-1062) that the hot path reads.
+ * Path integrator only (IntegratorPath).
+ */
+typedef struct bc_settings {
+  int32_t width, height, spp, bounces;
+  int32_t msaa, tsaa;             /* effectiveSPP factors (renderer.go:2395-2417) */
+  int32_t sampler;                /* BC_SAMPLER_* */
+  int32_t mis, power_light_sampling;
+  double firefly_clamp;           /* <= 0: off */
+  int32_t rr_depth;               /* < 1 means 4 (renderer.go:1550-1553) */
+  int32_t adaptive_sampling;
+  double adaptive_threshold;
+  int32_t denoise, taa, txaa;     /* a-trous passes = 2 + min(3, max(taa, txaa)) (renderer.go:2845) */
+  int32_t bloom, hdr;             /* bloom level, tone-map curve (renderer.go:2034-2053) */
+  double exposure, gamma;
+  uint64_t seed;                  /* path RNG seed: equal seeds give equal images */
+} bc_settings;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Availability probe; replaces openCLGPUAvailable() (gpu_opencl_windows.go:172,
+ * stub gpu_opencl_stub.go:10). Returns 1 if a usable device exists, else 0,
+ * and writes a one-line reason into reason[reason_len] either way. */
+int bc_gpu_available(char* reason, size_t reason_len);
+
+/* Create a context on a CUDA device ordinal (persistentCL initLocked,
+ * gpu_opencl_windows.go:224). */
+bc_status bc_create(int device_ordinal, bc_context** out);
+void bc_destroy(bc_context* ctx);
+/* Copies the last error message of this context (thread-local message when ctx is NULL). */
+bc_status bc_last_error(const bc_context* ctx, char* buf, size_t len);
+bc_status bc_device_name(const bc_context* ctx, char* buf, size_t len);
+
+/* ---- scene -------------------------------------------------------------- */
+
+/*
+ * Upload or update a scene; replaces ensureSceneLocked (gpu_opencl_windows.go:484-495)
+ * with uploadFullSceneLocked (379) and updateGeometryLocked (447). scene_id
+ * identifies the caller's scene object (Go: the *Scene pointer value). When
+ * scene_id and topology_rev match the resident scene, only geometry is
+ * re-packed if geometry_rev changed; when all three match, the call is a no-op.
+ * Leaves with more than 16 primitives or more than 2^27 nodes/primitives are
+ * rejected with BC_ERR_BAD_SCENE, as validateGPUSceneEncoding (470-482) does.
+ */
+bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t scene_id, uint64_t topology_rev,
+                          uint64_t geometry_rev);
+
+/* Statistics of the resident scene: out[0] BVH8 nodes, out[1] primitive slots,
+ * out[2] binary nodes, out[3] BVH8 depth, out[4] traversal stack entries needed,
+ * out[5] device bytes held by the scene. */
+bc_status bc_scene_stats(const bc_context* ctx, int64_t* out, int n_out);
+
+/* ---- ray casting (closest hit / any hit) -------------------------------- */
+
+/*
+ * Closest hit for n rays, each 8 floats: (ox, oy, oz, tmin, dx, dy, dz, tmax).
+ * Semantics are those of Scene.Hit (renderer.go:777-849) evaluated in fp64 on
+ * the fp32 ray: prim_out[i] is the Scene primitive index of the nearest hit
+ * (-1 on a miss) and t_out[i] = float32(t_fp64) (-1 on a miss). Exact: the hit
+ * index equals the fp64 CPU path's; distinct primitives at bit-identical fp64
+ * distances resolve to the later slot in Scene.Order.
+ * Host pointers; copies in and out are part of the call.
+ */
+bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out, int32_t* prim_out);
+/* Same on device pointers, enqueued on `stream` (a cudaStream_t, NULL = legacy default); asynchronous. */
+bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, float* d_t_out, int32_t* d_prim_out,
+                            void* stream);
+/* Any hit (Scene.Occluded, renderer.go:851-895): occluded_out[i] = 1 if any primitive
+ * is hit within [tmin, tmax], fp64-exact like bc_raycast. */
+bc_status bc_occluded(bc_context* ctx, const float* rays, int64_t n, uint8_t* occluded_out);
+bc_status bc_occluded_device(bc_context* ctx, const float* d_rays, int64_t n, uint8_t* d_occluded_out, void* stream);
+
+/* ---- rendering ---------------------------------------------------------- */
+
+/*
+ * Render rows [y0, y0 + rows) of the frame; replaces one chunk iteration of
+ * renderOpenCL (gpu_opencl_windows.go:643-720). linear_out receives rows*width
+ * RGB float triples (the linear HDR mean per pixel, Start's jobLinear).
+ * guide_out (may be NULL) receives rows*width*3 uint32 in the reference's
+ * compact guide encoding (gpu_opencl_windows.go:519-521, 791-797): depth float
+ * bits; valid<<31 | material<<20 | octN.y<<10 | octN.x; jitter v<<16 | u.
+ * rays_out (may be NULL) receives the number of extension rays traced (the
+ * reference's Rays, renderer.go:1491).
+ */
+bc_status bc_render_rows(bc_context* ctx, const bc_camera* cam, const bc_settings* settings, int32_t y0,
+                         int32_t rows, float* linear_out, uint32_t* guide_out, int64_t* rays_out);
+
+/*
+ * Whole frame with the post stack of RenderState.Start on the device
+ * (renderer.go:2844-2854, 2890-2895): a-trous denoise when settings->denoise,
+ * bloom when settings->bloom > 0, then tone map to RGBA8. Any output pointer may be NULL.
+ * linear_out: width*height RGB floats after denoise and bloom; rgba_out: packed
+ * 0xff<<24 | b<<16 | g<<8 | r (toRGBA, renderer.go:2055-2064).
+ */
+bc_status bc_render_frame(bc_context* ctx, const bc_camera* cam, const bc_settings* settings, float* linear_out,
+                          uint32_t* guide_out, uint32_t* rgba_out, int64_t* rays_out);
+
+/* Request cancellation of the running or next render of ctx; safe from any thread. */
+bc_status bc_cancel(bc_context* ctx);
+/* Clear a pending cancellation. */
+bc_status bc_reset_cancel(bc_context* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BC_GX_H */

@@ -1,0 +1,187 @@
+// Test infrastructure only: the CPU oracle for the Beamcast GX path-tracing
+// hot path. It restates the portable Go renderer (windows_portable/renderer.go)
+// in C++17 fp64 with floating-point contraction disabled, so that each
+// expression rounds exactly like the Go code compiled for amd64.
+//
+// Only tests, the smoke check and the CPU-baseline leg of the benchmark use
+// this library; the product path never links or calls it.
+//
+// Parity pins: structural results (BVH node sets, escape tables, light PMF,
+// Halton tables, presets, AABB slab test, stack/stackless/any-hit agreement)
+// are checked against the reference's own unit tests (renderer_test.go).
+// Rendered radiance has no golden image in the reference, and its RNG is
+// time-seeded (renderer.go:2741), so image parity is statistical.
+#pragma once
+#include <cmath>
+#include <cstdint>
+#include <vector>
+#include <string>
+#include <atomic>
+
+namespace orc {
+
+struct V3 {
+  double x, y, z;
+};
+// renderer.go:23-39. Every helper keeps Go's left-to-right evaluation order.
+inline V3 v3(double x, double y, double z) { return V3{x, y, z}; }
+inline V3 add(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 sub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 mul(V3 a, double s) { return v3(a.x * s, a.y * s, a.z * s); }
+inline V3 had(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) {
+  return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+double len(V3 a);
+V3 unit(V3 a);
+inline double gmax(double a, double b) { return a > b ? a : (b > a ? b : (a == 0 && b == 0 ? (std::signbit(a) ? b : a) : a)); }
+inline double gmin(double a, double b) { return a < b ? a : (b < a ? b : (a == 0 && b == 0 ? (std::signbit(a) ? a : b) : a)); }
+inline double maxcomp(V3 a) { return gmax(a.x, gmax(a.y, a.z)); }
+inline double clampd(double x, double a, double b) { return x < a ? a : (x > b ? b : x); }
+inline double luminance(V3 c) { return 0.2126 * c.x + 0.7152 * c.y + 0.0722 * c.z; }  // renderer.go:2142
+
+struct Ray { V3 o, d; };
+struct RayAccel {  // renderer.go:52-81
+  Ray ray;
+  V3 inv{0, 0, 0};
+  double dirLen2 = 0, invDirLen2 = 0;
+  bool zx = false, zy = false, zz = false;
+};
+RayAccel prepare_ray(const Ray& r);
+
+struct AABB { V3 mn, mx; };
+AABB empty_aabb();
+AABB expand_point(AABB b, V3 p);
+AABB expand_box(AABB b, const AABB& c);
+double surface_area(const AABB& b);
+bool aabb_hit(const AABB& b, const RayAccel& r, double tmin, double tmax, double* near_out);
+
+enum MatKind { MatDiffuse = 0, MatMetal = 1, MatGlass = 2, MatEmissive = 3 };
+struct Material {
+  int kind = MatDiffuse;
+  V3 color{0, 0, 0};
+  double roughness = 0, ior = 0;
+  V3 emission{0, 0, 0};
+};
+enum PrimKind { PrimSphere = 0, PrimTriangle = 1 };
+struct Primitive {
+  int kind = PrimTriangle;
+  int material = 0;
+  V3 center{0, 0, 0};
+  double radius = 0;
+  V3 a{0, 0, 0}, b{0, 0, 0}, c{0, 0, 0}, e1{0, 0, 0}, e2{0, 0, 0}, normal{0, 0, 0};
+  AABB box;
+  V3 centroid{0, 0, 0};
+};
+struct Node { AABB box; int left = -1, right = -1, start = 0, count = 0; };
+struct Hit { double t = 0; V3 n{0, 0, 0}; int material = 0; int primitive = -1; bool front = false; };
+
+// Traversal counters feed the algorithmic-bytes model of the benchmark:
+// boxes = AABB.HitAccel calls, tris = triHit calls, spheres = sphere tests.
+struct Counters { int64_t boxes = 0, tris = 0, spheres = 0; };
+
+struct Scene {
+  std::vector<Material> materials;
+  std::vector<Primitive> prims;
+  std::vector<Node> nodes;
+  std::vector<int> order;
+  std::vector<int> light_spheres;
+  std::vector<double> light_cdf;
+  std::vector<double> light_pdf_by_prim;
+  std::string bvh_mode = "SAH";
+  int bvh_bins = 16, bvh_leaf = 4;
+  uint64_t topo_rev = 0, geom_rev = 0;
+
+  int add_material(const Material& m);
+  void add_sphere(V3 c, double r, int mat);
+  void add_triangle(V3 a, V3 b, V3 c, int mat);
+  void rebuild_light_distribution();
+  void build();
+  void refit();
+  int build_sah(int start, int end);
+  int build_median(int start, int end);
+  void node_bounds(int start, int end, AABB* box, AABB* cb) const;
+
+  bool hit(const Ray& r, double tmin, double tmax, Hit* out, Counters* c) const;
+  bool occluded(const Ray& r, double tmin, double tmax, Counters* c) const;
+  bool hit_threaded(const Ray& r, double tmin, double tmax, const std::vector<int32_t>& esc, Hit* out) const;
+  bool hit_recursive(int ni, const RayAccel& ar, double tmin, double tmax, Hit* out, Counters* c) const;
+  bool occluded_recursive(int ni, const RayAccel& ar, double tmin, double tmax, Counters* c) const;
+};
+
+std::vector<int32_t> threaded_escapes(const std::vector<Node>& nodes);
+bool prim_hit(const Primitive& p, const RayAccel& ar, double tmin, double tmax, Hit* h);
+bool prim_any_hit(const Primitive& p, const RayAccel& ar, double tmin, double tmax);
+
+struct Camera { V3 position, target, up; double fov; };
+void camera_basis(const Camera& c, double aspect, V3* origin, V3* lower, V3* horiz, V3* vert);
+
+enum Sampler { SamplerRandom = 0, SamplerHalton = 1, SamplerR2 = 2 };
+struct Settings {
+  int width = 320, height = 240, spp = 16, bounces = 5;
+  int msaa = 1, tsaa = 0;
+  int sampler = SamplerHalton;
+  bool mis = true, power_light = true;
+  double firefly_clamp = 0;
+  int rr_depth = 4;
+  bool adaptive = false;
+  double adaptive_threshold = 0.0006;
+  bool denoise = false;
+  int taa = 0, txaa = 0, bloom = 0, hdr = 2;
+  double exposure = 0, gamma = 2.2;
+  int tile = 8;
+};
+int effective_spp(const Settings& s);  // renderer.go:2395
+
+// PCG32 stream; the GPU kernels draw from the same generator so that a
+// common-random-number run can replay a path decision by decision.
+struct Rng {
+  uint64_t state = 0, inc = 1;
+  uint32_t next_u32();
+  double float64();  // 24-bit uniform in [0,1)
+  int intn(int n);
+};
+Rng make_path_rng(uint64_t seed, uint64_t pixel_key, uint64_t sample);
+
+V3 rand_in_unit_sphere(Rng& r);
+V3 rand_unit_vector(Rng& r);
+V3 rand_cos_hemisphere(V3 n, Rng& r);
+V3 reflect(V3 v, V3 n);
+V3 refract(V3 uv, V3 n, double eta);
+double schlick(double c, double ref);
+V3 background(V3 d);
+double power_heuristic(double a, double b);
+double light_selection_pdf(const Scene& s, int prim, bool power);
+double light_directional_pdf(const Scene& s, int prim, V3 from, V3 lp, V3 ln, bool power);
+double radical_inverse(uint64_t n, uint64_t base);
+double fractd(double x);
+void pixel_sample_rotation(int x, int y, double* rx, double* ry);
+void build_sample_sequence(const Settings& s, std::vector<double>* X, std::vector<double>* Y);
+V3 clamp_firefly(V3 c, double limit);
+std::vector<int> make_tile_order(int tx, int ty, const std::string& mode);
+
+struct Guide { V3 p{0, 0, 0}, n{0, 0, 0}, albedo{0, 0, 0}; double depth = 0; bool valid = false; };
+struct TraceStats { int64_t segments = 0, shadow = 0; Counters c; };
+
+V3 trace(const Scene& s, Ray ray, const Settings& st, Rng& rng, TraceStats* stats, Guide* guide);
+
+struct RenderOut {
+  std::vector<V3> linear;   // mean radiance per pixel
+  std::vector<V3> sumsq;    // per-channel mean of squared sample radiance
+  std::vector<Guide> guides;
+  int64_t segments = 0, shadow = 0;
+  Counters c;
+};
+// Tile-parallel render shaped like RenderState.Start's CPU path
+// (renderer.go:2692-2826): center-first tiles, one-tile atomic claims.
+void render(const Scene& s, const Camera& cam, const Settings& st, uint64_t seed, int threads,
+            RenderOut* out, const std::atomic<bool>* cancel);
+
+std::vector<V3> atrous_denoise(const std::vector<V3>& img, const std::vector<Guide>& g, int w, int h, int iters);
+std::vector<V3> box_blur(const std::vector<V3>& img, int w, int h, int radius);
+std::vector<V3> apply_bloom(const std::vector<V3>& img, int w, int h, int level);
+V3 tone_map_hdr(V3 c, int hdr);
+uint32_t to_rgba(V3 c, double exposure, double gamma, int hdr);
+
+}  // namespace orc

@@ -127,6 +127,30 @@ class Context:
                                     ptr(rgba, C.c_uint32), C.byref(rays)), self._h)
         return {"linear": lin, "guides": g, "rgba": rgba, "rays": rays.value}
 
+    def render_moments(self, cam: Camera, settings: RenderSettings):
+        """Per-pixel mean and mean of squares of the sample radiance (no post)."""
+        W, H = settings.width, settings.height
+        mean = np.empty((H, W, 3), dtype=np.float32)
+        msq = np.empty((H, W, 3), dtype=np.float32)
+        rays = C.c_int64(0)
+        cc, sc = cam.c(), settings.c()
+        check(lib().bc_render_moments(self._h, C.byref(cc), C.byref(sc), ptr(mean, C.c_float), ptr(msq, C.c_float),
+                                      C.byref(rays)), self._h)
+        return mean, msq, rays.value
+
+    def post_process(self, linear: np.ndarray, guide_nd: np.ndarray | None, settings: RenderSettings,
+                     want_rgba: bool = True):
+        """Denoise / bloom / tone map on caller buffers: linear (H, W, 3), guide_nd (H, W, 4)."""
+        H, W = linear.shape[:2]
+        lin = np.ascontiguousarray(linear, dtype=np.float32)
+        g = None if guide_nd is None else np.ascontiguousarray(guide_nd, dtype=np.float32)
+        out = np.empty((H, W, 3), dtype=np.float32)
+        rgba = np.empty((H, W), dtype=np.uint32) if want_rgba else None
+        sc = settings.c()
+        check(lib().bc_post_process(self._h, W, H, ptr(lin, C.c_float), ptr(g, C.c_float), C.byref(sc),
+                                    ptr(out, C.c_float), ptr(rgba, C.c_uint32)), self._h)
+        return out, rgba
+
     def cancel(self):
         lib().bc_cancel(self._h)
 

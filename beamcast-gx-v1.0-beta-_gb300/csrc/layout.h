@@ -56,9 +56,9 @@ static_assert(sizeof(MatGPU) == 48, "MatGPU must be 48 bytes");
 struct alignas(16) LightGPU {
   float cx, cy, cz, r;
   float er, eg, eb, select_pdf;
-  float cdf;
   int32_t prim;
-  int32_t pad[2];
+  int32_t pad;
+  double cdf;  // fp64, so the CDF search takes the CPU's branch for every draw
 };
 static_assert(sizeof(LightGPU) == 48, "LightGPU must be 48 bytes");
 

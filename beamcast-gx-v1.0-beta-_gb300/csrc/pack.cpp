@@ -44,6 +44,9 @@ bc_status validate(const bc_scene_desc& d, std::string* err) {
     return fail(err, "scene descriptor is missing primitive or node arrays");
   if (d.n_materials < 1 || !d.mat_kind || !d.mat_color || !d.mat_emission)
     return fail(err, "scene requires at least one material");
+  for (int32_t i = 0; i < d.n_materials; i++)
+    if (d.mat_kind[i] < BC_MAT_DIFFUSE || d.mat_kind[i] > BC_MAT_EMISSIVE)
+      return fail(err, "material " + std::to_string(i) + " has an unknown kind");
   bool any_sphere = false, any_tri = false;
   for (int32_t i = 0; i < d.n_prims; i++) {
     if (d.prim_kind[i] == BC_PRIM_SPHERE) any_sphere = true;
@@ -250,7 +253,8 @@ void pack_lights(const bc_scene_desc& d, PackedScene* ps) {
     double pdf = d.light_pdf_by_prim ? d.light_pdf_by_prim[p] : 0.0;
     if (pdf <= 0) pdf = 1.0 / (double)d.n_lights;  // chooseLight fallback, renderer.go:1389-1391
     L.select_pdf = (float)pdf;
-    L.cdf = (float)d.light_cdf[i];
+    L.cdf = d.light_cdf[i];
+    L.pad = 0;
     L.prim = p;
   }
 }

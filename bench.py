@@ -250,7 +250,10 @@ def run_gpu(args):
     value = ws * N_RAYS * args.steps / (total_ms / 1e3) / 1e6
     e2e_value = ws * N_RAYS / e2e_s / 1e6
     peak, peak_kind = _peaks()
-    cpu_v, cores, sample, bytes_per_ray, counters = cpu_baseline(spec, rays)
+    if args.no_cpu_baseline:
+        cpu_v, cores, sample, bytes_per_ray, counters = None, 0, "skipped", float("nan"), {}
+    else:
+        cpu_v, cores, sample, bytes_per_ray, counters = cpu_baseline(spec, rays)
     avg_ms = total_ms / args.steps
     achieved = bytes_per_ray * N_RAYS / (avg_ms / 1e3) / 1e9
     traffic = None
@@ -283,12 +286,17 @@ def run_gpu(args):
 
 
 def main():
+    global N_TRIS, N_RAYS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--tris", type=int, default=N_TRIS, help="smaller case for profiling")
+    ap.add_argument("--rays", type=int, default=N_RAYS, help="smaller case for profiling")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
     args = ap.parse_args()
+    N_TRIS, N_RAYS = args.tris, args.rays
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":

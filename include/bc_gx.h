@@ -191,6 +191,27 @@ bc_status bc_render_rows(bc_context* ctx, const bc_camera* cam, const bc_setting
 bc_status bc_render_frame(bc_context* ctx, const bc_camera* cam, const bc_settings* settings, float* linear_out,
                           uint32_t* guide_out, uint32_t* rgba_out, int64_t* rays_out);
 
+/*
+ * Convergence statistics of a frame without post: mean_out and meansq_out each
+ * receive width*height RGB floats, the per-pixel mean of the (firefly-clamped)
+ * sample radiance and the mean of its square. The per-pixel Monte Carlo
+ * standard error is sqrt((meansq - mean^2) / (spp - 1)). Same samples as
+ * bc_render_frame with the same settings.
+ */
+bc_status bc_render_moments(bc_context* ctx, const bc_camera* cam, const bc_settings* settings, float* mean_out,
+                            float* meansq_out, int64_t* rays_out);
+
+/*
+ * The post stack alone, on caller buffers (the part of RenderState.Start that
+ * follows the render call, renderer.go:2844-2854 and 2890-2895): a-trous denoise
+ * with `2 + min(3, max(taa, txaa))` passes when settings->denoise, bloom when
+ * settings->bloom > 0, tone map to RGBA8. linear_in: width*height RGB floats;
+ * guide_nd: width*height (nx, ny, nz, depth) floats with depth < 0 for pixels
+ * without a first hit (may be NULL when denoise is off). Outputs may be NULL.
+ */
+bc_status bc_post_process(bc_context* ctx, int32_t width, int32_t height, const float* linear_in,
+                          const float* guide_nd, const bc_settings* settings, float* linear_out, uint32_t* rgba_out);
+
 /* Request cancellation of the running or next render of ctx; safe from any thread. */
 bc_status bc_cancel(bc_context* ctx);
 /* Clear a pending cancellation. */

@@ -194,6 +194,32 @@ void orc_hit_batch_f32(void* sp, int64_t n, const float* rays8, double* t_out, i
     for (auto& c : per) { counters[0] += c.boxes; counters[1] += c.tris; counters[2] += c.spheres; }
   }
 }
+// Brute force over every primitive (small scenes): the number of primitives
+// whose fp64 test gives exactly the minimal distance, and up to `k` of them.
+// Distinct primitives at bit-identical distances are resolved by the
+// reference's traversal order, which this tie set makes visible to tests.
+void orc_tie_sets_f32(void* sp, int64_t n, const float* rays8, int k, int32_t* count_out, int32_t* members) {
+  Scene* s = (Scene*)sp;
+  parallel_for(n, 0, [&](int64_t a, int64_t b, int) {
+    for (int64_t i = a; i < b; i++) {
+      const float* r8 = rays8 + 8 * i;
+      RayAccel ar = prepare_ray(Ray{v3(r8[0], r8[1], r8[2]), v3(r8[4], r8[5], r8[6])});
+      double best = (double)r8[7];
+      int cnt = 0;
+      for (int p = 0; p < (int)s->prims.size(); p++) {
+        Hit h;
+        if (!prim_hit(s->prims[p], ar, (double)r8[3], (double)r8[7], &h)) continue;
+        if (h.t < best || cnt == 0) { best = h.t; cnt = 0; }
+        if (h.t == best) {
+          if (cnt < k) members[i * k + cnt] = p;
+          cnt++;
+        }
+      }
+      count_out[i] = cnt;
+    }
+  });
+}
+
 void orc_occluded_batch_f32(void* sp, int64_t n, const float* rays8, uint8_t* out, int64_t* counters, int threads) {
   Scene* s = (Scene*)sp;
   int T = threads < 1 ? (int)std::max(1u, std::thread::hardware_concurrency()) : threads;

@@ -43,6 +43,7 @@ _SIG = [
     ("orc_hit_batch", None, [C.c_void_p, C.c_int64, f64p, C.c_double, C.c_double, C.c_int, f64p, i32p, i64p, C.c_int]),
     ("orc_hit_batch_f32", None, [C.c_void_p, C.c_int64, f32p, f64p, i32p, i64p, C.c_int]),
     ("orc_occluded_batch_f32", None, [C.c_void_p, C.c_int64, f32p, u8p, i64p, C.c_int]),
+    ("orc_tie_sets_f32", None, [C.c_void_p, C.c_int64, f32p, C.c_int, i32p, i32p]),
     ("orc_occluded_batch", None, [C.c_void_p, C.c_int64, f64p, f64p, C.c_double, u8p, C.c_int]),
     ("orc_radical_inverse", C.c_double, [C.c_uint64, C.c_uint64]),
     ("orc_pixel_sample_rotation", None, [C.c_int, C.c_int, f64p]),
@@ -210,6 +211,14 @@ class OracleScene:
         lib().orc_hit_batch_f32(self.h, n, _p(r, C.c_float), _p(t, C.c_double), _p(p, C.c_int32), _p(cnt, C.c_int64),
                                 threads)
         return t, p, cnt
+
+    def tie_sets_f32(self, rays8, k=8):
+        """(count, members) of primitives at exactly the minimal fp64 distance (brute force)."""
+        r = np.ascontiguousarray(rays8, dtype=np.float32).reshape(-1, 8)
+        cnt = np.zeros(len(r), np.int32)
+        mem = np.full((len(r), k), -1, np.int32)
+        lib().orc_tie_sets_f32(self.h, len(r), _p(r, C.c_float), k, _p(cnt, C.c_int32), _p(mem, C.c_int32))
+        return cnt, mem
 
     def occluded_f32(self, rays8, threads=0):
         r = np.ascontiguousarray(rays8, dtype=np.float32).reshape(-1, 8)

@@ -11,15 +11,26 @@ pytestmark = pytest.mark.gpu
 
 
 def _ulp_diff(a, b):
-    ai = a.astype(np.float32).view(np.int32).astype(np.int64)
-    bi = b.astype(np.float32).view(np.int32).astype(np.int64)
-    return np.abs(ai - bi)
+    """Distance in units in the last place, on the ordered-integer line (+0 == -0)."""
+    def ordered(x):
+        i = x.astype(np.float32).view(np.int32).astype(np.int64)
+        return np.where(i < 0, -(i & 0x7FFFFFFF), i)
+    return np.abs(ordered(a) - ordered(b))
 
 
-def _check(ctx, orc_scene, rays, max_ulp=0):
+def _check(ctx, orc_scene, rays, max_ulp=0, allow_ties=False):
+    """Bit-exact hit index; with allow_ties, rays whose minimal fp64 distance is
+    shared by several primitives (coplanar faces, t == +0 == -0) may return any
+    member of that exact tie set: the reference keeps the one its binary
+    traversal visits last, the GPU keeps the later Order slot."""
     t_gpu, p_gpu = ctx.raycast(rays)
     t_ref, p_ref, _ = orc_scene.hit_f32(rays)
     mism = np.nonzero(p_gpu != p_ref)[0]
+    if allow_ties and len(mism):
+        cnt, mem = orc_scene.tie_sets_f32(rays[mism])
+        ok = (cnt >= 2) & np.any(mem == p_gpu[mism][:, None], axis=1)
+        assert np.all(t_gpu[mism] == t_ref[mism].astype(np.float32))
+        mism = mism[~ok]
     assert len(mism) == 0, f"{len(mism)} hit-index mismatches, first {mism[:5]}: gpu {p_gpu[mism[:5]]} ref {p_ref[mism[:5]]}"
     hit = p_ref >= 0
     assert np.all(t_gpu[~hit] == -1.0)
@@ -114,7 +125,7 @@ def test_edge_rays(gpu_ctx, orc):
         tmax = 1e30 if rng.random() < 0.7 else rng.uniform(0.01, 2)
         rays.append([o[0], o[1], o[2], tmin, d[0], d[1], d[2], tmax])
     rays = np.array(rays, np.float32)
-    _check(gpu_ctx, ref, rays)
+    _check(gpu_ctx, ref, rays, allow_ties=True)
     odd = np.array([[0, 0, 0, 1e-4, 0, 0, 0, 1e30], [0.1, 0.2, 0.3, 1e-4, np.nan, 1, 0, 1e30],
                     [0, 0, 0, 1e-4, 1, 0, 0, np.nan]], np.float32)
     t, p = gpu_ctx.raycast(odd)

@@ -151,6 +151,14 @@ class Context:
                                     ptr(out, C.c_float), ptr(rgba, C.c_uint32)), self._h)
         return out, rgba
 
+    def set_option(self, name: str, value: int):
+        check(lib().bc_set_option(self._h, name.encode(), int(value)), self._h)
+
+    def get_option(self, name: str) -> int:
+        v = C.c_int64(0)
+        check(lib().bc_get_option(self._h, name.encode(), C.byref(v)), self._h)
+        return v.value
+
     def cancel(self):
         lib().bc_cancel(self._h)
 

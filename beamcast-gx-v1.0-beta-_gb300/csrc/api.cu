@@ -37,6 +37,7 @@ bc_status check_kernel_status(bc_context* ctx) {
     return set_error(ctx, BC_ERR_CAPACITY, "traversal stack overflow (scene deeper than the compiled stack)");
   if (h & kStatusTimeout) return set_error(ctx, BC_ERR_TIMEOUT, "a bounded device wait gave up");
   if (h & kStatusCapacity) return set_error(ctx, BC_ERR_CAPACITY, "a device queue exceeded its capacity");
+  if (h & kStatusBound) return set_error(ctx, BC_ERR_DEVICE, "fp32 error bound violated by an fp64 re-test");
   return set_error(ctx, BC_ERR_DEVICE, "unknown kernel status");
 }
 
@@ -222,7 +223,7 @@ bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, flo
   if (((uintptr_t)d_rays & 15u) != 0) return set_error(ctx, BC_ERR_INVALID_ARG, "rays must be 16-byte aligned");
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-  cudaError_t e = launch_raycast_closest(ctx->ds, (const float4*)d_rays, n, d_t_out, d_prim_out, ctx->d_status, 128, st);
+  cudaError_t e = launch_raycast_closest(ctx->ds, (const float4*)d_rays, n, d_t_out, d_prim_out, ctx->d_status, ctx->raycast_variant, st);
   return cuda_status(ctx, e, "ray-cast launch");
 }
 
@@ -239,7 +240,7 @@ bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out
   e = cudaMemcpyAsync(ctx->d_rays.p, rays, (size_t)n * 32, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess)
     e = launch_raycast_closest(ctx->ds, ctx->d_rays.as<float4>(), n, ctx->d_t.as<float>(), ctx->d_prim.as<int32_t>(),
-                               ctx->d_status, 128, ctx->stream);
+                               ctx->d_status, ctx->raycast_variant, ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(t_out, ctx->d_t.p, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(prim_out, ctx->d_prim.p, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -253,7 +254,7 @@ bc_status bc_occluded_device(bc_context* ctx, const float* d_rays, int64_t n, ui
   if (((uintptr_t)d_rays & 15u) != 0) return set_error(ctx, BC_ERR_INVALID_ARG, "rays must be 16-byte aligned");
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-  cudaError_t e = launch_raycast_any(ctx->ds, (const float4*)d_rays, n, d_out, ctx->d_status, 128, st);
+  cudaError_t e = launch_raycast_any(ctx->ds, (const float4*)d_rays, n, d_out, ctx->d_status, ctx->raycast_variant, st);
   return cuda_status(ctx, e, "any-hit launch");
 }
 
@@ -268,12 +269,39 @@ bc_status bc_occluded(bc_context* ctx, const float* rays, int64_t n, uint8_t* ou
     return cuda_status(ctx, e, "any-hit buffers");
   e = cudaMemcpyAsync(ctx->d_rays.p, rays, (size_t)n * 32, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess)
-    e = launch_raycast_any(ctx->ds, ctx->d_rays.as<float4>(), n, ctx->d_occ.as<uint8_t>(), ctx->d_status, 128,
+    e = launch_raycast_any(ctx->ds, ctx->d_rays.as<float4>(), n, ctx->d_occ.as<uint8_t>(), ctx->d_status, ctx->raycast_variant,
                            ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, ctx->d_occ.p, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_status(ctx, e, "any hit");
   return check_kernel_status(ctx);
+}
+
+bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
+  if (!ctx || !name) return set_error(ctx, BC_ERR_INVALID_ARG, "NULL argument");
+  const std::string n(name);
+  if (n == "raycast_minblocks") {
+    if (value != 1 && value != 6 && value != 8)
+      return set_error(ctx, BC_ERR_INVALID_ARG, "raycast_minblocks must be 1, 6 or 8");
+    ctx->raycast_minblocks = (int)value;
+    ctx->raycast_variant = ctx->raycast_exact ? (int)value : 0;
+    return BC_OK;
+  }
+  if (n == "raycast_exact") {
+    if (value != 0 && value != 1) return set_error(ctx, BC_ERR_INVALID_ARG, "raycast_exact must be 0 or 1");
+    ctx->raycast_exact = (int)value;
+    ctx->raycast_variant = value ? ctx->raycast_minblocks : 0;
+    return BC_OK;
+  }
+  return set_error(ctx, BC_ERR_INVALID_ARG, "unknown option " + n);
+}
+
+bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value) {
+  if (!ctx || !name || !value) return BC_ERR_INVALID_ARG;
+  const std::string n(name);
+  if (n == "raycast_minblocks") { *value = ctx->raycast_minblocks; return BC_OK; }
+  if (n == "raycast_exact") { *value = ctx->raycast_exact; return BC_OK; }
+  return BC_ERR_INVALID_ARG;
 }
 
 bc_status bc_cancel(bc_context* ctx) {

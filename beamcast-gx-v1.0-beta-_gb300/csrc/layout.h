@@ -29,6 +29,7 @@ constexpr int32_t kMaxIndex = 1 << 27;
 constexpr unsigned kStatusStackOverflow = 1u;
 constexpr unsigned kStatusTimeout = 2u;
 constexpr unsigned kStatusCapacity = 4u;
+constexpr unsigned kStatusBound = 8u;  // an fp32 hit classified as certain failed its fp64 test
 
 struct alignas(64) Node8 {
   float lox[8], hix[8], loy[8], hiy[8], loz[8], hiz[8];

@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(128) k_extend(SceneView sv, PathSoA ps, const 
     if (idx < n) {
       const int path = queue[idx];
       const Ray32 r = make_ray(ps.ox[path], ps.oy[path], ps.oz[path], ps.dx[path], ps.dy[path], ps.dz[path], 1e-4f);
-      const HitResult h = closest_hit<STACK, false, SPH>(sv, r, 1e30f, 1e30, status);
+      const HitResult h = closest_hit_fast<STACK, SPH>(sv, r, 1e30f, status);
       ps.hit_t[path] = h.t32;
       ps.hit_slot[path] = h.slot;
     }
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(128) k_connect(SceneView sv, PathSoA ps, Shado
     if (i < n) {
       const float4 o = sh.o[i], d = sh.d[i];
       const Ray32 r = make_ray(o.x, o.y, o.z, d.x, d.y, d.z, 1e-4f);
-      if (!any_hit<STACK, false, SPH>(sv, r, o.w, (double)o.w, status)) {
+      if (!any_hit_fast<STACK, SPH>(sv, r, o.w, status)) {
         const int path = sh.path[i];
         const float4 c = sh.c[i];
         ps.lx[path] += c.x;

@@ -120,7 +120,7 @@ __device__ __forceinline__ D3 dsub3(D3 a, D3 b) { return D3{ds(a.x, b.x), ds(a.y
 
 // triHit / triAnyHit (renderer.go:684-711, 744-763): returns true and t when
 // tmin <= t <= tmax.
-__device__ __forceinline__ bool tri_hit64(const double* __restrict__ q, D3 o, D3 d, double tmin, double tmax,
+static __device__ __noinline__ bool tri_hit64(const double* __restrict__ q, D3 o, D3 d, double tmin, double tmax,
                                           double* t_out) {
   const D3 a{__ldg(q + 0), __ldg(q + 1), __ldg(q + 2)};
   const D3 e1{__ldg(q + 3), __ldg(q + 4), __ldg(q + 5)};
@@ -143,7 +143,7 @@ __device__ __forceinline__ bool tri_hit64(const double* __restrict__ q, D3 o, D3
 
 // sphereHitAccel / sphereAnyHitAccel (renderer.go:650-678, 724-742).
 // `closest` selects the near root first, then the far root, as the reference does.
-__device__ __forceinline__ bool sphere_hit64(const double* __restrict__ q, D3 o, D3 d, double tmin, double tmax,
+static __device__ __noinline__ bool sphere_hit64(const double* __restrict__ q, D3 o, D3 d, double tmin, double tmax,
                                              double* t_out) {
   const double dl2 = ddot(d, d);
   if (!(dl2 > 1e-18)) return false;
@@ -165,12 +165,28 @@ __device__ __forceinline__ bool sphere_hit64(const double* __restrict__ q, D3 o,
   return true;
 }
 
-// fp32 Moller-Trumbore used as a filter: returns false only when the fp64
-// test of the same triangle is certain to reject it. The error bounds are
-// first-order forward bounds of each quantity against the exact result on
-// the fp64 inputs (the fp32 record holds those inputs rounded to nearest),
-// with at least a factor 2 of slack; R = max|A| + max|O-A|.
-__device__ __forceinline__ bool tri_candidate(float4 A, float4 E1, float4 E2, const Ray32& r, float tlim) {
+// fp32 Moller-Trumbore with forward error bounds, classifying a triangle
+// against the fp64 test of the same triangle (triHit, renderer.go:684-711):
+//   kMiss  - the fp64 test certainly rejects it,
+//   kHit   - the fp64 test certainly accepts it, and its fp64 distance lies in
+//            [t - et, t + et],
+//   kMaybe - undecided; only the fp64 test can tell.
+// The bounds are first-order forward bounds of each quantity against the
+// exact result on the fp64 inputs (the fp32 record holds those inputs rounded
+// to nearest), with at least a factor 2 of slack; R = max|A| + max|O - A|.
+constexpr int kMiss = 0, kHit = 1, kMaybe = 2;
+
+struct TriClass {
+  int state;
+  float t, et;
+};
+
+__device__ __forceinline__ TriClass tri_classify(float4 A, float4 E1, float4 E2, const Ray32& r, float tmax_ray,
+                                                 float tlim) {
+  TriClass c;
+  c.state = kMiss;
+  c.t = 0.0f;
+  c.et = 0.0f;
   const float hx = r.dy * E2.z - r.dz * E2.y;
   const float hy = r.dz * E2.x - r.dx * E2.z;
   const float hz = r.dx * E2.y - r.dy * E2.x;
@@ -178,25 +194,35 @@ __device__ __forceinline__ bool tri_candidate(float4 A, float4 E1, float4 E2, co
   const float Mh = r.dmax * E2.w;
   const float errDet = 96.0f * kU * E1.w * Mh;
   const float adet = fabsf(det);
-  if (adet + errDet < 1e-10f) return false;
-  if (adet <= 2.0f * errDet || adet - errDet < 1e-10f) return true;  // cannot bound: re-test in fp64
+  if (adet + errDet < 1e-10f) return c;
   const float sx = r.ox - A.x, sy = r.oy - A.y, sz = r.oz - A.z;
+  if (adet <= 2.0f * errDet || adet - errDet < 1e-10f) {  // cannot bound u, v, t
+    c.state = kMaybe;
+    c.et = __int_as_float(0x7f800000);
+    return c;
+  }
   const float R = A.w + fmaxf(fabsf(sx), fmaxf(fabsf(sy), fabsf(sz)));
   const float invd = 1.0f / (adet - errDet);
   const float f = 1.0f / det;
   const float u = f * (sx * hx + sy * hy + sz * hz);
   const float eu = (96.0f * kU * R * Mh + fabsf(u) * errDet) * invd + 4.0f * kU * fabsf(u);
-  if (u < -eu || u > 1.0f + eu) return false;
+  if (u < -eu || u > 1.0f + eu) return c;
   const float qx = sy * E1.z - sz * E1.y;
   const float qy = sz * E1.x - sx * E1.z;
   const float qz = sx * E1.y - sy * E1.x;
   const float v = f * (r.dx * qx + r.dy * qy + r.dz * qz);
   const float ev = (96.0f * kU * r.dmax * R * E1.w + fabsf(v) * errDet) * invd + 4.0f * kU * fabsf(v);
-  if (v < -ev || u + v > 1.0f + eu + ev + 4.0f * kU * fabsf(u + v)) return false;
+  const float euv = eu + ev + 4.0f * kU * fabsf(u + v);
+  if (v < -ev || u + v > 1.0f + euv) return c;
   const float t = f * (E2.x * qx + E2.y * qy + E2.z * qz);
   const float et = (112.0f * kU * E2.w * R * E1.w + fabsf(t) * errDet) * invd + 4.0f * kU * fabsf(t);
-  if (t + et < r.tmin || t - et > tlim) return false;
-  return true;
+  if (t + et < r.tmin || t - et > tlim) return c;
+  c.t = t;
+  c.et = et;
+  const bool sure = u >= eu && u <= 1.0f - eu && v >= ev && u + v <= 1.0f - euv && t - et >= r.tmin &&
+                    t + et <= tmax_ray;
+  c.state = sure ? kHit : kMaybe;
+  return c;
 }
 
 // Plain fp32 triangle test for rendering (reference thresholds).
@@ -255,150 +281,343 @@ struct HitResult {
   double t64;     // exact mode distance
 };
 
-// Closest hit. STACK >= the packer's stack_need; an overflow sets a status bit.
-template <int STACK, bool EXACT, bool SPHERES>
-__device__ __forceinline__ HitResult closest_hit(const SceneView& sv, const Ray32& r, float tmax32, double tmax64,
-                                                 unsigned* status) {
+constexpr uint32_t kEnd = 0x7fffffffu;  // "no node": bit 31 clear and above any node index
+
+// While-while BVH8 walk (Aila and Laine, "Understanding the Efficiency of Ray
+// Traversal on GPUs", HPG 2009): a lane descends inner nodes, postponing the
+// first leaf it reaches, until every active lane of the warp holds a leaf;
+// then leaves are tested in their own loop. Hit children are visited
+// near-first (sorting network) and culled against leaf.tlim when popped.
+// `Leaf` provides `float tlim`, `bool done` and `void operator()(uint32_t leaf_ref)`.
+template <int STACK, class Leaf>
+__device__ __forceinline__ void walk(const SceneView& sv, const Ray32& r, Leaf& leaf, unsigned* status) {
   uint2 st[STACK];
   int sp = 0;
-  HitResult res;
-  res.slot = -1;
-  res.t32 = tmax32;
-  res.t64 = tmax64;
-  float tlim = widen(tmax32);
-  const D3 o64{(double)r.ox, (double)r.oy, (double)r.oz};
-  const D3 d64{(double)r.dx, (double)r.dy, (double)r.dz};
-  const double tmin64 = (double)r.tmin;
-  uint32_t ref = 0;  // root Node8
+  uint32_t ref = 0;      // root Node8
+  uint32_t pending = 0;  // postponed leaf ref, 0 = none
   for (;;) {
-    if (!(ref & kLeafBit)) {
+    while (ref != kEnd && !(ref & kLeafBit)) {
       float nr[8];
       uint32_t ch[8];
-      node_children(sv.nodes + ref, r, tlim, nr, ch);
+      node_children(sv.nodes + ref, r, leaf.tlim, nr, ch);
       sort8(nr, ch);
-      if (nr[0] == __int_as_float(0x7f800000)) goto pop;
+      if (nr[0] == __int_as_float(0x7f800000)) {
+        ref = kEnd;
+        while (sp > 0) {
+          const uint2 e = st[--sp];
+          if (__uint_as_float(e.y) <= leaf.tlim) { ref = e.x; break; }
+        }
+      } else {
 #pragma unroll
-      for (int k = 7; k >= 1; k--) {
-        if (nr[k] != __int_as_float(0x7f800000)) {
-          if (sp < STACK) {
-            st[sp++] = make_uint2(ch[k], __float_as_uint(nr[k]));
-          } else {
-            atomicOr(status, kStatusStackOverflow);
+        for (int k = 7; k >= 1; k--) {
+          if (nr[k] != __int_as_float(0x7f800000)) {
+            if (sp < STACK) st[sp++] = make_uint2(ch[k], __float_as_uint(nr[k]));
+            else atomicOr(status, kStatusStackOverflow);
           }
+        }
+        ref = ch[0];
+      }
+      if (ref != kEnd && (ref & kLeafBit)) {
+        if (pending != 0) break;
+        pending = ref;
+        ref = kEnd;
+        while (sp > 0) {
+          const uint2 e = st[--sp];
+          if (__uint_as_float(e.y) <= leaf.tlim) { ref = e.x; break; }
         }
       }
-      ref = ch[0];
-      continue;
-    } else {
-      const int cnt = (int)((ref >> 27) & 15u) + 1;
-      const int s0 = (int)(ref & kSlotMask);
-      for (int k = 0; k < cnt; k++) {
-        const int s = s0 + k;
-        const float4 A = __ldg(sv.tri + 3 * s);
-        const float4 E1 = __ldg(sv.tri + 3 * s + 1);
-        const float4 E2 = __ldg(sv.tri + 3 * s + 2);
-        if (SPHERES && E2.w < 0.0f) {
-          if (EXACT) {
-            double t;
-            if (sphere_hit64(sv.slot64 + 9 * (size_t)s, o64, d64, tmin64, res.t64, &t) &&
-                (t < res.t64 || s > res.slot)) {
-              res.t64 = t; res.slot = s; tlim = widen(__double2float_ru(t));
-            }
-          } else {
-            float t;
-            if (sphere_hit32(A, E1, r, res.t32, &t)) { res.t32 = t; res.slot = s; tlim = widen(t); }
-          }
-          continue;
-        }
-        if (EXACT) {
-          if (!tri_candidate(A, E1, E2, r, tlim)) continue;
-          double t;
-          if (tri_hit64(sv.slot64 + 9 * (size_t)s, o64, d64, tmin64, res.t64, &t) && (t < res.t64 || s > res.slot)) {
-            res.t64 = t; res.slot = s; tlim = widen(__double2float_ru(t));
-          }
-        } else {
-          float t;
-          if (tri_hit32(A, E1, E2, r, res.t32, &t)) { res.t32 = t; res.slot = s; tlim = widen(t); }
+      if (__all_sync(__activemask(), pending != 0)) break;
+    }
+    while (pending != 0) {
+      leaf(pending);
+      if (leaf.done) return;
+      pending = 0;
+      if (ref != kEnd && (ref & kLeafBit)) {
+        pending = ref;
+        ref = kEnd;
+        while (sp > 0) {
+          const uint2 e = st[--sp];
+          if (__uint_as_float(e.y) <= leaf.tlim) { ref = e.x; break; }
         }
       }
     }
-  pop:
-    for (;;) {
-      if (sp == 0) return res;
-      const uint2 e = st[--sp];
-      if (__uint_as_float(e.y) <= tlim) {
-        ref = e.x;
-        break;
-      }
-    }
+    if (ref == kEnd) return;
   }
 }
 
-// Any hit within [tmin, tmax] (Scene.Occluded semantics). Children are pushed
-// unsorted; the first confirmed hit ends the walk.
-template <int STACK, bool EXACT, bool SPHERES>
-__device__ __forceinline__ bool any_hit(const SceneView& sv, const Ray32& r, float tmax32, double tmax64,
-                                        unsigned* status) {
-  uint32_t st[STACK];
-  int sp = 0;
-  const float tlim = widen(tmax32);
-  const D3 o64{(double)r.ox, (double)r.oy, (double)r.oz};
-  const D3 d64{(double)r.dx, (double)r.dy, (double)r.dz};
-  const double tmin64 = (double)r.tmin;
-  uint32_t ref = 0;
-  for (;;) {
-    if (!(ref & kLeafBit)) {
-      float nr[8];
-      uint32_t ch[8];
-      node_children(sv.nodes + ref, r, tlim, nr, ch);
-      int first = -1;
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        if (nr[k] != __int_as_float(0x7f800000)) {
-          if (first < 0) {
-            first = k;
-          } else if (sp < STACK) {
-            st[sp++] = ch[k];
-          } else {
-            atomicOr(status, kStatusStackOverflow);
-          }
-        }
-      }
-      if (first >= 0) {
-        ref = ch[first];
-        continue;
-      }
-    } else {
-      const int cnt = (int)((ref >> 27) & 15u) + 1;
-      const int s0 = (int)(ref & kSlotMask);
-      for (int k = 0; k < cnt; k++) {
-        const int s = s0 + k;
-        const float4 A = __ldg(sv.tri + 3 * s);
-        const float4 E1 = __ldg(sv.tri + 3 * s + 1);
-        const float4 E2 = __ldg(sv.tri + 3 * s + 2);
-        if (SPHERES && E2.w < 0.0f) {
-          if (EXACT) {
-            double t;
-            if (sphere_hit64(sv.slot64 + 9 * (size_t)s, o64, d64, tmin64, tmax64, &t)) return true;
-          } else {
-            float t;
-            if (sphere_hit32(A, E1, r, tmax32, &t)) return true;
-          }
-          continue;
-        }
-        if (EXACT) {
-          double t;
-          if (tri_candidate(A, E1, E2, r, tlim) && tri_hit64(sv.slot64 + 9 * (size_t)s, o64, d64, tmin64, tmax64, &t))
-            return true;
-        } else {
-          float t;
-          if (tri_hit32(A, E1, E2, r, tmax32, &t)) return true;
-        }
+// ---- exact closest hit -------------------------------------------------------
+// Candidates carry an fp32 interval [lo, hi] that holds their fp64 distance.
+// `best` is the certain hit with the smallest upper bound; candidates that
+// might still beat it (undecided ones, or certain ones whose interval overlaps
+// best's) wait in a short per-thread list. After the walk the warp is
+// re-converged and every remaining contender is settled in fp64 together, so
+// the slow fp64 pipe runs with all lanes active instead of one lane at a time.
+struct Contender {
+  int32_t slot;
+  float lo, hi;
+  double t64;
+  bool exact;
+};
+
+constexpr int kPending = 4;
+
+template <bool SPHERES>
+struct ExactClosestLeaf {
+  const SceneView& sv;
+  const Ray32& r;
+  unsigned* status;
+  float tmax_ray;
+  float tlim;
+  bool done;
+  Contender best;
+  int npend;
+  Contender pend[kPending];
+
+  __device__ ExactClosestLeaf(const SceneView& s, const Ray32& ray, float tmax, unsigned* st)
+      : sv(s), r(ray), status(st), tmax_ray(tmax), tlim(widen(tmax)), done(false), npend(0) {
+    best.slot = -1;
+    best.lo = tmax;
+    best.hi = tmax;
+    best.t64 = 0.0;
+    best.exact = false;
+  }
+  // fp64 distance of a contender (triHit in the reference's operation order).
+  __device__ __forceinline__ bool resolve(Contender& c) {
+    if (c.exact) return true;
+    double t;
+    const D3 o{(double)r.ox, (double)r.oy, (double)r.oz}, d{(double)r.dx, (double)r.dy, (double)r.dz};
+    if (!tri_hit64(sv.slot64 + 9 * (size_t)c.slot, o, d, (double)r.tmin, (double)tmax_ray, &t)) return false;
+    c.t64 = t;
+    c.lo = __double2float_rd(t);
+    c.hi = __double2float_ru(t);
+    c.exact = true;
+    return true;
+  }
+  // c is exact and valid: compare with best now (no deferral, no recursion).
+  __device__ __forceinline__ void settle_against_best(const Contender& c) {
+    if (best.slot < 0 || c.hi < best.lo) {
+      best = c;
+    } else if (c.lo <= best.hi) {
+      if (!resolve(best)) {
+        atomicOr(status, kStatusBound);  // a certain hit must pass its fp64 test
+        best = c;
+      } else if (c.t64 < best.t64 || (c.t64 == best.t64 && c.slot > best.slot)) {
+        best = c;
       }
     }
-    if (sp == 0) return false;
-    ref = st[--sp];
+    tlim = widen(best.hi);
   }
+  // c may hit and may beat best: keep it for the converged settlement, or
+  // settle it now when the list is full.
+  __device__ __forceinline__ void defer_maybe(Contender c) {
+    if (npend < kPending) {
+      pend[npend++] = c;
+      return;
+    }
+    if (resolve(c)) settle_against_best(c);
+  }
+  // c certainly hits; best keeps the smallest upper bound, an overlapping
+  // loser waits in the list (or both are settled now when it is full).
+  __device__ __forceinline__ void take_certain(Contender c) {
+    if (best.slot < 0 || c.hi < best.lo) {
+      best = c;
+    } else if (c.lo > best.hi) {
+      return;
+    } else if (npend < kPending) {
+      if (c.hi < best.hi) {
+        pend[npend++] = best;
+        best = c;
+      } else {
+        pend[npend++] = c;
+      }
+    } else {
+      if (!resolve(c)) {
+        atomicOr(status, kStatusBound);
+        return;
+      }
+      settle_against_best(c);
+      return;
+    }
+    tlim = widen(best.hi);
+  }
+  __device__ __forceinline__ void operator()(uint32_t ref) {
+    const int cnt = (int)((ref >> 27) & 15u) + 1;
+    const int s0 = (int)(ref & kSlotMask);
+    for (int k = 0; k < cnt; k++) {
+      const int s = s0 + k;
+      const float4 A = __ldg(sv.tri + 3 * s);
+      const float4 E1 = __ldg(sv.tri + 3 * s + 1);
+      const float4 E2 = __ldg(sv.tri + 3 * s + 2);
+      Contender c;
+      c.slot = s;
+      c.exact = false;
+      c.t64 = 0.0;
+      if (SPHERES && E2.w < 0.0f) {  // spheres are rare: settle in fp64 at once
+        double t;
+        const D3 o{(double)r.ox, (double)r.oy, (double)r.oz}, d{(double)r.dx, (double)r.dy, (double)r.dz};
+        if (!sphere_hit64(sv.slot64 + 9 * (size_t)s, o, d, (double)r.tmin, (double)tmax_ray, &t)) continue;
+        c.t64 = t;
+        c.lo = __double2float_rd(t);
+        c.hi = __double2float_ru(t);
+        c.exact = true;
+        take_certain(c);
+        continue;
+      }
+      const TriClass tc = tri_classify(A, E1, E2, r, tmax_ray, tlim);
+      if (tc.state == kMiss) continue;
+      c.lo = __fsub_rd(tc.t, tc.et);
+      c.hi = __fadd_ru(tc.t, tc.et);
+      if (best.slot >= 0 && c.lo > best.hi) continue;
+      if (tc.state == kHit) take_certain(c);
+      else defer_maybe(c);
+    }
+  }
+  // After the walk, warp converged: settle best and every pending contender
+  // that can still win; the smallest fp64 distance wins, ties to the later slot.
+  __device__ __forceinline__ void finish() {
+    Contender win;
+    win.slot = -1;
+    win.t64 = 0.0;
+    if (best.slot >= 0) {
+      if (resolve(best)) win = best;
+      else atomicOr(status, kStatusBound);  // a certain hit must pass its fp64 test
+    }
+#pragma unroll
+    for (int k = 0; k < kPending; k++) {
+      if (k < npend && !(best.slot >= 0 && pend[k].lo > best.hi)) {
+        Contender c = pend[k];
+        if (resolve(c) &&
+            (win.slot < 0 || c.t64 < win.t64 || (c.t64 == win.t64 && c.slot > win.slot)))
+          win = c;
+      }
+    }
+    best = win;
+  }
+};
+
+template <int STACK, bool SPHERES>
+__device__ __forceinline__ HitResult closest_hit_exact(const SceneView& sv, const Ray32& r, float tmax32,
+                                                       unsigned* status, bool active) {
+  ExactClosestLeaf<SPHERES> leaf(sv, r, tmax32, status);
+  if (active) walk<STACK>(sv, r, leaf, status);
+  __syncwarp();
+  if (active) leaf.finish();
+  HitResult h;
+  h.slot = active ? leaf.best.slot : -1;
+  h.t32 = 0.0f;
+  h.t64 = h.slot >= 0 ? leaf.best.t64 : -1.0;
+  return h;
+}
+
+// ---- exact any hit --------------------------------------------------------------
+template <bool SPHERES>
+struct ExactAnyLeaf {
+  const SceneView& sv;
+  const Ray32& r;
+  float tmax_ray;
+  float tlim;
+  bool done;
+  __device__ ExactAnyLeaf(const SceneView& s, const Ray32& ray, float tmax)
+      : sv(s), r(ray), tmax_ray(tmax), tlim(widen(tmax)), done(false) {}
+  __device__ __forceinline__ void operator()(uint32_t ref) {
+    const int cnt = (int)((ref >> 27) & 15u) + 1;
+    const int s0 = (int)(ref & kSlotMask);
+    const D3 o{(double)r.ox, (double)r.oy, (double)r.oz}, d{(double)r.dx, (double)r.dy, (double)r.dz};
+    for (int k = 0; k < cnt && !done; k++) {
+      const int s = s0 + k;
+      const float4 A = __ldg(sv.tri + 3 * s);
+      const float4 E1 = __ldg(sv.tri + 3 * s + 1);
+      const float4 E2 = __ldg(sv.tri + 3 * s + 2);
+      double t;
+      if (SPHERES && E2.w < 0.0f) {
+        done = sphere_hit64(sv.slot64 + 9 * (size_t)s, o, d, (double)r.tmin, (double)tmax_ray, &t);
+        continue;
+      }
+      const TriClass tc = tri_classify(A, E1, E2, r, tmax_ray, tlim);
+      if (tc.state == kHit) done = true;
+      else if (tc.state == kMaybe)
+        done = tri_hit64(sv.slot64 + 9 * (size_t)s, o, d, (double)r.tmin, (double)tmax_ray, &t);
+    }
+  }
+};
+
+template <int STACK, bool SPHERES>
+__device__ __forceinline__ bool any_hit_exact(const SceneView& sv, const Ray32& r, float tmax32, unsigned* status) {
+  ExactAnyLeaf<SPHERES> leaf(sv, r, tmax32);
+  walk<STACK>(sv, r, leaf, status);
+  return leaf.done;
+}
+
+// ---- fast (rendering) closest / any hit -------------------------------------------
+template <bool SPHERES>
+struct FastClosestLeaf {
+  const SceneView& sv;
+  const Ray32& r;
+  float best_t;
+  int32_t best_slot;
+  float tlim;
+  bool done;
+  __device__ FastClosestLeaf(const SceneView& s, const Ray32& ray, float tmax)
+      : sv(s), r(ray), best_t(tmax), best_slot(-1), tlim(widen(tmax)), done(false) {}
+  __device__ __forceinline__ void operator()(uint32_t ref) {
+    const int cnt = (int)((ref >> 27) & 15u) + 1;
+    const int s0 = (int)(ref & kSlotMask);
+    for (int k = 0; k < cnt; k++) {
+      const int s = s0 + k;
+      const float4 A = __ldg(sv.tri + 3 * s);
+      const float4 E1 = __ldg(sv.tri + 3 * s + 1);
+      const float4 E2 = __ldg(sv.tri + 3 * s + 2);
+      float t;
+      const bool hit = (SPHERES && E2.w < 0.0f) ? sphere_hit32(A, E1, r, best_t, &t) : tri_hit32(A, E1, E2, r, best_t, &t);
+      if (hit) {
+        best_t = t;
+        best_slot = s;
+        tlim = widen(t);
+      }
+    }
+  }
+};
+
+template <bool SPHERES>
+struct FastAnyLeaf {
+  const SceneView& sv;
+  const Ray32& r;
+  float tmax;
+  float tlim;
+  bool done;
+  __device__ FastAnyLeaf(const SceneView& s, const Ray32& ray, float tm)
+      : sv(s), r(ray), tmax(tm), tlim(widen(tm)), done(false) {}
+  __device__ __forceinline__ void operator()(uint32_t ref) {
+    const int cnt = (int)((ref >> 27) & 15u) + 1;
+    const int s0 = (int)(ref & kSlotMask);
+    for (int k = 0; k < cnt && !done; k++) {
+      const int s = s0 + k;
+      const float4 A = __ldg(sv.tri + 3 * s);
+      const float4 E1 = __ldg(sv.tri + 3 * s + 1);
+      const float4 E2 = __ldg(sv.tri + 3 * s + 2);
+      float t;
+      done = (SPHERES && E2.w < 0.0f) ? sphere_hit32(A, E1, r, tmax, &t) : tri_hit32(A, E1, E2, r, tmax, &t);
+    }
+  }
+};
+
+template <int STACK, bool SPHERES>
+__device__ __forceinline__ HitResult closest_hit_fast(const SceneView& sv, const Ray32& r, float tmax32,
+                                                      unsigned* status) {
+  FastClosestLeaf<SPHERES> leaf(sv, r, tmax32);
+  walk<STACK>(sv, r, leaf, status);
+  HitResult h;
+  h.slot = leaf.best_slot;
+  h.t32 = leaf.best_t;
+  h.t64 = 0.0;
+  return h;
+}
+
+template <int STACK, bool SPHERES>
+__device__ __forceinline__ bool any_hit_fast(const SceneView& sv, const Ray32& r, float tmax32, unsigned* status) {
+  FastAnyLeaf<SPHERES> leaf(sv, r, tmax32);
+  walk<STACK>(sv, r, leaf, status);
+  return leaf.done;
 }
 
 }  // namespace bcgx

@@ -191,6 +191,10 @@ def run_gpu(args):
     spec, rays = _make_workload()
     scene = scenes.to_scene(spec)
     ctx = bcgx.Context(local)
+    if args.minblocks:
+        ctx.set_option("raycast_minblocks", args.minblocks)
+    if args.fast:
+        ctx.set_option("raycast_exact", 0)
     ctx.upload(scene)
     stats = ctx.scene_stats()
 
@@ -275,6 +279,8 @@ def run_gpu(args):
                      "algorithmic_bytes_per_ray": bytes_per_ray, **counters},
         "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
         "gpu_launches": args.steps,
+        "raycast_minblocks": ctx.get_option("raycast_minblocks"),
+        "raycast_exact": ctx.get_option("raycast_exact"),
         "clocks": clk,
         "kernel_ms": [round(x, 4) for x in kernel_ms],
     }
@@ -295,6 +301,8 @@ def main():
     ap.add_argument("--tris", type=int, default=N_TRIS, help="smaller case for profiling")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="smaller case for profiling")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
+    ap.add_argument("--minblocks", type=int, default=0, help="ray-cast register variant (1, 6, 8; 0 = library default)")
+    ap.add_argument("--fast", action="store_true", help="plain fp32 closest hit instead of the exact contract")
     args = ap.parse_args()
     N_TRIS, N_RAYS = args.tris, args.rays
     if args.warmup < 3 and args.impl == "gb300":

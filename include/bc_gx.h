@@ -212,6 +212,19 @@ bc_status bc_render_moments(bc_context* ctx, const bc_camera* cam, const bc_sett
 bc_status bc_post_process(bc_context* ctx, int32_t width, int32_t height, const float* linear_in,
                           const float* guide_nd, const bc_settings* settings, float* linear_out, uint32_t* rgba_out);
 
+/*
+ * Tuning options of a context (no counterpart in the reference, whose OpenCL
+ * path picks a work-group size once, gpu_opencl_windows.go:285-304):
+ *   "raycast_minblocks"  1, 6 or 8: register budget of the ray-cast kernels
+ *                        (resident 128-thread blocks per SM the allocation must allow).
+ *   "raycast_exact"      1 (default): bc_raycast is exact as documented there;
+ *                        0: plain fp32 closest hit, t = the fp32 distance, with no
+ *                        exactness contract near edges and ties.
+ * Unknown names or values return BC_ERR_INVALID_ARG.
+ */
+bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value);
+bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value);
+
 /* Request cancellation of the running or next render of ctx; safe from any thread. */
 bc_status bc_cancel(bc_context* ctx);
 /* Clear a pending cancellation. */

@@ -66,6 +66,8 @@ SIGNATURES = [
     ("bc_render_frame", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, u32p, u32p, i64p]),
     ("bc_render_moments", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, f32p, i64p]),
     ("bc_post_process", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, f32p, f32p, P(SettingsC), f32p, u32p]),
+    ("bc_post_process_noalloc", C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, P(SettingsC), C.c_void_p,
+                                          C.c_void_p, C.c_void_p]),
     ("bc_set_option", C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     ("bc_get_option", C.c_int, [C.c_void_p, C.c_char_p, i64p]),
     ("bc_cancel", C.c_int, [C.c_void_p]),

@@ -3,7 +3,9 @@
 // boxBlur, 2490-2555) and tone mapping to RGBA8 (toneMapHDR + toRGBA, 2034-2064).
 // All passes are memory-bound stencils over linear RGB (fp32, 12 B/pixel) and
 // guides (float4 normal + depth, 16 B/pixel; depth < 0 marks an invalid guide).
+#include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "context.h"
 
@@ -221,4 +223,96 @@ extern "C" bc_status bc_post_process(bc_context* ctx, int32_t width, int32_t hei
   if (!e && rgba_out) e = cudaMemcpyAsync(rgba_out, t.rgba, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, ctx->stream);
   if (!e) e = cudaStreamSynchronize(ctx->stream);
   return cuda_status(ctx, e, "post process");
+}
+
+// ---- allocation-free post stack ---------------------------------------------
+// For callers that cannot allocate device memory at the time they post-process
+// a frame: code running inside an engine or plugin host whose GPU memory is
+// owned and budgeted elsewhere, allocation-free real-time loops, and callers
+// that must not synchronise the device (cudaMalloc and cudaFree can). The
+// caller passes device buffers for the input, the guides and the outputs; the
+// two scratch images the passes need live in this file-scope array, which
+// every GPU that loads the library holds for the life of the process.
+constexpr int kNoAllocMaxPixels = 1280 * 720;  // 921,600 pixels: 2 x 11,059,200 bytes of scratch
+static __device__ __align__(256) float g_post_scratch[2 * 3 * kNoAllocMaxPixels];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+float* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_post_scratch for the current device, looked up once per
+// device with that device current (the host-side symbol is not a device address).
+cudaError_t scratch_for_current_device(float** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_post_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_ptr[dev] = static_cast<float*>(p);
+  }
+  *out = g_scratch_ptr[dev];
+  return cudaSuccess;
+}
+}  // namespace
+
+extern "C" bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_linear_in,
+                                             const float* d_guide_nd, const bc_settings* settings,
+                                             float* d_linear_out, uint32_t* d_rgba_out, void* stream) {
+  if (!d_linear_in || !d_linear_out || !settings || width < 1 || height < 1)
+    return set_error(nullptr, BC_ERR_INVALID_ARG, "bad post-process arguments");
+  if ((int64_t)width * height > kNoAllocMaxPixels)
+    return set_error(nullptr, BC_ERR_INVALID_ARG,
+                     "frame exceeds the static scratch of bc_post_process_noalloc (921600 pixels)");
+  if (d_linear_in == d_linear_out)
+    return set_error(nullptr, BC_ERR_INVALID_ARG, "input and output images must not alias");
+  if (settings->denoise && !d_guide_nd) return set_error(nullptr, BC_ERR_INVALID_ARG, "denoise needs guides");
+  float* scratch = nullptr;
+  cudaError_t e = scratch_for_current_device(&scratch);
+  if (e != cudaSuccess) return cuda_status(nullptr, e, "static scratch address");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int W = width, H = height, n = W * H;
+  const dim3 blk(32, 8), grd((W + 31) / 32, (H + 7) / 8);
+  // Nothing in the scratch has to start at zero: every pass writes every pixel
+  // it or a later pass reads.
+  // No pass reads and writes the same buffer.
+  float* sa = scratch;                            // denoised image when bloom follows
+  float* sb = scratch + 3 * (size_t)kNoAllocMaxPixels;  // horizontal bloom blur
+  const bool bloom = settings->bloom > 0;
+  const float* img = d_linear_in;
+  if (settings->denoise) {
+    // a-trous passes ping-pong between the output and scratch A so that the
+    // last pass lands in A when bloom follows, else in the output
+    const int passes = 2 + std::min(3, std::max(settings->taa, settings->txaa));
+    float* last = bloom ? sa : d_linear_out;
+    float* other = bloom ? d_linear_out : sa;
+    const float* cur = d_linear_in;
+    for (int it = 0; it < passes; it++) {
+      float* dst = ((passes - 1 - it) % 2 == 0) ? last : other;
+      k_atrous<<<grd, blk, 0, st>>>(W, H, 1 << it, cur, reinterpret_cast<const float4*>(d_guide_nd), dst);
+      cur = dst;
+    }
+    img = last;
+  }
+  if (bloom) {
+    const float threshold = (float)(1.25 - 0.2 * (double)settings->bloom);
+    const float strength = (float)(0.08 + 0.09 * (double)settings->bloom);
+    k_bloom_h<<<grd, blk, 0, st>>>(W, H, 1 + settings->bloom, threshold, img, sb);
+    k_bloom_v<<<grd, blk, 0, st>>>(W, H, 1 + settings->bloom, strength, img, sb, d_linear_out);
+    img = d_linear_out;
+  }
+  if (img != d_linear_out) {
+    e = cudaMemcpyAsync(d_linear_out, img, 3 * sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_status(nullptr, e, "post copy");
+  }
+  if (d_rgba_out) {
+    const float scale = (float)std::pow(2.0, settings->exposure);
+    const float inv_gamma = (float)(1.0 / std::max(0.1, settings->gamma));
+    k_tonemap<<<(n + 255) / 256, 256, 0, st>>>(n, scale, inv_gamma, settings->hdr, d_linear_out, d_rgba_out);
+  }
+  return cuda_status(nullptr, cudaGetLastError(), "post launch");
 }

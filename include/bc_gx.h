@@ -213,6 +213,29 @@ bc_status bc_post_process(bc_context* ctx, int32_t width, int32_t height, const 
                           const float* guide_nd, const bc_settings* settings, float* linear_out, uint32_t* rgba_out);
 
 /*
+ * Allocation-free variant of bc_post_process. It has no counterpart in the
+ * reference. It is for callers that cannot allocate device memory when they
+ * post-process a frame: an engine or plugin host that owns the GPU memory
+ * budget, an allocation-free real-time loop, or code that must not synchronise
+ * the device (cudaMalloc and cudaFree can). It needs no context, takes device
+ * pointers for every image (width*height RGB floats in and out, width*height
+ * (nx, ny, nz, depth) guides, width*height RGBA8 words or NULL), enqueues on
+ * `stream` (a cudaStream_t, NULL = legacy default) and returns once the work is
+ * enqueued. It calls no cudaMalloc, cudaFree or allocating library routine.
+ * Its scratch is a static device array of two images of at most 921,600 pixels
+ * (22 MB), which every GPU that loads the library holds until the process
+ * exits; larger frames are rejected with BC_ERR_INVALID_ARG, as are aliased
+ * input and output. Every call shares that array: calls that overlap on the
+ * GPU (different streams, or devices sharing it across threads without
+ * ordering) race on it. The first call on each device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.
+ */
+bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_linear_in, const float* d_guide_nd,
+                                  const bc_settings* settings, float* d_linear_out, uint32_t* d_rgba_out,
+                                  void* stream);
+
+/*
  * Tuning options of a context (no counterpart in the reference, whose OpenCL
  * path picks a work-group size once, gpu_opencl_windows.go:285-304):
  *   "raycast_minblocks"  1, 6 or 8: register budget of the ray-cast kernels

@@ -66,9 +66,9 @@ struct bc_context {
   bcgx::DeviceScene ds;
   bcgx::DevBuf d_nodes, d_tri, d_slot64, d_snorm, d_slot_prim, d_mats, d_lights, d_lpdf;
   int64_t stats[6] = {0, 0, 0, 0, 0, 0};
-  int raycast_minblocks = 6;  // register budget of the exact ray-cast kernels (bc_set_option)
+  int raycast_minblocks = 8;  // register budget of the exact ray-cast kernels (bc_set_option)
   int raycast_exact = 1;      // 0: plain fp32 closest hit (bc_set_option "raycast_exact")
-  int raycast_variant = 6;    // 0 = fast kernel, else the exact kernel's minblocks
+  int raycast_variant = 8;    // 0 = fast kernel, else the exact kernel's minblocks
   // ray-cast staging
   bcgx::DevBuf d_rays, d_t, d_prim, d_occ;
   unsigned* d_status = nullptr;

@@ -81,12 +81,14 @@ class Context:
         return dict(zip(keys, list(out)))
 
     # -- ray casting --
-    def raycast(self, rays: np.ndarray):
-        """rays: (n, 8) float32 (ox, oy, oz, tmin, dx, dy, dz, tmax) -> (t float32, prim int32)."""
+    def raycast(self, rays: np.ndarray, t_out: np.ndarray | None = None, prim_out: np.ndarray | None = None):
+        """rays: (n, 8) float32 (ox, oy, oz, tmin, dx, dy, dz, tmax) -> (t float32, prim int32).
+        Optional output arrays (e.g. in pinned host memory) are filled in place."""
         r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
         n = len(r)
-        t = np.empty(n, dtype=np.float32)
-        p = np.empty(n, dtype=np.int32)
+        t = np.empty(n, dtype=np.float32) if t_out is None else t_out
+        p = np.empty(n, dtype=np.int32) if prim_out is None else prim_out
+        assert t.dtype == np.float32 and p.dtype == np.int32 and len(t) == n and len(p) == n
         check(lib().bc_raycast(self._h, ptr(r, C.c_float), n, ptr(t, C.c_float), ptr(p, C.c_int32)), self._h)
         return t, p
 

@@ -1,6 +1,7 @@
 // C-ABI: context lifetime, scene upload and the ray-cast entry points.
 // Mirrors the call sequence of renderOpenCL (gpu_opencl_windows.go:565-720):
 // init once, ensure the scene by revision, then launch and read back.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -106,6 +107,10 @@ bc_status bc_create(int device_ordinal, bc_context** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_status, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_work, 64);
+  if (e == cudaSuccess) {
+    e = cudaMemset(ctx->d_work, 0, 64);
+  }
   if (e == cudaSuccess) e = cudaHostAlloc((void**)&ctx->h_cancel, sizeof(int), cudaHostAllocMapped);
   if (e == cudaSuccess) {
     *ctx->h_cancel = 0;
@@ -129,7 +134,9 @@ void bc_destroy(bc_context* ctx) {
                     &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ})
     b->release();
   if (ctx->d_status) cudaFree(ctx->d_status);
+  if (ctx->d_work) cudaFree(ctx->d_work);
   if (ctx->h_cancel) cudaFreeHost(ctx->h_cancel);
+  if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -223,10 +230,14 @@ bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, flo
   if (((uintptr_t)d_rays & 15u) != 0) return set_error(ctx, BC_ERR_INVALID_ARG, "rays must be 16-byte aligned");
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-  cudaError_t e = launch_raycast_closest(ctx->ds, (const float4*)d_rays, n, d_t_out, d_prim_out, ctx->d_status, ctx->raycast_variant, st);
+  cudaError_t e = launch_raycast_closest(ctx->ds, (const float4*)d_rays, n, d_t_out, d_prim_out, ctx->d_status,
+                                         ctx->d_work + 2, ctx->raycast_variant, st);
   return cuda_status(ctx, e, "ray-cast launch");
 }
 
+// Host-buffer ray cast, pipelined: the rays go in chunks of 1 Mi over two
+// streams, so the copy of chunk c+1 in, the kernel on chunk c and the copy of
+// chunk c-1 out overlap (copy engines and SMs work at the same time).
 bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out, int32_t* prim_out) {
   if (!ctx) return set_error(nullptr, BC_ERR_INVALID_ARG, "NULL context");
   if (n < 0 || (n > 0 && (!rays || !t_out || !prim_out))) return set_error(ctx, BC_ERR_INVALID_ARG, "bad ray-cast arguments");
@@ -237,13 +248,28 @@ bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out
   if ((e = ctx->d_rays.ensure((size_t)n * 32)) || (e = ctx->d_t.ensure((size_t)n * 4)) ||
       (e = ctx->d_prim.ensure((size_t)n * 4)))
     return cuda_status(ctx, e, "ray-cast buffers");
-  e = cudaMemcpyAsync(ctx->d_rays.p, rays, (size_t)n * 32, cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess)
-    e = launch_raycast_closest(ctx->ds, ctx->d_rays.as<float4>(), n, ctx->d_t.as<float>(), ctx->d_prim.as<int32_t>(),
-                               ctx->d_status, ctx->raycast_variant, ctx->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(t_out, ctx->d_t.p, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(prim_out, ctx->d_prim.p, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (!ctx->aux_stream) {
+    e = cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(ctx, e, "ray-cast stream");
+  }
+  const int64_t chunk = (int64_t)1 << 20;
+  cudaStream_t streams[2] = {ctx->stream, ctx->aux_stream};
+  for (int64_t off = 0, c = 0; off < n && e == cudaSuccess; off += chunk, c++) {
+    const int64_t m = std::min(chunk, n - off);
+    cudaStream_t st = streams[c & 1];
+    float4* dr = ctx->d_rays.as<float4>() + 2 * off;
+    e = cudaMemcpyAsync(dr, rays + 8 * off, (size_t)m * 32, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = launch_raycast_closest(ctx->ds, dr, m, ctx->d_t.as<float>() + off, ctx->d_prim.as<int32_t>() + off,
+                                 ctx->d_status, ctx->d_work + (c & 1), ctx->raycast_variant, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(t_out + off, ctx->d_t.as<float>() + off, (size_t)m * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(prim_out + off, ctx->d_prim.as<int32_t>() + off, (size_t)m * 4, cudaMemcpyDeviceToHost, st);
+  }
+  cudaError_t e2 = cudaStreamSynchronize(ctx->aux_stream);
+  cudaError_t e1 = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = e1 != cudaSuccess ? e1 : e2;
   if (e != cudaSuccess) return cuda_status(ctx, e, "ray cast");
   return check_kernel_status(ctx);
 }

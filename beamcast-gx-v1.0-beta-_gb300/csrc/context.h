@@ -58,6 +58,7 @@ struct HostBuf {
 struct bc_context {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t aux_stream = nullptr;  // second stream of the pipelined host-buffer ray cast
   std::string err;
   std::string name;
   // resident scene
@@ -66,12 +67,15 @@ struct bc_context {
   bcgx::DeviceScene ds;
   bcgx::DevBuf d_nodes, d_tri, d_slot64, d_snorm, d_slot_prim, d_mats, d_lights, d_lpdf;
   int64_t stats[6] = {0, 0, 0, 0, 0, 0};
-  int raycast_minblocks = 8;  // register budget of the exact ray-cast kernels (bc_set_option)
+  int raycast_minblocks = 6;  // register budget of the exact ray-cast kernels (bc_set_option)
   int raycast_exact = 1;      // 0: plain fp32 closest hit (bc_set_option "raycast_exact")
-  int raycast_variant = 8;    // 0 = fast kernel, else the exact kernel's minblocks
+  int raycast_variant = 6;    // 0 = fast kernel, else the exact kernel's minblocks
   // ray-cast staging
   bcgx::DevBuf d_rays, d_t, d_prim, d_occ;
   unsigned* d_status = nullptr;
+  // work counters of the persistent ray-cast kernels: [0], [1] the two streams of
+  // bc_raycast, [2] bc_raycast_device
+  unsigned long long* d_work = nullptr;
   // rendering state (render.cu)
   struct RenderBuffers* rb = nullptr;
   std::atomic<int> cancel{0};

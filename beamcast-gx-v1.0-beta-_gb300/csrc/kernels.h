@@ -25,8 +25,10 @@ struct DeviceScene {
 int stack_variant(int need);
 
 // Exact closest hit over n rays (8 floats each); see bc_raycast in bc_gx.h.
+// `work` is an 8-byte device counter private to this launch's stream (persistent kernels).
 cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int64_t n, float* t_out,
-                                   int32_t* prim_out, unsigned* status, int variant, cudaStream_t st);
+                                   int32_t* prim_out, unsigned* status, unsigned long long* work, int variant,
+                                   cudaStream_t st);
 // Exact any hit.
 cudaError_t launch_raycast_any(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
                                int variant, cudaStream_t st);

@@ -2,9 +2,8 @@
 // packer (pack.cpp) and the CUDA kernels.
 //
 // HBM layout (all arrays 256-byte aligned by cudaMalloc):
-//   Node8  nodes[n8]      256 B each: child boxes SoA (6 x 8 fp32), 8 child refs,
-//                         child count. One node = four 64-byte sectors, fetched
-//                         with 128-bit loads.
+//   Node8  nodes[n8]      96 B each: quantization grid (origin, 3 exponents),
+//                         child count, 8 child refs, 8-bit child box bounds.
 //   float4 tri[3*slots]   48 B per primitive slot, slots in Scene.Order order so a
 //                         leaf's primitives are contiguous:
 //                           triangle: (A, max|A|) (E1, max|E1|) (E2, max|E2|)
@@ -31,13 +30,19 @@ constexpr unsigned kStatusTimeout = 2u;
 constexpr unsigned kStatusCapacity = 4u;
 constexpr unsigned kStatusBound = 8u;  // an fp32 hit classified as certain failed its fp64 test
 
-struct alignas(64) Node8 {
-  float lox[8], hix[8], loy[8], hiy[8], loz[8], hiz[8];
+// Wide node with quantized child boxes (96 bytes, six 128-bit loads). Each
+// axis has a power-of-two grid anchored at (px, py, pz): a child's box on that
+// axis is [p + qlo * 2^(e-127), p + qhi * 2^(e-127)], decoded on the device with
+// round-down / round-up FMAs. The packer picks p, e and q so that every decoded
+// box strictly contains the fp64 box of the binary node it stands for.
+struct alignas(16) Node8 {
+  float px, py, pz;
+  uint8_t ex, ey, ez;  // biased exponents of the grid step per axis
+  uint8_t nchild;
   uint32_t child[8];
-  int32_t nchild;
-  int32_t pad[7];
+  uint8_t qlox[8], qhix[8], qloy[8], qhiy[8], qloz[8], qhiz[8];
 };
-static_assert(sizeof(Node8) == 256, "Node8 must be 256 bytes");
+static_assert(sizeof(Node8) == 96, "Node8 must be 96 bytes");
 
 struct alignas(16) F4 {
   float x, y, z, w;

@@ -139,15 +139,50 @@ void pack_slots(const bc_scene_desc& d, PackedScene* ps) {
   }
 }
 
-// Outward-rounded fp32 box with one extra ulp of slack, so that a ray origin
-// lying exactly on an fp64 face is strictly inside the fp32 box.
-void store_child_box(Node8& n, int slot, const double* b) {
-  n.lox[slot] = std::nextafterf(round_down_f32(b[0]), -INFINITY);
-  n.loy[slot] = std::nextafterf(round_down_f32(b[1]), -INFINITY);
-  n.loz[slot] = std::nextafterf(round_down_f32(b[2]), -INFINITY);
-  n.hix[slot] = std::nextafterf(round_up_f32(b[3]), INFINITY);
-  n.hiy[slot] = std::nextafterf(round_up_f32(b[4]), INFINITY);
-  n.hiz[slot] = std::nextafterf(round_up_f32(b[5]), INFINITY);
+// Quantizes the child boxes of one node. Per axis: p = the children's union
+// minimum rounded down to fp32 and stepped one ulp further down, the grid step
+// 2^e the smallest power of two with 254 * 2^e >= extent, qlo = the largest q
+// with p + q 2^e < lo (strict), qhi = the smallest q with p + q 2^e > hi. The
+// device decodes with round-down (lo) and round-up (hi) FMAs, which keeps the
+// strict inequalities, so a ray origin on a face of the fp64 box is strictly
+// inside the decoded box (the reference's zero-direction axes test origins
+// against closed boxes).
+void quantize_node(Node8& n, const double* boxes, int nk) {
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int k = 0; k < nk; k++)
+    for (int a = 0; a < 3; a++) {
+      lo[a] = std::min(lo[a], boxes[6 * k + a]);
+      hi[a] = std::max(hi[a], boxes[6 * k + 3 + a]);
+    }
+  float p[3];
+  uint8_t eb[3];
+  double scale[3];
+  for (int a = 0; a < 3; a++) {
+    p[a] = std::nextafterf(round_down_f32(lo[a]), -INFINITY);
+    const double extent = hi[a] - (double)p[a];
+    int e = -126;
+    while (e < 127 && std::ldexp(254.0, e) < extent) e++;
+    eb[a] = (uint8_t)(e + 127);
+    scale[a] = std::ldexp(1.0, e);
+  }
+  n.px = p[0]; n.py = p[1]; n.pz = p[2];
+  n.ex = eb[0]; n.ey = eb[1]; n.ez = eb[2];
+  n.nchild = (uint8_t)nk;
+  uint8_t* qlo[3] = {n.qlox, n.qloy, n.qloz};
+  uint8_t* qhi[3] = {n.qhix, n.qhiy, n.qhiz};
+  for (int k = 0; k < 8; k++)
+    for (int a = 0; a < 3; a++) {
+      if (k >= nk) { qlo[a][k] = 255; qhi[a][k] = 0; continue; }
+      const double bl = boxes[6 * k + a], bh = boxes[6 * k + 3 + a];
+      double ql = std::floor((bl - (double)p[a]) / scale[a]);
+      ql = std::max(0.0, std::min(255.0, ql));
+      while (ql > 0 && (double)p[a] + ql * scale[a] >= bl) ql -= 1;
+      double qh = std::ceil((bh - (double)p[a]) / scale[a]);
+      qh = std::max(0.0, std::min(255.0, qh));
+      while (qh < 255 && (double)p[a] + qh * scale[a] <= bh) qh += 1;
+      qlo[a][k] = (uint8_t)ql;
+      qhi[a][k] = (uint8_t)qh;
+    }
 }
 
 uint32_t leaf_ref(const bc_scene_desc& d, int32_t i) {
@@ -194,16 +229,12 @@ void collapse(const bc_scene_desc& d, PackedScene* ps) {
     }
     Node8& n = ps->nodes[idx];
     std::memset(&n, 0, sizeof(n));
-    n.nchild = nk;
-    for (int k = nk; k < 8; k++) {  // unused slots: empty boxes, never read
-      n.lox[k] = n.loy[k] = n.loz[k] = INFINITY;
-      n.hix[k] = n.hiy[k] = n.hiz[k] = -INFINITY;
-      n.child[k] = 0;
-    }
+    double boxes[48];
+    for (int k = 0; k < nk; k++) std::memcpy(boxes + 6 * k, d.node_box + 6 * (size_t)kids[k], 6 * sizeof(double));
+    quantize_node(n, boxes, nk);
     ps->depth = std::max(ps->depth, j.depth);
     ps->stack_need = std::max(ps->stack_need, j.acc + nk + 1);
     for (int k = nk - 1; k >= 0; k--) {
-      store_child_box(ps->nodes[idx], k, d.node_box + 6 * (size_t)kids[k]);
       if (d.node_count[kids[k]] > 0) {
         ps->nodes[idx].child[k] = leaf_ref(d, kids[k]);
       } else {

@@ -1,6 +1,8 @@
 // Ray-cast kernels: exact closest hit and any hit over the BVH8, one thread
 // per ray. Rays are 32-byte records (ox, oy, oz, tmin, dx, dy, dz, tmax) read
 // with two 128-bit loads; results are written as coalesced 4-byte streams.
+#include <algorithm>
+
 #include "kernels.h"
 #include "trace_core.cuh"
 
@@ -66,6 +68,186 @@ __global__ void __launch_bounds__(128) k_closest_fast(SceneView sv, const float4
   prim_out[i] = h.slot >= 0 ? __ldg(sv.slot_prim + h.slot) : -1;
 }
 
+// ---- persistent kernels with per-lane refill -------------------------------
+// A lane whose ray is done fetches the next ray index at once (one atomic per
+// warp for all lanes that need work), so the warp does not idle until its
+// slowest ray ends. The exact kernel parks each finished ray's contenders in a
+// per-warp queue in shared memory; when 32 are parked, the warp settles them
+// in fp64 with every lane active. Triangle-only scenes (spheres settle at
+// once and use the kernels above).
+struct ParkQueue {
+  long long idx[32];
+  int bslot[32];
+  float bhi[32];
+  int npend[32];
+  int pslot[kPending][32];
+  float plo[kPending][32];
+};
+
+__device__ __forceinline__ void settle_parked(const SceneView& sv, const float4* __restrict__ rays,
+                                              const ParkQueue& q, int k, float* __restrict__ t_out,
+                                              int32_t* __restrict__ prim_out, unsigned* status) {
+  const long long i = q.idx[k];
+  const float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
+  const D3 o{(double)a.x, (double)a.y, (double)a.z}, d{(double)b.x, (double)b.y, (double)b.z};
+  const double tmin = (double)a.w, tmax = (double)b.w;
+  const int bslot = q.bslot[k];
+  const float bhi = q.bhi[k];
+  int win = -1;
+  double wt = 0.0;
+  if (bslot >= 0) {
+    double t;
+    if (tri_hit64(sv.slot64 + 9 * (size_t)bslot, o, d, tmin, tmax, &t)) {
+      win = bslot;
+      wt = t;
+    } else {
+      atomicOr(status, kStatusBound);  // a certain hit must pass its fp64 test
+    }
+  }
+  const int np = q.npend[k];
+#pragma unroll
+  for (int j = 0; j < kPending; j++) {
+    if (j < np && !(bslot >= 0 && q.plo[j][k] > bhi)) {
+      const int sj = q.pslot[j][k];
+      double t;
+      if (tri_hit64(sv.slot64 + 9 * (size_t)sj, o, d, tmin, tmax, &t) &&
+          (win < 0 || t < wt || (t == wt && sj > win))) {
+        win = sj;
+        wt = t;
+      }
+    }
+  }
+  if (win >= 0) {
+    t_out[i] = __double2float_rn(wt);
+    prim_out[i] = __ldg(sv.slot_prim + win);
+  } else {
+    t_out[i] = -1.0f;
+    prim_out[i] = -1;
+  }
+}
+
+template <int STACK, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_closest_exact_persistent(SceneView sv, const float4* __restrict__ rays,
+                                                                        int64_t n, float* __restrict__ t_out,
+                                                                        int32_t* __restrict__ prim_out,
+                                                                        unsigned* status, unsigned long long* work) {
+  __shared__ ParkQueue park[4];
+  ParkQueue& q = park[threadIdx.x >> 5];
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  long long idx = -1;
+  bool exhausted = false;
+  Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
+  ExactClosestLeaf<false> leaf(sv, r, 0.0f, status);
+  Walker<STACK> w;
+  w.reset();
+  int parked = 0;  // warp-uniform
+  for (;;) {
+    const bool need = idx < 0 && !exhausted;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if ((int)lane == leader) base = atomicAdd(work, (unsigned long long)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const unsigned long long my = base + (unsigned long long)__popc(m & below);
+        if (my < (unsigned long long)n) {
+          idx = (long long)my;
+          const float4 a = __ldg(rays + 2 * idx), b = __ldg(rays + 2 * idx + 1);
+          r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
+          leaf.reset(b.w);
+          w.reset();
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    const bool active = idx >= 0;
+    if (!__any_sync(0xffffffffu, active)) break;
+    bool finished = false;
+    if (active) finished = w.step(sv, r, leaf, status);
+    const unsigned pm = __ballot_sync(0xffffffffu, finished);
+    if (pm) {
+      if (parked + __popc(pm) > 32) {
+        __syncwarp();
+        if ((int)lane < parked) settle_parked(sv, rays, q, (int)lane, t_out, prim_out, status);
+        __syncwarp();
+        parked = 0;
+      }
+      if (finished) {
+        const int k = parked + __popc(pm & below);
+        q.idx[k] = idx;
+        q.bslot[k] = leaf.best.slot;
+        q.bhi[k] = leaf.best.hi;
+        q.npend[k] = leaf.npend;
+#pragma unroll
+        for (int j = 0; j < kPending; j++) {
+          q.pslot[j][k] = leaf.pend[j].slot;
+          q.plo[j][k] = leaf.pend[j].lo;
+        }
+        idx = -1;
+      }
+      parked += __popc(pm);
+    }
+  }
+  __syncwarp();
+  if ((int)lane < parked) settle_parked(sv, rays, q, (int)lane, t_out, prim_out, status);
+}
+
+template <int STACK>
+__global__ void __launch_bounds__(128) k_closest_fast_persistent(SceneView sv, const float4* __restrict__ rays,
+                                                                 int64_t n, float* __restrict__ t_out,
+                                                                 int32_t* __restrict__ prim_out, unsigned* status,
+                                                                 unsigned long long* work) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  long long idx = -1;
+  bool exhausted = false;
+  Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
+  FastClosestLeaf<false> leaf(sv, r, 0.0f);
+  Walker<STACK> w;
+  w.reset();
+  for (;;) {
+    const bool need = idx < 0 && !exhausted;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if ((int)lane == leader) base = atomicAdd(work, (unsigned long long)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const unsigned long long my = base + (unsigned long long)__popc(m & below);
+        if (my < (unsigned long long)n) {
+          idx = (long long)my;
+          const float4 a = __ldg(rays + 2 * idx), b = __ldg(rays + 2 * idx + 1);
+          r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
+          leaf.reset(b.w);
+          w.reset();
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    const bool active = idx >= 0;
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (active && w.step(sv, r, leaf, status)) {
+      t_out[idx] = leaf.best_slot >= 0 ? leaf.best_t : -1.0f;
+      prim_out[idx] = leaf.best_slot >= 0 ? __ldg(sv.slot_prim + leaf.best_slot) : -1;
+      idx = -1;
+    }
+  }
+}
+
+template <class K>
+int persistent_blocks(K kernel) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 128, 0);
+  return sms * (per > 0 ? per : 1);
+}
+
 SceneView view_of(const DeviceScene& s) {
   SceneView v;
   v.nodes = s.nodes;
@@ -81,12 +263,18 @@ SceneView view_of(const DeviceScene& s) {
 // 8: <= 64 registers). Selected per context (bc_set_option "raycast_minblocks").
 template <int STACK, int MINB>
 cudaError_t closest_stack(const DeviceScene& s, const float4* rays, int64_t n, float* t, int32_t* p, unsigned* status,
-                          cudaStream_t st) {
+                          unsigned long long* work, cudaStream_t st) {
   const int64_t grid = (n + 127) / 128;
-  if (s.has_spheres)
+  if (s.has_spheres) {
     k_closest_exact<STACK, true, MINB><<<(unsigned)grid, 128, 0, st>>>(view_of(s), rays, n, t, p, status);
-  else
-    k_closest_exact<STACK, false, MINB><<<(unsigned)grid, 128, 0, st>>>(view_of(s), rays, n, t, p, status);
+  } else {
+    static int blocks = 0;
+    if (!blocks) blocks = persistent_blocks(k_closest_exact_persistent<STACK, MINB>);
+    cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    const int g = (int)std::min<int64_t>(blocks, (n + 127) / 128);
+    k_closest_exact_persistent<STACK, MINB><<<g, 128, 0, st>>>(view_of(s), rays, n, t, p, status, work);
+  }
   return cudaGetLastError();
 }
 
@@ -103,19 +291,25 @@ cudaError_t any_stack(const DeviceScene& s, const float4* rays, int64_t n, uint8
 
 template <int STACK>
 cudaError_t closest_var(const DeviceScene& s, const float4* rays, int64_t n, float* t, int32_t* p, unsigned* status,
-                        int variant, cudaStream_t st) {
+                        unsigned long long* work, int variant, cudaStream_t st) {
   if (variant == 0) {  // fast, not exact
     const int64_t grid = (n + 127) / 128;
-    if (s.has_spheres)
+    if (s.has_spheres) {
       k_closest_fast<STACK, true><<<(unsigned)grid, 128, 0, st>>>(view_of(s), rays, n, t, p, status);
-    else
-      k_closest_fast<STACK, false><<<(unsigned)grid, 128, 0, st>>>(view_of(s), rays, n, t, p, status);
+    } else {
+      static int blocks = 0;
+      if (!blocks) blocks = persistent_blocks(k_closest_fast_persistent<STACK>);
+      cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), st);
+      if (e != cudaSuccess) return e;
+      const int g = (int)std::min<int64_t>(blocks, grid);
+      k_closest_fast_persistent<STACK><<<g, 128, 0, st>>>(view_of(s), rays, n, t, p, status, work);
+    }
     return cudaGetLastError();
   }
   switch (variant) {
-    case 6: return closest_stack<STACK, 6>(s, rays, n, t, p, status, st);
-    case 8: return closest_stack<STACK, 8>(s, rays, n, t, p, status, st);
-    default: return closest_stack<STACK, 1>(s, rays, n, t, p, status, st);
+    case 6: return closest_stack<STACK, 6>(s, rays, n, t, p, status, work, st);
+    case 8: return closest_stack<STACK, 8>(s, rays, n, t, p, status, work, st);
+    default: return closest_stack<STACK, 1>(s, rays, n, t, p, status, work, st);
   }
 }
 
@@ -132,12 +326,13 @@ cudaError_t any_var(const DeviceScene& s, const float4* rays, int64_t n, uint8_t
 }  // namespace
 
 cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int64_t n, float* t_out,
-                                   int32_t* prim_out, unsigned* status, int variant, cudaStream_t st) {
+                                   int32_t* prim_out, unsigned* status, unsigned long long* work, int variant,
+                                   cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   switch (stack_variant(s.stack_need)) {
-    case 64: return closest_var<64>(s, rays, n, t_out, prim_out, status, variant, st);
-    case 128: return closest_var<128>(s, rays, n, t_out, prim_out, status, variant, st);
-    case 256: return closest_var<256>(s, rays, n, t_out, prim_out, status, variant, st);
+    case 64: return closest_var<64>(s, rays, n, t_out, prim_out, status, work, variant, st);
+    case 128: return closest_var<128>(s, rays, n, t_out, prim_out, status, work, variant, st);
+    case 256: return closest_var<256>(s, rays, n, t_out, prim_out, status, work, variant, st);
     default: return cudaErrorInvalidValue;
   }
 }

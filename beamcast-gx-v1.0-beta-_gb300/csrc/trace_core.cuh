@@ -61,27 +61,39 @@ __device__ __forceinline__ float slab_near(float lox, float hix, float loy, floa
   return tn <= tf ? tn : __int_as_float(0x7f800000);
 }
 
-// Test all children of a node; near[k] = entry distance or +inf.
+// Exact float of an unsigned byte: 2^23 + b built in the bit pattern, minus 2^23.
+__device__ __forceinline__ float byte_f(uint32_t word, int j) {
+  return __uint_as_float(__byte_perm(word, 0x4b000000u, 0x7540u | (uint32_t)j)) - 8388608.0f;
+}
+
+// Test all children of a node; near[k] = entry distance or +inf. Child boxes
+// are decoded conservatively (round-down lower, round-up upper bounds).
 __device__ __forceinline__ void node_children(const Node8* __restrict__ node, const Ray32& r, float tlim,
                                               float near[8], uint32_t child[8]) {
   const float4* p = reinterpret_cast<const float4*>(node);
-  const float4 lx0 = __ldg(p + 0), lx1 = __ldg(p + 1), hx0 = __ldg(p + 2), hx1 = __ldg(p + 3);
-  const float4 ly0 = __ldg(p + 4), ly1 = __ldg(p + 5), hy0 = __ldg(p + 6), hy1 = __ldg(p + 7);
-  const float4 lz0 = __ldg(p + 8), lz1 = __ldg(p + 9), hz0 = __ldg(p + 10), hz1 = __ldg(p + 11);
-  const uint4 c0 = __ldg(reinterpret_cast<const uint4*>(p + 12));
-  const uint4 c1 = __ldg(reinterpret_cast<const uint4*>(p + 13));
-  const int nchild = __ldg(reinterpret_cast<const int*>(p + 14));
-  const float lox[8] = {lx0.x, lx0.y, lx0.z, lx0.w, lx1.x, lx1.y, lx1.z, lx1.w};
-  const float hix[8] = {hx0.x, hx0.y, hx0.z, hx0.w, hx1.x, hx1.y, hx1.z, hx1.w};
-  const float loy[8] = {ly0.x, ly0.y, ly0.z, ly0.w, ly1.x, ly1.y, ly1.z, ly1.w};
-  const float hiy[8] = {hy0.x, hy0.y, hy0.z, hy0.w, hy1.x, hy1.y, hy1.z, hy1.w};
-  const float loz[8] = {lz0.x, lz0.y, lz0.z, lz0.w, lz1.x, lz1.y, lz1.z, lz1.w};
-  const float hiz[8] = {hz0.x, hz0.y, hz0.z, hz0.w, hz1.x, hz1.y, hz1.z, hz1.w};
+  const float4 w0 = __ldg(p + 0);
+  const uint4 c0 = __ldg(reinterpret_cast<const uint4*>(p + 1));
+  const uint4 c1 = __ldg(reinterpret_cast<const uint4*>(p + 2));
+  const uint4 qx = __ldg(reinterpret_cast<const uint4*>(p + 3));
+  const uint4 qy = __ldg(reinterpret_cast<const uint4*>(p + 4));
+  const uint4 qz = __ldg(reinterpret_cast<const uint4*>(p + 5));
+  const uint32_t meta = __float_as_uint(w0.w);
+  const float sx = __uint_as_float((meta & 0xffu) << 23);
+  const float sy = __uint_as_float(((meta >> 8) & 0xffu) << 23);
+  const float sz = __uint_as_float(((meta >> 16) & 0xffu) << 23);
+  const int nchild = (int)(meta >> 24);
   child[0] = c0.x; child[1] = c0.y; child[2] = c0.z; child[3] = c0.w;
   child[4] = c1.x; child[5] = c1.y; child[6] = c1.z; child[7] = c1.w;
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    float t = slab_near(lox[k], hix[k], loy[k], hiy[k], loz[k], hiz[k], r, tlim);
+    const int j = k & 3;
+    const uint32_t wlx = k < 4 ? qx.x : qx.y, whx = k < 4 ? qx.z : qx.w;
+    const uint32_t wly = k < 4 ? qy.x : qy.y, why = k < 4 ? qy.z : qy.w;
+    const uint32_t wlz = k < 4 ? qz.x : qz.y, whz = k < 4 ? qz.z : qz.w;
+    const float lox = __fmaf_rd(byte_f(wlx, j), sx, w0.x), hix = __fmaf_ru(byte_f(whx, j), sx, w0.x);
+    const float loy = __fmaf_rd(byte_f(wly, j), sy, w0.y), hiy = __fmaf_ru(byte_f(why, j), sy, w0.y);
+    const float loz = __fmaf_rd(byte_f(wlz, j), sz, w0.z), hiz = __fmaf_ru(byte_f(whz, j), sz, w0.z);
+    const float t = slab_near(lox, hix, loy, hiy, loz, hiz, r, tlim);
     near[k] = k < nchild ? t : __int_as_float(0x7f800000);
   }
 }
@@ -345,6 +357,67 @@ __device__ __forceinline__ void walk(const SceneView& sv, const Ray32& r, Leaf& 
   }
 }
 
+// The same while-while walk as a resumable per-lane state machine, for
+// persistent kernels that refill a lane with a new ray as soon as its ray is
+// done. step() runs one outer iteration and returns true once the walk of the
+// current ray has finished (stack empty, or leaf.done).
+template <int STACK>
+struct Walker {
+  uint2 st[STACK];
+  int sp;
+  uint32_t ref;
+  uint32_t pending;
+  __device__ __forceinline__ void reset() {
+    sp = 0;
+    ref = 0;
+    pending = 0;
+  }
+  __device__ __forceinline__ uint32_t pop(float tlim) {
+    while (sp > 0) {
+      const uint2 e = st[--sp];
+      if (__uint_as_float(e.y) <= tlim) return e.x;
+    }
+    return kEnd;
+  }
+  template <class Leaf>
+  __device__ __forceinline__ bool step(const SceneView& sv, const Ray32& r, Leaf& leaf, unsigned* status) {
+    while (ref != kEnd && !(ref & kLeafBit)) {
+      float nr[8];
+      uint32_t ch[8];
+      node_children(sv.nodes + ref, r, leaf.tlim, nr, ch);
+      sort8(nr, ch);
+      if (nr[0] == __int_as_float(0x7f800000)) {
+        ref = pop(leaf.tlim);
+      } else {
+#pragma unroll
+        for (int k = 7; k >= 1; k--) {
+          if (nr[k] != __int_as_float(0x7f800000)) {
+            if (sp < STACK) st[sp++] = make_uint2(ch[k], __float_as_uint(nr[k]));
+            else atomicOr(status, kStatusStackOverflow);
+          }
+        }
+        ref = ch[0];
+      }
+      if (ref != kEnd && (ref & kLeafBit)) {
+        if (pending != 0) break;
+        pending = ref;
+        ref = pop(leaf.tlim);
+      }
+      if (__all_sync(__activemask(), pending != 0)) break;
+    }
+    while (pending != 0) {
+      leaf(pending);
+      if (leaf.done) return true;
+      pending = 0;
+      if (ref != kEnd && (ref & kLeafBit)) {
+        pending = ref;
+        ref = pop(leaf.tlim);
+      }
+    }
+    return ref == kEnd;
+  }
+};
+
 // ---- exact closest hit -------------------------------------------------------
 // Candidates carry an fp32 interval [lo, hi] that holds their fp64 distance.
 // `best` is the certain hit with the smallest upper bound; candidates that
@@ -374,7 +447,14 @@ struct ExactClosestLeaf {
   Contender pend[kPending];
 
   __device__ ExactClosestLeaf(const SceneView& s, const Ray32& ray, float tmax, unsigned* st)
-      : sv(s), r(ray), status(st), tmax_ray(tmax), tlim(widen(tmax)), done(false), npend(0) {
+      : sv(s), r(ray), status(st) {
+    reset(tmax);
+  }
+  __device__ __forceinline__ void reset(float tmax) {
+    tmax_ray = tmax;
+    tlim = widen(tmax);
+    done = false;
+    npend = 0;
     best.slot = -1;
     best.lo = tmax;
     best.hi = tmax;
@@ -559,6 +639,12 @@ struct FastClosestLeaf {
   bool done;
   __device__ FastClosestLeaf(const SceneView& s, const Ray32& ray, float tmax)
       : sv(s), r(ray), best_t(tmax), best_slot(-1), tlim(widen(tmax)), done(false) {}
+  __device__ __forceinline__ void reset(float tmax) {
+    best_t = tmax;
+    best_slot = -1;
+    tlim = widen(tmax);
+    done = false;
+  }
   __device__ __forceinline__ void operator()(uint32_t ref) {
     const int cnt = (int)((ref >> 27) & 15u) + 1;
     const int s0 = (int)(ref & kSlotMask);

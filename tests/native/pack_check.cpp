@@ -1,0 +1,114 @@
+// Host check of the BVH8 packer (compiled and run by tests/test_pack_native.py):
+// every quantized child box, decoded the way the device decodes it (round-down
+// lower bound, round-up upper bound of p + q * 2^e), must strictly contain the
+// fp64 box of the binary node it stands for, and the BVH8 leaves must be exactly
+// the binary tree's leaves.
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <random>
+#include <vector>
+
+#include "bc_host_scene.h"
+#include "pack.h"
+
+using namespace bcgx;
+
+static float rd(double x) { return round_down_f32(x); }
+static float ru(double x) { return round_up_f32(x); }
+
+static int check_scene(bc_hscene* s) {
+  bc_scene_desc d;
+  if (bc_hscene_describe(s, &d) != BC_OK) return 1;
+  PackedScene ps;
+  std::string err;
+  if (pack_scene(d, &ps, &err) != BC_OK) { std::printf("pack failed: %s\n", err.c_str()); return 1; }
+  // map leaf ref -> binary leaf box, and count leaves
+  std::map<uint32_t, int> leaf_of;
+  int binary_leaves = 0;
+  for (int i = 0; i < d.n_nodes; i++)
+    if (d.node_count[i] > 0) {
+      binary_leaves++;
+      uint32_t ref = kLeafBit | ((uint32_t)(d.node_count[i] - 1) & 0xfu) << 27 | ((uint32_t)d.node_start[i] & kSlotMask);
+      leaf_of[ref] = i;
+    }
+  int leaves = 0, bad = 0;
+  // walk BVH8 and the binary boxes in parallel: record for each Node8 child the binary node box
+  // by re-deriving the box from the referenced subtree (leaf: its box; inner: union of descendants)
+  // compute union box of each Node8 subtree bottom-up (children indices are larger than parents)
+  std::vector<std::array<double, 6>> sub(ps.nodes.size());
+  for (int i = (int)ps.nodes.size() - 1; i >= 0; i--) {
+    std::array<double, 6> u = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    const Node8& n = ps.nodes[i];
+    for (int k = 0; k < n.nchild; k++) {
+      const double* b;
+      std::array<double, 6> cb;
+      if (n.child[k] & kLeafBit) {
+        auto it = leaf_of.find(n.child[k]);
+        if (it == leaf_of.end()) { std::printf("unknown leaf ref\n"); return 1; }
+        b = d.node_box + 6 * (size_t)it->second;
+        leaves++;
+      } else {
+        cb = sub[n.child[k]];
+        b = cb.data();
+      }
+      for (int a = 0; a < 3; a++) { u[a] = std::min(u[a], b[a]); u[3 + a] = std::max(u[3 + a], b[3 + a]); }
+      const float p[3] = {n.px, n.py, n.pz};
+      const uint8_t e[3] = {n.ex, n.ey, n.ez};
+      const uint8_t ql[3] = {n.qlox[k], n.qloy[k], n.qloz[k]};
+      const uint8_t qh[3] = {n.qhix[k], n.qhiy[k], n.qhiz[k]};
+      for (int a = 0; a < 3; a++) {
+        const double sc = std::ldexp(1.0, (int)e[a] - 127);
+        const float lo = rd((double)p[a] + ql[a] * sc), hi = ru((double)p[a] + qh[a] * sc);
+        if (!((double)lo < b[a]) || !((double)hi > b[3 + a])) bad++;
+      }
+    }
+    sub[i] = u;
+  }
+  if (leaves != binary_leaves) { std::printf("leaf count %d vs binary %d\n", leaves, binary_leaves); return 1; }
+  if (bad) { std::printf("%d non-conservative child bounds\n", bad); return 1; }
+  std::printf("ok nodes=%zu leaves=%d\n", ps.nodes.size(), leaves);
+  return 0;
+}
+
+int main() {
+  std::mt19937_64 rng(12345);
+  int rc = 0;
+  for (int trial = 0; trial < 6; trial++) {
+    bc_hscene* s = bc_hscene_create();
+    double c0[3] = {0.5, 0.5, 0.5}, e0[3] = {0, 0, 0};
+    int m = bc_hscene_add_material(s, BC_MAT_DIFFUSE, c0, 0, 0, e0);
+    const double scale = trial < 2 ? 1.0 : (trial < 4 ? 1000.0 : 1e-2);
+    const double offset = trial % 2 ? 5e5 : 0.0;
+    std::uniform_real_distribution<double> U(0, 1);
+    std::lognormal_distribution<double> LN(-5, 0.5);
+    const int n = 20000;
+    std::vector<double> v(9 * n);
+    std::vector<int32_t> mats(n, m);
+    for (int t = 0; t < n; t++) {
+      double c[3] = {U(rng) * scale + offset, U(rng) * scale, U(rng) * scale};
+      for (int j = 0; j < 3; j++)
+        for (int a = 0; a < 3; a++) v[9 * t + 3 * j + a] = c[a] + (U(rng) - 0.5) * LN(rng) * scale;
+    }
+    // axis-aligned and degenerate-extent triangles
+    for (int t = 0; t < 200; t++) {
+      // axis-aligned triangles on a few shared planes (flat boxes, exact coordinates)
+      double y = std::floor(U(rng) * 8) * 0.125 * scale;
+      double x = offset + std::floor(U(rng) * 64) / 64 * scale, z = std::floor(U(rng) * 64) / 64 * scale;
+      double tri[9] = {x, y, z, x + scale * 0.01, y, z, x, y, z + scale * 0.01};
+      std::memcpy(&v[9 * t], tri, sizeof(tri));
+    }
+    bc_hscene_add_triangles(s, n, v.data(), mats.data());
+    for (int k = 0; k < 50; k++) {
+      double c[3] = {U(rng) * scale + offset, U(rng) * scale, U(rng) * scale};
+      bc_hscene_add_sphere(s, c, 0.01 * scale, m);
+    }
+    bc_hscene_set_bvh(s, trial % 3 == 0 ? "Median" : "SAH", 32, 1 + trial);
+    bc_hscene_build(s);
+    rc |= check_scene(s);
+    bc_hscene_destroy(s);
+  }
+  return rc;
+}

@@ -1,0 +1,24 @@
+"""Host checks of the device scene packer (no GPU): quantized BVH8 child boxes
+are strictly conservative and the BVH8 leaves are the binary tree's leaves."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+from conftest import PKG_DIR, ROOT
+
+
+def test_quantized_nodes_conservative(tmp_path):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    exe = tmp_path / "pack_check"
+    csrc = os.path.join(PKG_DIR, "csrc")
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I" + csrc, "-I" + os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "native", "pack_check.cpp"), os.path.join(csrc, "pack.cpp"),
+           os.path.join(csrc, "host_scene.cpp"), "-o", str(exe)]
+    subprocess.run(cmd, check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.count("ok nodes=") == 6

@@ -236,3 +236,94 @@ def stress_scene() -> tuple[SceneSpec, Camera]:
             sp.sphere((float(x) * .58, -.65, -3 - float(z) * .58), .22, blue)
     sp.sphere((0, 8, -8), 1.2, light)
     return sp, Camera((9, 5, 8), (0, -.5, -8), (0, 1, 0), 42)
+
+
+# ---------------------------------------------------------------------------
+# Workload 3: Ultra-Realism-shaped frame.
+def _icosahedron():
+    t = (1.0 + 5 ** 0.5) / 2.0
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], dtype=np.float64)
+    f = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2],
+                  [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5],
+                  [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]])
+    return v / np.linalg.norm(v, axis=1, keepdims=True), f
+
+
+def geodesic_sphere(freq: int = 5) -> np.ndarray:
+    """Unit geodesic sphere: each icosahedron face split into freq^2 triangles, (20 freq^2, 3, 3)."""
+    v, f = _icosahedron()
+    tris = []
+    for a, b, c in f:
+        A, B, C = v[a], v[b], v[c]
+
+        def P(i, j):  # barycentric grid point i along AB, j along AC
+            p = A + (B - A) * (i / freq) + (C - A) * (j / freq)
+            return p / np.linalg.norm(p)
+        for i in range(freq):
+            for j in range(freq - i):
+                tris.append([P(i, j), P(i + 1, j), P(i, j + 1)])
+                if i + j < freq - 1:
+                    tris.append([P(i + 1, j), P(i + 1, j + 1), P(i, j + 1)])
+    return np.array(tris)
+
+
+def _value_noise(p: np.ndarray, seed: int) -> np.ndarray:
+    """Seeded trilinear value noise in [-1, 1] on an integer lattice (period 64)."""
+    rng = np.random.default_rng(seed)
+    lat = rng.uniform(-1, 1, size=(64, 64, 64))
+    q = np.floor(p).astype(np.int64)
+    f = p - q
+    s = f * f * (3 - 2 * f)
+    out = np.zeros(len(p))
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                w = ((s[:, 0] if dx else 1 - s[:, 0]) * (s[:, 1] if dy else 1 - s[:, 1]) *
+                     (s[:, 2] if dz else 1 - s[:, 2]))
+                out += w * lat[(q[:, 0] + dx) % 64, (q[:, 1] + dy) % 64, (q[:, 2] + dz) % 64]
+    return out
+
+
+def icosphere_grid(seed: int = SEED_C3, n: int = 64, freq: int = 5, spacing: float = 1.0, radius: float = 0.4,
+                   amplitude: float = 0.05, n_lights: int = 64) -> tuple[SceneSpec, Camera, RenderSettings]:
+    """n x n displaced icospheres (20 freq^2 triangles each), a ground quad and n_lights
+    emissive quads with LogNormal(1, 1) luminance; spheres are 50% diffuse
+    (albedo U[0.2, 0.8]^3) and 50% rough metal (roughness U[0.05, 1]: the
+    reference has no GGX material, its metal fuzz stands in)."""
+    rng = np.random.default_rng(seed)
+    sp = SceneSpec(name=f"icosphere-grid-{n}x{n}", bvh_mode="SAH", bvh_bins=32, bvh_leaf=4)
+    base = geodesic_sphere(freq)                       # (T, 3, 3) on the unit sphere
+    uniq, inv = np.unique(np.round(base.reshape(-1, 3), 12), axis=0, return_inverse=True)
+    inv = inv.reshape(-1)
+    ground = sp.material(Material(MAT_DIFFUSE, (0.45, 0.45, 0.45)))
+    ext = n * spacing
+    sp.triangles(quad((-1, 0, -1), (-1, 0, ext + 1), (ext + 1, 0, ext + 1), (ext + 1, 0, -1)), ground)
+    mats = []
+    for k in range(n * n):
+        if rng.random() < 0.5:
+            mats.append(sp.material(Material(MAT_DIFFUSE, tuple(rng.uniform(0.2, 0.8, 3)))))
+        else:
+            mats.append(sp.material(Material(MAT_METAL, tuple(rng.uniform(0.5, 0.95, 3)),
+                                             roughness=float(rng.uniform(0.05, 1.0)))))
+    verts = np.empty((n * n, len(base), 9))
+    for k in range(n * n):
+        cx, cz = (k % n + 0.5) * spacing, (k // n + 0.5) * spacing
+        center = np.array([cx, radius + amplitude, cz])
+        disp = _value_noise(uniq * 3.0 + np.array([k % 61, k // 61, 7.0]), seed) * amplitude
+        pts = center + uniq * (radius + disp)[:, None]
+        verts[k] = pts[inv].reshape(-1, 9)
+    sp.triangles(verts.reshape(-1, 9), np.repeat(np.array(mats, dtype=np.int32), len(base)))
+    for k in range(n_lights):
+        lum = rng.lognormal(1.0, 1.0)
+        tint = rng.uniform(0.6, 1.0, 3)
+        em = tuple(tint / (0.2126 * tint[0] + 0.7152 * tint[1] + 0.0722 * tint[2]) * lum)
+        m = sp.material(Material(MAT_EMISSIVE, emission=em))
+        x, z = rng.uniform(0, ext, 2)
+        s, y = rng.uniform(0.5, 1.5), rng.uniform(2.5, 4.0)
+        sp.triangles(quad((x, y, z), (x + s, y, z), (x + s, y, z + s), (x, y, z + s)), m)
+    cam = Camera((ext * 0.5, ext * 0.35, -ext * 0.25), (ext * 0.5, 0.0, ext * 0.45), (0, 1, 0), 50.0)
+    st = quality("Ultra Realism")
+    st.adaptive_sampling = False  # equal spp, as the reference's own benchmark recipe (benchmark.go:82)
+    st.progressive_updates = False
+    return sp, cam, st

@@ -84,9 +84,10 @@ __device__ __forceinline__ int warp_reserve(int* counter, bool pred) {
 
 // ---- generate --------------------------------------------------------------
 __global__ void k_generate(WaveParams wp, PathSoA ps, int* __restrict__ queue, const double* __restrict__ seqX,
-                           const double* __restrict__ seqY, uint32_t* __restrict__ guide_jit) {
+                           const double* __restrict__ seqY, uint32_t* __restrict__ guide_jit, WaveCounters* cnt) {
   const int n = wp.npix * wp.S;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) cnt->q[0] = n;  // the first bounce's queue holds every path of the wave
   if (i >= n) return;
   const int p = i % wp.npix, sl = i / wp.npix;
   const int x = p % wp.W, y = wp.y0 + p / wp.W;
@@ -125,24 +126,46 @@ __global__ void k_generate(WaveParams wp, PathSoA ps, int* __restrict__ queue, c
 }
 
 // ---- extend ----------------------------------------------------------------
+// Persistent: a lane whose ray is done takes the next queue entry at once (one
+// atomic per warp for all lanes that need work).
 template <int STACK, bool SPH>
 __global__ void __launch_bounds__(128) k_extend(SceneView sv, PathSoA ps, const int* __restrict__ queue,
                                                 WaveCounters* cnt, int cur, unsigned* status) {
   const int n = *((volatile int*)&cnt->q[cur]);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->rays, (unsigned long long)n);
   const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  int path = -1;
+  bool exhausted = false;
+  Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
+  FastClosestLeaf<SPH> leaf(sv, r, 1e30f);
+  Walker<STACK> w;
+  w.reset();
   for (;;) {
-    int base = 0;
-    if (lane == 0) base = atomicAdd(&cnt->work_ext, 32);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= n) break;
-    const int idx = base + (int)lane;
-    if (idx < n) {
-      const int path = queue[idx];
-      const Ray32 r = make_ray(ps.ox[path], ps.oy[path], ps.oz[path], ps.dx[path], ps.dy[path], ps.dz[path], 1e-4f);
-      const HitResult h = closest_hit_fast<STACK, SPH>(sv, r, 1e30f, status);
-      ps.hit_t[path] = h.t32;
-      ps.hit_slot[path] = h.slot;
+    const bool need = path < 0 && !exhausted;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      int base = 0;
+      if ((int)lane == leader) base = atomicAdd(&cnt->work_ext, __popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const int my = base + __popc(m & below);
+        if (my < n) {
+          path = queue[my];
+          r = make_ray(ps.ox[path], ps.oy[path], ps.oz[path], ps.dx[path], ps.dy[path], ps.dz[path], 1e-4f);
+          leaf.reset(1e30f);
+          w.reset();
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, path >= 0)) break;
+    if (path >= 0 && w.step(sv, r, leaf, status)) {
+      ps.hit_t[path] = leaf.best_t;
+      ps.hit_slot[path] = leaf.best_slot;
+      path = -1;
     }
   }
 }
@@ -375,22 +398,44 @@ __global__ void __launch_bounds__(128) k_connect(SceneView sv, PathSoA ps, Shado
   const int n = *((volatile int*)&cnt->shadow);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->shadow_rays, (unsigned long long)n);
   const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  int i = -1;
+  bool exhausted = false;
+  Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
+  FastAnyLeaf<SPH> leaf(sv, r, 0.0f);
+  Walker<STACK> w;
+  w.reset();
   for (;;) {
-    int base = 0;
-    if (lane == 0) base = atomicAdd(&cnt->work_con, 32);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= n) break;
-    const int i = base + (int)lane;
-    if (i < n) {
-      const float4 o = sh.o[i], d = sh.d[i];
-      const Ray32 r = make_ray(o.x, o.y, o.z, d.x, d.y, d.z, 1e-4f);
-      if (!any_hit_fast<STACK, SPH>(sv, r, o.w, status)) {
+    const bool need = i < 0 && !exhausted;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      int base = 0;
+      if ((int)lane == leader) base = atomicAdd(&cnt->work_con, __popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const int my = base + __popc(m & below);
+        if (my < n) {
+          i = my;
+          const float4 o = sh.o[i], d = sh.d[i];
+          r = make_ray(o.x, o.y, o.z, d.x, d.y, d.z, 1e-4f);
+          leaf.reset(o.w);
+          w.reset();
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, i >= 0)) break;
+    if (i >= 0 && w.step(sv, r, leaf, status)) {
+      if (!leaf.done) {  // no occluder: the light sample counts
         const int path = sh.path[i];
         const float4 c = sh.c[i];
         ps.lx[path] += c.x;
         ps.ly[path] += c.y;
         ps.lz[path] += c.z;
       }
+      i = -1;
     }
   }
 }
@@ -631,9 +676,12 @@ static cudaError_t launch_bounce(bc_context* ctx, const WaveParams& wp, const Sh
   e = cudaMemsetAsync(&c->shadow, 0, sizeof(int), st);
   if (e) return e;
   k_extend<STACK, SPH><<<ext_grid, 128, 0, st>>>(sc.sv, rb->ps, rb->q[cur], c, cur, ctx->d_status);
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
   k_shade<<<sms * 8, 256, 0, st>>>(wp, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1], rb->sh, c, cur, bounce, rb->guide_nd,
                                    rb->guide_c, rb->guide_jit);
   if (wp.n_lights > 0)
@@ -647,9 +695,8 @@ static cudaError_t run_wave(bc_context* ctx, const WaveParams& wp, const ShadeSc
   cudaStream_t st = ctx->stream;
   const int n = wp.npix * wp.S;
   WaveCounters* c = rb->cnt;
-  cudaError_t e = cudaMemcpyAsync(&c->q[0], &n, sizeof(int), cudaMemcpyHostToDevice, st);
-  if (e) return e;
-  k_generate<<<(n + 255) / 256, 256, 0, st>>>(wp, rb->ps, rb->q[0], rb->seqX, rb->seqY, rb->guide_jit);
+  cudaError_t e = cudaSuccess;
+  k_generate<<<(n + 255) / 256, 256, 0, st>>>(wp, rb->ps, rb->q[0], rb->seqX, rb->seqY, rb->guide_jit, c);
   int cur = 0;
   for (int b = 0; b < wp.bounces; b++) {
     e = launch_bounce<STACK, SPH>(ctx, wp, sc, b, cur);

@@ -46,8 +46,12 @@ __device__ __forceinline__ Ray32 make_ray(float ox, float oy, float oz, float dx
   return r;
 }
 
-// Conservative limit for box culling against the current closest distance.
-__device__ __forceinline__ float widen(float t) { return fmaf(fabsf(t), kFarSlack, t); }
+// Moves a far distance away from zero by the slack (conservative box test and
+// culling bound). Infinities stay infinite: a slab whose far distance is -inf
+// (a zero direction component with the box entirely to one side) must still
+// reject the box; fma(|t|, slack, t) would turn -inf into NaN, which fminf
+// ignores, and the box would be entered.
+__device__ __forceinline__ float widen(float t) { return t * (t >= 0.0f ? 1.0f + kFarSlack : 1.0f - kFarSlack); }
 
 // Slab test of one child box; returns the entry distance or +inf on a miss.
 __device__ __forceinline__ float slab_near(float lox, float hix, float loy, float hiy, float loz, float hiz,
@@ -673,6 +677,11 @@ struct FastAnyLeaf {
   bool done;
   __device__ FastAnyLeaf(const SceneView& s, const Ray32& ray, float tm)
       : sv(s), r(ray), tmax(tm), tlim(widen(tm)), done(false) {}
+  __device__ __forceinline__ void reset(float tm) {
+    tmax = tm;
+    tlim = widen(tm);
+    done = false;
+  }
   __device__ __forceinline__ void operator()(uint32_t ref) {
     const int cnt = (int)((ref >> 27) & 15u) + 1;
     const int s0 = (int)(ref & kSlotMask);

@@ -293,6 +293,78 @@ def run_gpu(args):
     return 0
 
 
+def run_render(args):
+    """Render workloads (one JSON line each): `cornell` = the Cornell-box
+    configuration (320x240, 16 spp, 5 bounces, RR from 3, Halton, MIS, power
+    lights); `ultra` = the Ultra-Realism-shaped frame (2560x1440, 256 spp,
+    16 bounces, RR from 6, 2,048,130 triangles, denoise 3 passes, bloom, ACES).
+    value = extension rays (path segments) / device-resident frame time (no
+    readback); e2e = the same frame with the linear image and RGBA8 read back."""
+    import numpy as np
+    import bcgx
+    from bcgx import scenes
+    if args.workload == "cornell":
+        spec, cam, st = scenes.cornell_box()
+        workload = "cornell box: 36 tris, 320x240, 16 spp, 5 bounces, RR from bounce 3, Halton, MIS, power lights"
+    else:
+        spec, cam, st = scenes.icosphere_grid()
+        workload = ("ultra-realism shape: 2,048,130 tris (64x64 displaced icospheres + ground + 64 emissive quads), "
+                    "2560x1440, 256 spp, 16 bounces, RR from bounce 6, denoise x3, bloom 1, ACES")
+    if args.spp:
+        st.spp = args.spp
+    scene = scenes.to_scene(spec)
+    ctx = bcgx.Context(0)
+    ctx.upload(scene)
+    L = bcgx.lib()
+    import ctypes as C
+    cc, sc = cam.c(), st.c()
+
+    def frame(readback):
+        rays = C.c_int64(0)
+        W, H = st.width, st.height
+        lin = np.empty((H, W, 3), np.float32) if readback else None
+        rgba = np.empty((H, W), np.uint32) if readback else None
+        t0 = time.perf_counter()
+        bcgx._lib.check(L.bc_render_frame(ctx.handle, C.byref(cc), C.byref(sc), bcgx._lib.ptr(lin, C.c_float), None,
+                                          bcgx._lib.ptr(rgba, C.c_uint32), C.byref(rays)), ctx.handle)
+        return time.perf_counter() - t0, rays.value, lin
+
+    for _ in range(args.warmup):
+        frame(False)
+    clocks = ClockSampler(0)
+    clocks.start()
+    times, rays = [], 0
+    for _ in range(args.steps):
+        dt, r, _ = frame(False)
+        times.append(dt)
+        rays += r
+    e2e_t, e2e_r, lin = frame(True)
+    clk = clocks.stop()
+    value = rays / sum(times) / 1e6
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (fp64 primary rays)", "data": "synthetic, seeded",
+            "config": {"workload": workload, "spp": st.spp, "segments_per_frame": rays // max(1, args.steps)},
+            "e2e": {"value": e2e_r / e2e_t / 1e6, "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": st.width * st.height * 16},
+            "gpu_launches": None, "clocks": clk}
+    if not args.no_cpu_baseline:
+        import oracle
+        ref = oracle.OracleScene.from_spec(spec)
+        cst = st.copy()
+        if args.workload == "ultra":  # bounded sample: the same camera at 1/16 of the pixels, 4 spp
+            cst.width, cst.height, cst.spp = st.width // 4, st.height // 4, 4
+        t0 = time.perf_counter()
+        out = ref.render(cam, cst, seed=7, threads=0)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": out["stats"]["segments"] / dt / 1e6, "unit": METRIC,
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{cst.width}x{cst.height} at {cst.spp} spp, {dt:.1f} s"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     global N_TRIS, N_RAYS
     ap = argparse.ArgumentParser()
@@ -305,12 +377,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
     ap.add_argument("--minblocks", type=int, default=0, help="ray-cast register variant (1, 6, 8; 0 = library default)")
     ap.add_argument("--fast", action="store_true", help="plain fp32 closest hit instead of the exact contract")
+    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra"],
+                    help="raycast (default, the headline line) or a render workload")
+    ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
     args = ap.parse_args()
     N_TRIS, N_RAYS = args.tris, args.rays
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "raycast":
+        return run_render(args)
     return run_gpu(args)
 
 

@@ -49,6 +49,10 @@ class SettingsC(C.Structure):
     ]
 
 
+class ViewC(C.Structure):
+    _fields_ = [("scene", C.c_int32), ("reserved", C.c_int32), ("camera", CameraC), ("settings", SettingsC)]
+
+
 # (name, restype, argtypes) for every exported symbol of the two headers.
 SIGNATURES = [
     ("bc_gpu_available", C.c_int, [C.c_char_p, C.c_size_t]),
@@ -57,6 +61,7 @@ SIGNATURES = [
     ("bc_last_error", C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     ("bc_device_name", C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     ("bc_scene_upload", C.c_int, [C.c_void_p, P(SceneDesc), C.c_uint64, C.c_uint64, C.c_uint64]),
+    ("bc_scene_set_upload", C.c_int, [C.c_void_p, P(SceneDesc), C.c_int32, C.c_uint64, C.c_uint64]),
     ("bc_scene_stats", C.c_int, [C.c_void_p, i64p, C.c_int]),
     ("bc_raycast", C.c_int, [C.c_void_p, f32p, C.c_int64, f32p, i32p]),
     ("bc_raycast_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -65,6 +70,7 @@ SIGNATURES = [
     ("bc_render_rows", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), C.c_int32, C.c_int32, f32p, u32p, i64p]),
     ("bc_render_frame", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, u32p, u32p, i64p]),
     ("bc_render_moments", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, f32p, i64p]),
+    ("bc_render_batch", C.c_int, [C.c_void_p, P(ViewC), C.c_int32, P(f32p), i64p]),
     ("bc_post_process", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, f32p, f32p, P(SettingsC), f32p, u32p]),
     ("bc_post_process_noalloc", C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, P(SettingsC), C.c_void_p,
                                           C.c_void_p, C.c_void_p]),

@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import check, lib, ptr
+from ._lib import SceneDesc, ViewC, check, lib, ptr
 from .scene import Scene, SceneArrays
 from .settings import Camera, RenderSettings
 
@@ -73,6 +73,18 @@ class Context:
         g = g if geometry_rev is None else geometry_rev
         check(lib().bc_scene_upload(self._h, C.byref(d), sid, t, g), self._h)
         self._desc_keep = scene
+
+    def upload_set(self, scenes, set_id: int | None = None, revision: int = 1):
+        """Resident scene set for render_batch: scenes[k] is scene k of the set."""
+        descs = []
+        for sc in scenes:
+            if not isinstance(sc, (Scene, SceneArrays)):
+                raise TypeError("scenes must be Scene or SceneArrays objects")
+            descs.append(sc.desc())
+        arr = (SceneDesc * len(descs))(*descs)
+        sid = id(scenes) if set_id is None else set_id
+        check(lib().bc_scene_set_upload(self._h, arr, len(descs), sid, revision), self._h)
+        self._desc_keep = list(scenes)
 
     def scene_stats(self) -> dict:
         out = (C.c_int64 * 6)()
@@ -139,6 +151,25 @@ class Context:
         check(lib().bc_render_moments(self._h, C.byref(cc), C.byref(sc), ptr(mean, C.c_float), ptr(msq, C.c_float),
                                       C.byref(rays)), self._h)
         return mean, msq, rays.value
+
+    def render_batch(self, views, readback: bool = True):
+        """views: list of (scene_index, Camera, RenderSettings) over the resident set.
+        Returns ([linear (H, W, 3)] or None per view, extension rays)."""
+        n = len(views)
+        vc = (ViewC * n)()
+        outs = []
+        ptrs = (C.POINTER(C.c_float) * n)()
+        for i, (k, cam, st) in enumerate(views):
+            vc[i].scene = int(k)
+            vc[i].reserved = 0
+            vc[i].camera = cam.c()
+            vc[i].settings = st.c()
+            o = np.empty((st.height, st.width, 3), dtype=np.float32) if readback else None
+            outs.append(o)
+            ptrs[i] = ptr(o, C.c_float)
+        rays = C.c_int64(0)
+        check(lib().bc_render_batch(self._h, vc, n, ptrs if readback else None, C.byref(rays)), self._h)
+        return outs, rays.value
 
     def post_process(self, linear: np.ndarray, guide_nd: np.ndarray | None, settings: RenderSettings,
                      want_rgba: bool = True):

@@ -12,6 +12,10 @@ checker. Seeds and shapes:
   random_rays      origins U[0,1]^3, directions uniform on the sphere.
   icosphere_grid   seed 0xBEAC0003: 64 x 64 displaced frequency-5 icospheres
                    (500 tris each), ground quad, 64 emissive quads.
+  batch_views      seed 0xBEAC0004: 4 random-triangle scenes (10k / 50k / 200k /
+                   500k tris, one emissive quad each) and 64 views with
+                   log-uniform sizes 128x128 .. 1920x1080, spp U{4..64},
+                   8 bounces, cameras orbiting the unit cube.
 The reference's own scenes (renderer.go:2944-2994) are test inputs only.
 """
 from __future__ import annotations
@@ -327,3 +331,44 @@ def icosphere_grid(seed: int = SEED_C3, n: int = 64, freq: int = 5, spacing: flo
     st.adaptive_sampling = False  # equal spp, as the reference's own benchmark recipe (benchmark.go:82)
     st.progressive_updates = False
     return sp, cam, st
+
+
+# ---------------------------------------------------------------------------
+# Workload 4: many views over a resident scene set.
+def batch_scene(n_tris: int, seed: int) -> SceneSpec:
+    """The random-triangle generator in the unit cube, plus one emissive quad above it."""
+    sp = SceneSpec(name=f"batch-tris-{n_tris}", bvh_mode="SAH", bvh_bins=32, bvh_leaf=4)
+    m = sp.material(Material(MAT_DIFFUSE, (0.7, 0.7, 0.7)))
+    sp.triangles(random_triangle_verts(n_tris, seed), m)
+    e = sp.material(Material(MAT_EMISSIVE, emission=(8.0, 7.0, 6.0)))
+    sp.triangles(quad((0.25, 1.3, 0.25), (0.75, 1.3, 0.25), (0.75, 1.3, 0.75), (0.25, 1.3, 0.75)), e)
+    return sp
+
+
+def batch_views(seed: int = SEED_C4, n_views: int = 64, sizes=(10_000, 50_000, 200_000, 500_000),
+                max_side: tuple[int, int] = (1920, 1080), spp_range: tuple[int, int] = (4, 64), bounces: int = 8):
+    """Scenes and views of the batching workload: view v renders scene v mod len(sizes)
+    at W = round(128 * r_w^t), H = round(128 * r_h^t), t ~ U[0, 1] (log-uniform from
+    128 x 128 up to max_side), spp ~ U{spp_range}, from a seeded orbit camera."""
+    rng = np.random.default_rng(seed)
+    specs = [batch_scene(n, seed + 1 + k) for k, n in enumerate(sizes)]
+    rw, rh = max_side[0] / 128.0, max_side[1] / 128.0
+    views = []
+    for v in range(n_views):
+        t = rng.uniform()
+        W, H = int(round(128 * rw ** t)), int(round(128 * rh ** t))
+        spp = int(rng.integers(spp_range[0], spp_range[1] + 1))
+        az, el = rng.uniform(0, 2 * np.pi), rng.uniform(0.1, 0.6)
+        dist = rng.uniform(1.8, 2.6)
+        c = np.array([0.5, 0.5, 0.5])
+        pos = c + dist * np.array([np.cos(el) * np.cos(az), np.sin(el), np.cos(el) * np.sin(az)])
+        cam = Camera(tuple(pos), tuple(c), (0, 1, 0), 45.0)
+        st = quality("Draft")
+        st.width, st.height, st.spp, st.bounces = W, H, spp, bounces
+        st.msaa, st.tsaa = 1, 0
+        st.sampler, st.mis, st.power_light_sampling = "Halton", True, True
+        st.firefly_clamp, st.rr_depth, st.adaptive_sampling = 0.0, 4, False
+        st.denoise, st.bloom = False, 0
+        st.seed = seed + 0x100 + v
+        views.append((v % len(sizes), cam, st))
+    return specs, views

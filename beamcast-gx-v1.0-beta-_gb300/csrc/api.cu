@@ -154,16 +154,12 @@ bc_status bc_device_name(const bc_context* ctx, char* buf, size_t len) {
   return BC_OK;
 }
 
-bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t scene_id, uint64_t topology_rev,
-                          uint64_t geometry_rev) {
-  if (!ctx || !scene) return set_error(ctx, BC_ERR_INVALID_ARG, "NULL context or scene");
-  if (ctx->has_scene && ctx->scene_id == scene_id && ctx->topo_rev == topology_rev && ctx->geom_rev == geometry_rev)
-    return BC_OK;
-  cudaSetDevice(ctx->device);
-  PackedScene ps;
-  std::string err;
-  bc_status st = pack_scene(*scene, &ps, &err);
-  if (st != BC_OK) return set_error(ctx, st, err);
+}  // extern "C"
+
+namespace bcgx {
+
+// Makes `ps` the resident scene set.
+static bc_status install_scene(bc_context* ctx, const PackedScene& ps, const std::vector<SceneRange>& ranges) {
   if (stack_variant(ps.stack_need) == 0)
     return set_error(ctx, BC_ERR_BAD_SCENE,
                      "BVH too deep for the compiled traversal stack (needs " + std::to_string(ps.stack_need) + ")");
@@ -171,7 +167,9 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_status(ctx, e, "scene upload");
   ctx->has_scene = false;
+  ctx->ranges.clear();
   const size_t slots = (size_t)ps.n_prims;
+  bc_status st;
   if ((st = upload(ctx, ctx->d_nodes, ps.nodes.data(), ps.nodes.size() * sizeof(Node8), "BVH8 upload")) ||
       (st = upload(ctx, ctx->d_tri, ps.tri.data(), ps.tri.size() * sizeof(F4), "primitive upload")) ||
       (st = upload(ctx, ctx->d_slot64, ps.slot64.data(), ps.slot64.size() * sizeof(double), "fp64 upload")) ||
@@ -182,7 +180,7 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
       (st = upload(ctx, ctx->d_lpdf, ps.light_pdf_by_prim.data(), ps.light_pdf_by_prim.size() * sizeof(float),
                    "light pdf upload")))
     return st;
-  // The host arrays of `ps` die at return: drain the copies first.
+  // The host arrays of `ps` may die once this returns: drain the copies first.
   e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_status(ctx, e, "scene upload");
   DeviceScene& ds = ctx->ds;
@@ -195,7 +193,7 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
   ds.lights = ctx->d_lights.as<LightGPU>();
   ds.light_pdf_by_prim = ctx->d_lpdf.as<float>();
   ds.n_mats = (int32_t)ps.mats.size();
-  ds.n_lights = (int32_t)ps.lights.size();
+  ds.n_lights = ranges.empty() ? 0 : ranges[0].n_lights;  // the single-view calls see scene 0
   ds.n_prims = ps.n_prims;
   ds.stack_need = ps.stack_need;
   ds.has_spheres = ps.has_spheres;
@@ -208,10 +206,54 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
                             ps.slot64.size() * sizeof(double) + ps.snorm.size() * sizeof(F4) +
                             slots * sizeof(int32_t) + ps.mats.size() * sizeof(MatGPU) +
                             ps.lights.size() * sizeof(LightGPU) + ps.light_pdf_by_prim.size() * sizeof(float));
+  ctx->ranges = ranges;
   ctx->has_scene = true;
+  return BC_OK;
+}
+
+}  // namespace bcgx
+
+extern "C" {
+
+bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t scene_id, uint64_t topology_rev,
+                          uint64_t geometry_rev) {
+  if (!ctx || !scene) return set_error(ctx, BC_ERR_INVALID_ARG, "NULL context or scene");
+  if (ctx->has_scene && !ctx->is_set && ctx->scene_id == scene_id && ctx->topo_rev == topology_rev &&
+      ctx->geom_rev == geometry_rev)
+    return BC_OK;
+  cudaSetDevice(ctx->device);
+  PackedScene ps;
+  std::string err;
+  bc_status st = pack_scene(*scene, &ps, &err);
+  if (st != BC_OK) return set_error(ctx, st, err);
+  SceneRange r;
+  r.n_lights = (int32_t)ps.lights.size();
+  r.n_slots = ps.n_prims;
+  if ((st = install_scene(ctx, ps, std::vector<SceneRange>{r}))) return st;
+  ctx->is_set = false;
   ctx->scene_id = scene_id;
   ctx->topo_rev = topology_rev;
   ctx->geom_rev = geometry_rev;
+  return BC_OK;
+}
+
+bc_status bc_scene_set_upload(bc_context* ctx, const bc_scene_desc* scenes, int32_t n_scenes, uint64_t set_id,
+                              uint64_t revision) {
+  if (!ctx || !scenes || n_scenes < 1) return set_error(ctx, BC_ERR_INVALID_ARG, "NULL argument or empty set");
+  if (ctx->has_scene && ctx->is_set && ctx->scene_id == set_id && ctx->geom_rev == revision &&
+      (int32_t)ctx->ranges.size() == n_scenes)
+    return BC_OK;
+  cudaSetDevice(ctx->device);
+  PackedScene ps;
+  std::vector<SceneRange> ranges;
+  std::string err;
+  bc_status st = pack_scene_set(scenes, n_scenes, &ps, &ranges, &err);
+  if (st != BC_OK) return set_error(ctx, st, err);
+  if ((st = install_scene(ctx, ps, ranges))) return st;
+  ctx->is_set = true;
+  ctx->scene_id = set_id;
+  ctx->topo_rev = 0;
+  ctx->geom_rev = revision;
   return BC_OK;
 }
 
@@ -319,6 +361,17 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     ctx->raycast_variant = value ? ctx->raycast_minblocks : 0;
     return BC_OK;
   }
+  if (n == "render_wave_cap") {
+    if (value < 4096 || value > (1 << 25))
+      return set_error(ctx, BC_ERR_INVALID_ARG, "render_wave_cap must be in [4096, 2^25]");
+    ctx->render_wave_cap = (long long)value;
+    return BC_OK;
+  }
+  if (n == "render_graph") {
+    if (value != 0 && value != 1) return set_error(ctx, BC_ERR_INVALID_ARG, "render_graph must be 0 or 1");
+    ctx->render_graph = (int)value;
+    return BC_OK;
+  }
   return set_error(ctx, BC_ERR_INVALID_ARG, "unknown option " + n);
 }
 
@@ -327,6 +380,8 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
   const std::string n(name);
   if (n == "raycast_minblocks") { *value = ctx->raycast_minblocks; return BC_OK; }
   if (n == "raycast_exact") { *value = ctx->raycast_exact; return BC_OK; }
+  if (n == "render_wave_cap") { *value = ctx->render_wave_cap; return BC_OK; }
+  if (n == "render_graph") { *value = ctx->render_graph; return BC_OK; }
   return BC_ERR_INVALID_ARG;
 }
 

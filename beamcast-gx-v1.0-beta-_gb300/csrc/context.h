@@ -4,6 +4,7 @@
 
 #include <atomic>
 #include <string>
+#include <vector>
 
 #include "../../include/bc_gx.h"
 #include "kernels.h"
@@ -66,6 +67,8 @@ struct bc_context {
   uint64_t scene_id = 0, topo_rev = 0, geom_rev = 0;
   bcgx::DeviceScene ds;
   bcgx::DevBuf d_nodes, d_tri, d_slot64, d_snorm, d_slot_prim, d_mats, d_lights, d_lpdf;
+  std::vector<bcgx::SceneRange> ranges;  // scenes of the resident set (one for bc_scene_upload)
+  bool is_set = false;                    // resident scenes came from bc_scene_set_upload
   int64_t stats[6] = {0, 0, 0, 0, 0, 0};
   int raycast_minblocks = 6;  // register budget of the exact ray-cast kernels (bc_set_option)
   int raycast_exact = 1;      // 0: plain fp32 closest hit (bc_set_option "raycast_exact")
@@ -76,6 +79,8 @@ struct bc_context {
   // work counters of the persistent ray-cast kernels: [0], [1] the two streams of
   // bc_raycast, [2] bc_raycast_device
   unsigned long long* d_work = nullptr;
+  long long render_wave_cap = 1 << 22;  // paths per wave (bc_set_option "render_wave_cap")
+  int render_graph = 1;                 // replay a captured wave graph (bc_set_option "render_graph")
   // rendering state (render.cu)
   struct RenderBuffers* rb = nullptr;
   std::atomic<int> cancel{0};

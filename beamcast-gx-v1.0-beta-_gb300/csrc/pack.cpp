@@ -313,6 +313,68 @@ bc_status pack_scene(const bc_scene_desc& d, PackedScene* out, std::string* err)
   return BC_OK;
 }
 
+bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::vector<SceneRange>* ranges,
+                         std::string* err) {
+  if (n < 1 || !d) {
+    if (err) *err = "a scene set needs at least one scene";
+    return BC_ERR_INVALID_ARG;
+  }
+  *out = PackedScene();
+  ranges->assign(n, SceneRange());
+  for (int k = 0; k < n; k++) {
+    PackedScene ps;
+    bc_status st = pack_scene(d[k], &ps, err);
+    if (st != BC_OK) {
+      if (err) *err = "scene " + std::to_string(k) + ": " + *err;
+      return st;
+    }
+    SceneRange& r = (*ranges)[k];
+    r.root = (int32_t)out->nodes.size();
+    r.slot_off = out->n_prims;
+    r.n_slots = ps.n_prims;
+    r.prim_off = out->n_prims;  // primitive indices and slots share one numbering per scene
+    r.mat_off = (int32_t)out->mats.size();
+    r.light_off = (int32_t)out->lights.size();
+    r.n_lights = (int32_t)ps.lights.size();
+    if ((int64_t)out->nodes.size() + ps.nodes.size() >= kMaxIndex || (int64_t)out->n_prims + ps.n_prims >= kMaxIndex) {
+      if (err) *err = "scene set exceeds 2^27 nodes or primitives";
+      return BC_ERR_BAD_SCENE;
+    }
+    for (Node8 nd : ps.nodes) {
+      for (int c = 0; c < nd.nchild; c++) {
+        if (nd.child[c] & kLeafBit) nd.child[c] += (uint32_t)r.slot_off;  // start field: low 27 bits
+        else nd.child[c] += (uint32_t)r.root;
+      }
+      out->nodes.push_back(nd);
+    }
+    out->tri.insert(out->tri.end(), ps.tri.begin(), ps.tri.end());
+    out->slot64.insert(out->slot64.end(), ps.slot64.begin(), ps.slot64.end());
+    const int32_t n_mats = (int32_t)ps.mats.size();
+    for (F4 f : ps.snorm) {
+      int32_t m;
+      std::memcpy(&m, &f.w, 4);
+      // an index outside the scene's own table ends the path; keep it outside the set's
+      m = (m >= 0 && m < n_mats) ? m + r.mat_off : -1;
+      std::memcpy(&f.w, &m, 4);
+      out->snorm.push_back(f);
+    }
+    for (int32_t p : ps.slot_prim) out->slot_prim.push_back(p + r.prim_off);
+    out->mats.insert(out->mats.end(), ps.mats.begin(), ps.mats.end());
+    for (LightGPU L : ps.lights) {
+      L.prim += r.prim_off;
+      out->lights.push_back(L);
+    }
+    out->light_pdf_by_prim.insert(out->light_pdf_by_prim.end(), ps.light_pdf_by_prim.begin(),
+                                  ps.light_pdf_by_prim.end());
+    out->n_prims += ps.n_prims;
+    out->n_binary += ps.n_binary;
+    out->depth = std::max(out->depth, ps.depth);
+    out->stack_need = std::max(out->stack_need, ps.stack_need);
+    out->has_spheres = out->has_spheres || ps.has_spheres;
+  }
+  return BC_OK;
+}
+
 bc_status repack_geometry(const bc_scene_desc& d, PackedScene* io, std::string* err) {
   if (d.n_prims != io->n_prims || d.n_nodes != io->n_binary) {
     if (err) *err = "geometry update changes the topology; a full upload is required";

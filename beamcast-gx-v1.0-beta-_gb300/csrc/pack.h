@@ -25,8 +25,23 @@ struct PackedScene {
   float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
 };
 
+// One scene of a resident scene set: where its records start in the
+// concatenated arrays.
+struct SceneRange {
+  int32_t root = 0;                    // Node8 index of its root
+  int32_t light_off = 0, n_lights = 0; // its sphere lights in `lights`
+  int32_t slot_off = 0, n_slots = 0;
+  int32_t prim_off = 0;                // added to its primitive indices (slot_prim, light prims)
+  int32_t mat_off = 0;
+};
+
 // Fills `out`; returns BC_OK or BC_ERR_BAD_SCENE / BC_ERR_INVALID_ARG with a message.
 bc_status pack_scene(const bc_scene_desc& d, PackedScene* out, std::string* err);
+// Packs several scenes into one set of arrays: node references, slots,
+// materials and light primitives of scene k are offset past scenes 0..k-1, and
+// `ranges[k]` tells where each scene starts. stack_need is the maximum.
+bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::vector<SceneRange>* ranges,
+                         std::string* err);
 // Re-packs only geometry (boxes and primitive records) for an unchanged topology.
 bc_status repack_geometry(const bc_scene_desc& d, PackedScene* io, std::string* err);
 

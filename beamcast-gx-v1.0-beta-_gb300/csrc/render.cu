@@ -1,25 +1,31 @@
 // Wavefront path tracer: the reference CPU integrator (trace, renderer.go:1484-1563;
 // directLight 1427-1465; adaptivePixel's sample loop 1928-1970) as separate
-// kernels over compacted queues of path slots:
+// kernels over compacted queues of path slots, for one view or a batch of
+// views over a resident scene set:
 //
-//   generate  -> one path per (pixel, sample) of the wave: Halton jitter with the
-//                per-pixel rotation, fp64 primary ray (rounded to fp32), PCG32 stream
-//   extend    -> closest hit for every queued path (persistent warps fetch 32 rays
-//                at a time from an atomic work counter)
+//   generate  -> the wave's paths: global path index -> (view, sample, pixel);
+//                Halton jitter with the per-pixel rotation, fp64 primary ray
+//                (rounded to fp32), one PCG32 stream per (pixel, sample)
+//   extend    -> closest hit of every queued path from its view's scene root
+//                (persistent: a lane takes the next path as soon as its walk ends)
 //   shade     -> miss / emissive (MIS weight) / diffuse (NEE shadow ray + cosine
 //                bounce) / metal / glass, Russian roulette; survivors and shadow
 //                rays are pushed with warp-ballot compaction (one atomic per warp)
 //   connect   -> any hit for the shadow queue; unoccluded contributions are added
-//   accumulate-> per pixel, the firefly-clamped sample radiance summed in sample order
+//   accumulate-> per pixel, the firefly-clamped sample radiance of the wave,
+//                summed in sample order (no atomics: one thread per pixel)
+//   advance   -> moves the device-side wave start
 //
-// Path state is structure-of-arrays indexed by path slot; queues hold slot
-// indices. Waves are sample-major (slot = sample_in_wave * npix + pixel), so
-// accumulation is a deterministic per-pixel loop and every (pixel, sample)
-// draws from its own seeded stream: the image does not depend on the wave
-// split, the chunking into rows, or the launch shape.
+// Every view's paths are sample-major (path = sample * npix + pixel) in one
+// global index space; a wave is the next `cap` indices, read from device
+// memory, so the same launch sequence (or one CUDA graph of it) is replayed
+// until the batch is done. Each (pixel, sample) draws from its own seeded
+// stream, so an image does not depend on the wave split or the launch shape.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <string>
 #include <vector>
 
 #include "context.h"
@@ -38,6 +44,9 @@ struct PathSoA {
   uint32_t* flags;         // bit 0: prevWasDiffuse
   float* hit_t;
   int32_t* hit_slot;
+  int32_t* view;           // view of the path
+  int32_t* pix;            // pixel within the view's rows
+  int32_t* samp;           // sample index
 };
 
 struct ShadowSoA {
@@ -58,17 +67,31 @@ struct WaveCounters {
   unsigned long long shadow_rays;
 };
 
-struct WaveParams {
-  int W, H, y0, rows, npix;
-  int S, s0, bounces, rr_depth;
-  int mis, power, sampler, nseq;
-  int n_mats, n_lights, want_guides;
-  float clamp;
-  uint64_t seed;
+// One view of a batch (or the single view of a frame / row chunk).
+struct ViewGPU {
   double origin[3], lower[3], horiz[3], vert[3];
+  long long path_off;  // first global path index of the view
+  long long pix_off;   // first pixel of the view's rows in the frame buffers
+  int W, H, y0, rows, npix;
+  int spp, bounces, rr_depth, sampler, mis, power;
+  int nseq, seq_off;   // Halton table slice
+  int n_lights, light_off, root;
+  int want_guides;
+  float clamp;
+  int pad;
+  unsigned long long seed;
+};
+
+// Device-side wave cursor of a batch.
+struct BatchState {
+  long long w0;     // first global path index of the current wave
+  long long total;  // paths of the batch
+  int cap;          // paths per wave
+  int n_views;
 };
 
 constexpr float kPi = 3.14159265358979323846f;
+constexpr int kMaxBounces = 1024;  // a wave is one launch sequence of max(bounces) steps
 
 __device__ __forceinline__ int warp_reserve(int* counter, bool pred) {
   const unsigned lane = threadIdx.x & 31u;
@@ -82,34 +105,50 @@ __device__ __forceinline__ int warp_reserve(int* counter, bool pred) {
   return base + __popc(mask & ((1u << lane) - 1u));
 }
 
+__device__ __forceinline__ int view_of(const ViewGPU* __restrict__ views, int n_views, long long g) {
+  int lo = 0, hi = n_views - 1;  // last view with path_off <= g
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (views[mid].path_off <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 // ---- generate --------------------------------------------------------------
-__global__ void k_generate(WaveParams wp, PathSoA ps, int* __restrict__ queue, const double* __restrict__ seqX,
-                           const double* __restrict__ seqY, uint32_t* __restrict__ guide_jit, WaveCounters* cnt) {
-  const int n = wp.npix * wp.S;
+// seq: the views' sample tables, (x, y) pairs
+__global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __restrict__ views, PathSoA ps,
+                           int* __restrict__ queue, const double2* __restrict__ seq,
+                           uint32_t* __restrict__ guide_jit, WaveCounters* cnt) {
+  const long long w0 = bs->w0;
+  const int n = (int)min((long long)bs->cap, bs->total - w0);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) cnt->q[0] = n;  // the first bounce's queue holds every path of the wave
+  if (i == 0) cnt->q[0] = max(n, 0);  // the first bounce's queue holds every path of the wave
   if (i >= n) return;
-  const int p = i % wp.npix, sl = i / wp.npix;
-  const int x = p % wp.W, y = wp.y0 + p / wp.W;
-  const int s = wp.s0 + sl;
-  Pcg32 rng = make_path_rng(wp.seed, (uint64_t)y * (uint64_t)wp.W + (uint64_t)x, (uint64_t)s);
+  const long long g = w0 + i;
+  const int v = view_of(views, bs->n_views, g);
+  const ViewGPU& V = views[v];
+  const long long local = g - V.path_off;
+  const int s = (int)(local / V.npix), p = (int)(local - (long long)s * V.npix);
+  const int x = p % V.W, y = V.y0 + p / V.W;
+  Pcg32 rng = make_path_rng(V.seed, (uint64_t)y * (uint64_t)V.W + (uint64_t)x, (uint64_t)s);
   double jx, jy;
-  if (wp.sampler != BC_SAMPLER_RANDOM && s < wp.nseq) {
+  if (V.sampler != BC_SAMPLER_RANDOM && s < V.nseq) {
     double rx, ry;
     pixel_rotation(x, y, &rx, &ry);
-    double a = seqX[s] + rx, b = seqY[s] + ry;
+    const double2 q = seq[V.seq_off + s];
+    double a = q.x + rx, b = q.y + ry;
     jx = a - floor(a);
     jy = b - floor(b);
   } else {
     jx = (double)rng.uniform();
     jy = (double)rng.uniform();
   }
-  const double u = ((double)x + jx) / (double)max(wp.W - 1, 1);
-  const double v = ((double)(wp.H - 1 - y) + jy) / (double)max(wp.H - 1, 1);
+  const double u = ((double)x + jx) / (double)max(V.W - 1, 1);
+  const double vv = ((double)(V.H - 1 - y) + jy) / (double)max(V.H - 1, 1);
   float d[3];
 #pragma unroll
-  for (int k = 0; k < 3; k++) d[k] = (float)(((wp.lower[k] + wp.horiz[k] * u) + wp.vert[k] * v) - wp.origin[k]);
-  ps.ox[i] = (float)wp.origin[0]; ps.oy[i] = (float)wp.origin[1]; ps.oz[i] = (float)wp.origin[2];
+  for (int k = 0; k < 3; k++) d[k] = (float)(((V.lower[k] + V.horiz[k] * u) + V.vert[k] * vv) - V.origin[k]);
+  ps.ox[i] = (float)V.origin[0]; ps.oy[i] = (float)V.origin[1]; ps.oz[i] = (float)V.origin[2];
   ps.dx[i] = d[0]; ps.dy[i] = d[1]; ps.dz[i] = d[2];
   ps.tx[i] = 1.0f; ps.ty[i] = 1.0f; ps.tz[i] = 1.0f;
   ps.lx[i] = 0.0f; ps.ly[i] = 0.0f; ps.lz[i] = 0.0f;
@@ -117,11 +156,14 @@ __global__ void k_generate(WaveParams wp, PathSoA ps, int* __restrict__ queue, c
   ps.flags[i] = 0u;
   ps.rs[i] = rng.state;
   ps.ri[i] = rng.inc;
+  ps.view[i] = v;
+  ps.pix[i] = p;
+  ps.samp[i] = s;
   queue[i] = i;
-  if (s == 0 && wp.want_guides) {
+  if (s == 0 && V.want_guides) {
     uint32_t a = (uint32_t)rintf(fminf(fmaxf((float)jx, 0.0f), 1.0f) * 65535.0f);
     uint32_t b = (uint32_t)rintf(fminf(fmaxf((float)jy, 0.0f), 1.0f) * 65535.0f);
-    guide_jit[p] = (b << 16) | a;
+    guide_jit[V.pix_off + p] = (b << 16) | a;
   }
 }
 
@@ -129,8 +171,9 @@ __global__ void k_generate(WaveParams wp, PathSoA ps, int* __restrict__ queue, c
 // Persistent: a lane whose ray is done takes the next queue entry at once (one
 // atomic per warp for all lanes that need work).
 template <int STACK, bool SPH>
-__global__ void __launch_bounds__(128) k_extend(SceneView sv, PathSoA ps, const int* __restrict__ queue,
-                                                WaveCounters* cnt, int cur, unsigned* status) {
+__global__ void __launch_bounds__(128) k_extend(SceneView sv, const ViewGPU* __restrict__ views, PathSoA ps,
+                                                const int* __restrict__ queue, WaveCounters* cnt, int cur,
+                                                unsigned* status) {
   const int n = *((volatile int*)&cnt->q[cur]);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->rays, (unsigned long long)n);
   const unsigned lane = threadIdx.x & 31u;
@@ -155,7 +198,7 @@ __global__ void __launch_bounds__(128) k_extend(SceneView sv, PathSoA ps, const 
           path = queue[my];
           r = make_ray(ps.ox[path], ps.oy[path], ps.oz[path], ps.dx[path], ps.dy[path], ps.dz[path], 1e-4f);
           leaf.reset(1e30f);
-          w.reset();
+          w.reset(views[ps.view[path]].root);
         } else {
           exhausted = true;
         }
@@ -179,7 +222,7 @@ struct ShadeScene {
 };
 
 // lightDirectionalPDF (renderer.go:1404-1425) for a sphere light hit.
-__device__ __forceinline__ float light_dir_pdf(const ShadeScene& sc, const WaveParams& wp, int prim, float radius,
+__device__ __forceinline__ float light_dir_pdf(const ShadeScene& sc, int n_lights, int power, int prim, float radius,
                                                float3 from, float3 lp, float3 ln) {
   if (!(radius > 0.0f)) return 0.0f;
   float3 to = lp - from;
@@ -189,24 +232,25 @@ __device__ __forceinline__ float light_dir_pdf(const ShadeScene& sc, const WaveP
   float cosL = fmaxf(0.0f, dot3(ln, ld * -1.0f));
   if (cosL <= 1e-12f) return 0.0f;
   float area = 4.0f * kPi * radius * radius;
-  float sel = wp.n_lights == 0 ? 0.0f : (wp.power ? __ldg(sc.lpdf_by_prim + prim) : 1.0f / (float)wp.n_lights);
+  float sel = n_lights == 0 ? 0.0f : (power ? __ldg(sc.lpdf_by_prim + prim) : 1.0f / (float)n_lights);
   return sel * dist2 / (cosL * area);
 }
 
-__global__ void __launch_bounds__(256) k_shade(WaveParams wp, ShadeScene sc, PathSoA ps, const int* __restrict__ qcur,
-                                               int* __restrict__ qnext, ShadowSoA sh, WaveCounters* cnt, int cur,
-                                               int bounce, float4* __restrict__ guide_nd,
-                                               uint32_t* __restrict__ guide_c,
-                                               const uint32_t* __restrict__ guide_jit) {
+__global__ void __launch_bounds__(256) k_shade(const ViewGPU* __restrict__ views, int n_mats, ShadeScene sc,
+                                                 PathSoA ps, const int* __restrict__ qcur, int* __restrict__ qnext,
+                                                 ShadowSoA sh, WaveCounters* cnt, int cur, int bounce,
+                                                 float4* __restrict__ guide_nd, uint32_t* __restrict__ guide_c,
+                                                 const uint32_t* __restrict__ guide_jit) {
   const int n = *((volatile int*)&cnt->q[cur]);
   const int stride = gridDim.x * blockDim.x;
-  const int rr_depth = wp.rr_depth < 1 ? 4 : wp.rr_depth;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
     const int idx = base + threadIdx.x;
     const int path = idx < n ? qcur[idx] : -1;
     bool alive = false, shadow = false;
     float4 so = make_float4(0, 0, 0, 0), sd = so, scon = so;
     if (path >= 0) {
+      const ViewGPU& wp = views[ps.view[path]];
+      const int rr_depth = wp.rr_depth < 1 ? 4 : wp.rr_depth;
       float3 o = f3(ps.ox[path], ps.oy[path], ps.oz[path]);
       float3 d = f3(ps.dx[path], ps.dy[path], ps.dz[path]);
       float3 tp = f3(ps.tx[path], ps.ty[path], ps.tz[path]);
@@ -218,7 +262,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams wp, ShadeScene sc, Pat
       } else {
         const float4 nrm = __ldg(sc.sv.snorm + slot);
         const int m = __float_as_int(nrm.w);
-        if (m >= 0 && m < wp.n_mats) {
+        if (m >= 0 && m < n_mats) {
           Pcg32 rng;
           rng.state = ps.rs[path];
           rng.inc = ps.ri[path];
@@ -243,8 +287,9 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams wp, ShadeScene sc, Pat
           }
           const MatGPU M = sc.mats[m];
           const int kind = (int)M.kind;
-          if (bounce == 0 && wp.want_guides && wp.s0 == 0 && path < wp.npix) {
-            guide_nd[wp.y0 * wp.W + path] = make_float4(N.x, N.y, N.z, t);
+          if (bounce == 0 && wp.want_guides && ps.samp[path] == 0) {
+            const int gp = ps.pix[path];
+            guide_nd[wp.pix_off + gp] = make_float4(N.x, N.y, N.z, t);
             // compact guide (gpu_opencl_windows.go:791-797): Euclidean depth,
             // octahedral normal 10:10, material 11 bits, valid bit, jitter
             const float dl = sqrtf(dot3(d, d));
@@ -259,10 +304,10 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams wp, ShadeScene sc, Pat
             py = fminf(fmaxf(py * 0.5f + 0.5f, 0.0f), 1.0f);
             const uint32_t qx = (uint32_t)rintf(px * 1023.0f), qy = (uint32_t)rintf(py * 1023.0f);
             const uint32_t mm = (uint32_t)min(max(m, 0), 2047);
-            uint32_t* g = guide_c + 3 * (size_t)(wp.y0 * wp.W + path);
+            uint32_t* g = guide_c + 3 * (size_t)(wp.pix_off + gp);
             g[0] = __float_as_uint(t * dl);
             g[1] = 0x80000000u | (mm << 20) | (qy << 10) | qx;
-            g[2] = guide_jit[path];
+            g[2] = guide_jit[wp.pix_off + gp];
           }
           if (kind == BC_MAT_EMISSIVE) {
             float w = 1.0f;
@@ -270,7 +315,8 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams wp, ShadeScene sc, Pat
               float lpdf = 0.0f;
               if (sphere) {
                 const int prim = __ldg(sc.sv.slot_prim + slot);
-                lpdf = light_dir_pdf(sc, wp, prim, radius, f3(ps.px[path], ps.py[path], ps.pz[path]), p, N);
+                lpdf = light_dir_pdf(sc, wp.n_lights, wp.power, prim, radius,
+                                     f3(ps.px[path], ps.py[path], ps.pz[path]), p, N);
               }
               w = power_heuristic(ppdf, lpdf);
             }
@@ -290,12 +336,12 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams wp, ShadeScene sc, Pat
                   int lo = 0, hi = wp.n_lights;
                   while (lo < hi) {
                     int mid = (lo + hi) >> 1;
-                    if (!(__ldg(&sc.lights[mid].cdf) >= r)) lo = mid + 1; else hi = mid;
+                    if (!(__ldg(&sc.lights[wp.light_off + mid].cdf) >= r)) lo = mid + 1; else hi = mid;
                   }
                   li = min(lo, wp.n_lights - 1);
-                  sel = __ldg(&sc.lights[li].select_pdf);
+                  sel = __ldg(&sc.lights[wp.light_off + li].select_pdf);
                 }
-                const LightGPU Lg = sc.lights[li];
+                const LightGPU Lg = sc.lights[wp.light_off + li];
                 const float3 ln = sel > 0.0f ? rand_unit_vector(rng) : f3(0, 0, 1);
                 const float3 q = f3(Lg.cx, Lg.cy, Lg.cz) + ln * Lg.r;
                 const float3 to = q - p;
@@ -322,7 +368,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveParams wp, ShadeScene sc, Pat
                         const float3 dirn = sdv * (1.0f / dist);
                         shadow = true;
                         so = make_float4(from.x, from.y, from.z, dist - 1e-4f);
-                        sd = make_float4(dirn.x, dirn.y, dirn.z, 0.0f);
+                        sd = make_float4(dirn.x, dirn.y, dirn.z, __int_as_float(wp.root));
                         scon = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
                       }
                     }
@@ -420,7 +466,7 @@ __global__ void __launch_bounds__(128) k_connect(SceneView sv, PathSoA ps, Shado
           const float4 o = sh.o[i], d = sh.d[i];
           r = make_ray(o.x, o.y, o.z, d.x, d.y, d.z, 1e-4f);
           leaf.reset(o.w);
-          w.reset();
+          w.reset((uint32_t)__float_as_int(d.w));  // the scene root rides in d.w
         } else {
           exhausted = true;
         }
@@ -440,31 +486,56 @@ __global__ void __launch_bounds__(128) k_connect(SceneView sv, PathSoA ps, Shado
   }
 }
 
-// ---- accumulate ----------------------------------------------------------------
-__global__ void k_accumulate(WaveParams wp, PathSoA ps, float* __restrict__ sum, float* __restrict__ sumsq) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= wp.npix) return;
-  float3 acc = f3(0, 0, 0), acc2 = f3(0, 0, 0);
-  for (int sl = 0; sl < wp.S; sl++) {
-    const int i = sl * wp.npix + p;
-    float3 c = f3(ps.lx[i], ps.ly[i], ps.lz[i]);
-    if (wp.clamp > 0.0f) {  // clampFirefly (renderer.go:1917-1926)
-      const float m = maxcomp(c);
-      if (!(m <= wp.clamp || m <= 0.0f)) c = c * (wp.clamp / m);
+// ---- accumulate --------------------------------------------------------------
+// For every view the wave touches, each pixel adds its samples of the wave in
+// sample order (path = view.path_off + s * npix + p): no atomics, and the sum
+// does not depend on thread scheduling.
+__global__ void k_accumulate(const BatchState* __restrict__ bs, const ViewGPU* __restrict__ views, PathSoA ps,
+                             float* __restrict__ sum, float* __restrict__ sumsq) {
+  const long long w0 = bs->w0;
+  const long long w1 = min(bs->total, w0 + (long long)bs->cap);
+  if (w1 <= w0) return;
+  const int v0 = view_of(views, bs->n_views, w0), v1 = view_of(views, bs->n_views, w1 - 1);
+  const int stride = gridDim.x * blockDim.x;
+  for (int v = v0; v <= v1; v++) {
+    const ViewGPU& V = views[v];
+    const long long a = max(w0, V.path_off);
+    const long long b = min(w1, V.path_off + (long long)V.npix * V.spp);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < V.npix; p += stride) {
+      const long long lo = a - V.path_off - p, hi = b - V.path_off - p;  // >= -(npix-1)
+      const int s_lo = (int)max(0LL, (lo + V.npix - 1) / V.npix);
+      const int s_hi = (int)((hi + V.npix - 1) / V.npix);
+      if (s_hi <= s_lo) continue;
+      // continue the stored running sum sample by sample: the rounding sequence is
+      // that of one pass over samples 0..spp-1, whatever the wave boundaries
+      float* sp = sum + 3 * (size_t)(V.pix_off + p);
+      float* qp = sumsq ? sumsq + 3 * (size_t)(V.pix_off + p) : nullptr;
+      float3 acc = f3(sp[0], sp[1], sp[2]);
+      float3 acc2 = qp ? f3(qp[0], qp[1], qp[2]) : f3(0, 0, 0);
+      for (int s = s_lo; s < s_hi; s++) {
+        const long long i = V.path_off + (long long)s * V.npix + p - w0;
+        float3 c = f3(ps.lx[i], ps.ly[i], ps.lz[i]);
+        if (V.clamp > 0.0f) {  // clampFirefly (renderer.go:1917-1926)
+          const float mx = maxcomp(c);
+          if (!(mx <= V.clamp || mx <= 0.0f)) c = c * (V.clamp / mx);
+        }
+        acc = acc + c;
+        acc2 = acc2 + had(c, c);
+      }
+      sp[0] = acc.x;
+      sp[1] = acc.y;
+      sp[2] = acc.z;
+      if (qp) {
+        qp[0] = acc2.x;
+        qp[1] = acc2.y;
+        qp[2] = acc2.z;
+      }
     }
-    acc = acc + c;
-    acc2 = acc2 + had(c, c);
   }
-  float* s = sum + 3 * (size_t)(wp.y0 * wp.W + p);
-  s[0] += acc.x;
-  s[1] += acc.y;
-  s[2] += acc.z;
-  if (sumsq) {
-    float* q = sumsq + 3 * (size_t)(wp.y0 * wp.W + p);
-    q[0] += acc2.x;
-    q[1] += acc2.y;
-    q[2] += acc2.z;
-  }
+}
+
+__global__ void k_advance(BatchState* bs) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) bs->w0 = min(bs->total, bs->w0 + (long long)bs->cap);
 }
 
 __global__ void k_clear_guides(int n, float4* __restrict__ nd, uint32_t* __restrict__ c) {
@@ -476,10 +547,16 @@ __global__ void k_clear_guides(int n, float4* __restrict__ nd, uint32_t* __restr
   c[3 * i + 2] = 0u;
 }
 
-__global__ void k_finish(int n, int spp, const float* __restrict__ sum, float* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 3 * n) return;
-  out[i] = sum[i] * (1.0f / (float)spp);
+// mean = sum / spp for every pixel of every view
+__global__ void k_finish_views(const ViewGPU* __restrict__ views, int n_views, const float* __restrict__ sum,
+                               float* __restrict__ out) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int v = 0; v < n_views; v++) {
+    const ViewGPU& V = views[v];
+    const float inv = 1.0f / (float)V.spp;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * V.npix; k += stride)
+      out[3 * (size_t)V.pix_off + k] = sum[3 * (size_t)V.pix_off + k] * inv;
+  }
 }
 
 // ---- host orchestration ----------------------------------------------------------
@@ -493,16 +570,17 @@ T* carve(char*& p, size_t n) {
 }  // namespace bcgx
 
 struct RenderBuffers {
-  int cap = 0;        // path slots
-  int frame_px = 0;   // pixels of the frame buffers
-  bcgx::DevBuf paths, shadow, queues, counters, seq, frame;
+  int cap = 0;          // path slots
+  size_t frame_px = 0;  // pixels of the frame buffers
+  bcgx::DevBuf paths, shadow, queues, counters, seq, frame, table;
+  bcgx::HostBuf staging;
   bcgx::PathSoA ps{};
   bcgx::ShadowSoA sh{};
   int* q[2] = {nullptr, nullptr};
   bcgx::WaveCounters* cnt = nullptr;
-  double* seqX = nullptr;
-  double* seqY = nullptr;
-  int nseq = 0;
+  bcgx::BatchState* bs = nullptr;
+  bcgx::ViewGPU* views = nullptr;
+  double2* seq_xy = nullptr;
   float* sum = nullptr;        // 3 per pixel
   float* sumsq = nullptr;      // 3 per pixel (sample second moments, on request)
   bool want_sumsq = false;
@@ -513,31 +591,40 @@ struct RenderBuffers {
   uint32_t* guide_c = nullptr; // compact guide
   uint32_t* guide_jit = nullptr;
   uint32_t* rgba = nullptr;
-  int ext_grid = 0, con_grid = 0, shade_grid = 0;
+  // one wave as an instantiated CUDA graph, and the launch arguments it was captured with
+  cudaGraphExec_t graph = nullptr;
+  std::vector<uintptr_t> graph_key;
 };
 
 namespace bcgx {
 
 void destroy_render_buffers(bc_context* ctx) {
   if (!ctx->rb) return;
-  ctx->rb->paths.release();
-  ctx->rb->shadow.release();
-  ctx->rb->queues.release();
-  ctx->rb->counters.release();
-  ctx->rb->seq.release();
-  ctx->rb->frame.release();
-  delete ctx->rb;
+  RenderBuffers* rb = ctx->rb;
+  if (rb->graph) cudaGraphExecDestroy(rb->graph);
+  rb->paths.release();
+  rb->shadow.release();
+  rb->queues.release();
+  rb->counters.release();
+  rb->seq.release();
+  rb->frame.release();
+  rb->table.release();
+  rb->staging.release();
+  delete rb;
   ctx->rb = nullptr;
 }
 
 static bc_status ensure_paths(bc_context* ctx, int cap) {
   RenderBuffers* rb = ctx->rb;
   if (rb->cap >= cap) return BC_OK;
-  size_t per = 16 * sizeof(float) + 2 * sizeof(uint64_t) + sizeof(uint32_t) + sizeof(float) + sizeof(int32_t);
+  size_t per = 16 * sizeof(float) + 2 * sizeof(uint64_t) + sizeof(uint32_t) + sizeof(float) + 4 * sizeof(int32_t);
   cudaError_t e = rb->paths.ensure((size_t)cap * per + 64 * 256);
   if (e == cudaSuccess) e = rb->shadow.ensure((size_t)cap * (3 * sizeof(float4) + sizeof(int32_t)) + 8 * 256);
   if (e == cudaSuccess) e = rb->queues.ensure((size_t)cap * 2 * sizeof(int) + 4 * 256);
-  if (e != cudaSuccess) return cuda_status(ctx, e, "path buffers");
+  if (e != cudaSuccess) {
+    rb->cap = 0;
+    return cuda_status(ctx, e, "path buffers");
+  }
   char* p = (char*)rb->paths.p;
   PathSoA& s = rb->ps;
   float** fl[] = {&s.ox, &s.oy, &s.oz, &s.dx, &s.dy, &s.dz, &s.tx, &s.ty, &s.tz, &s.lx, &s.ly, &s.lz, &s.px, &s.py, &s.pz, &s.ppdf};
@@ -547,6 +634,9 @@ static bc_status ensure_paths(bc_context* ctx, int cap) {
   s.flags = carve<uint32_t>(p, cap);
   s.hit_t = carve<float>(p, cap);
   s.hit_slot = carve<int32_t>(p, cap);
+  s.view = carve<int32_t>(p, cap);
+  s.pix = carve<int32_t>(p, cap);
+  s.samp = carve<int32_t>(p, cap);
   char* q = (char*)rb->shadow.p;
   rb->sh.o = carve<float4>(q, cap);
   rb->sh.d = carve<float4>(q, cap);
@@ -559,20 +649,23 @@ static bc_status ensure_paths(bc_context* ctx, int cap) {
   return BC_OK;
 }
 
-static bc_status ensure_frame(bc_context* ctx, int px) {
+static bc_status ensure_frame(bc_context* ctx, size_t px) {
   RenderBuffers* rb = ctx->rb;
   if (rb->frame_px >= px) return BC_OK;
-  size_t bytes = (size_t)px * (5 * 3 * sizeof(float) + sizeof(float4) + 5 * sizeof(uint32_t)) + 16 * 256;
+  size_t bytes = px * (5 * 3 * sizeof(float) + sizeof(float4) + 5 * sizeof(uint32_t)) + 16 * 256;
   cudaError_t e = rb->frame.ensure(bytes);
-  if (e != cudaSuccess) return cuda_status(ctx, e, "frame buffers");
+  if (e != cudaSuccess) {
+    rb->frame_px = 0;
+    return cuda_status(ctx, e, "frame buffers");
+  }
   char* p = (char*)rb->frame.p;
-  rb->sum = carve<float>(p, 3 * (size_t)px);
-  rb->sumsq = carve<float>(p, 3 * (size_t)px);
-  rb->out = carve<float>(p, 3 * (size_t)px);
-  rb->post_tmp = carve<float>(p, 3 * (size_t)px);
-  rb->post_tmp2 = carve<float>(p, 3 * (size_t)px);
+  rb->sum = carve<float>(p, 3 * px);
+  rb->sumsq = carve<float>(p, 3 * px);
+  rb->out = carve<float>(p, 3 * px);
+  rb->post_tmp = carve<float>(p, 3 * px);
+  rb->post_tmp2 = carve<float>(p, 3 * px);
   rb->guide_nd = carve<float4>(p, px);
-  rb->guide_c = carve<uint32_t>(p, 3 * (size_t)px);
+  rb->guide_c = carve<uint32_t>(p, 3 * px);
   rb->guide_jit = carve<uint32_t>(p, px);
   rb->rgba = carve<uint32_t>(p, px);
   rb->frame_px = px;
@@ -587,28 +680,24 @@ int effective_spp(const bc_settings& s) {  // renderer.go:2395-2417
 }
 
 // Halton table (buildSampleSequence, renderer.go:1883-1904), computed on the
-// host in fp64 exactly as the reference does.
+// host in fp64 exactly as the reference does; appended to X, Y.
 static void sample_sequence(const bc_settings& s, std::vector<double>* X, std::vector<double>* Y) {
-  X->clear();
-  Y->clear();
   if (s.sampler == BC_SAMPLER_RANDOM) return;
   const int n = effective_spp(s);
-  X->resize(n);
-  Y->resize(n);
   if (s.sampler == BC_SAMPLER_R2) {
     const double g = 1.324717957244746;
     const double a1 = 1.0 / g, a2 = 1.0 / (g * g);
     for (int i = 0; i < n; i++) {
       double a = 0.5 + (double)(i + 1) * a1, b = 0.5 + (double)(i + 1) * a2;
-      (*X)[i] = a - std::floor(a);
-      (*Y)[i] = b - std::floor(b);
+      X->push_back(a - std::floor(a));
+      Y->push_back(b - std::floor(b));
     }
     return;
   }
   for (int i = 0; i < n; i++) {
     uint64_t m = (uint64_t)(i + 1), r = 0;
     for (int k = 0; k < 64; k++) { r = (r << 1) | (m & 1); m >>= 1; }
-    (*X)[i] = (double)r * 5.421010862427522e-20;
+    X->push_back((double)r * 5.421010862427522e-20);
     uint64_t n3 = (uint64_t)(i + 1);
     double invBase = 1.0 / 3.0, inv = invBase, res = 0;
     while (n3 > 0) {
@@ -616,7 +705,7 @@ static void sample_sequence(const bc_settings& s, std::vector<double>* X, std::v
       n3 /= 3;
       inv *= invBase;
     }
-    (*Y)[i] = res;
+    Y->push_back(res);
   }
 }
 
@@ -652,121 +741,238 @@ static void camera_basis(const bc_camera& c, double aspect, double o[3], double 
   }
 }
 
-template <int STACK, bool SPH>
-static int persistent_grid(const void* fn, int block) {
-  int dev = 0, sms = 0, per = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, 0);
-  return std::max(1, sms * std::max(1, per));
-}
-
-template <int STACK, bool SPH>
-static cudaError_t launch_bounce(bc_context* ctx, const WaveParams& wp, const ShadeScene& sc, int bounce, int cur) {
-  RenderBuffers* rb = ctx->rb;
-  cudaStream_t st = ctx->stream;
-  static int ext_grid = 0, con_grid = 0;
-  if (!ext_grid) ext_grid = persistent_grid<STACK, SPH>((const void*)k_extend<STACK, SPH>, 128);
-  if (!con_grid) con_grid = persistent_grid<STACK, SPH>((const void*)k_connect<STACK, SPH>, 128);
-  WaveCounters* c = rb->cnt;
-  cudaError_t e = cudaMemsetAsync(&c->work_ext, 0, sizeof(int) * 2, st);
-  if (e) return e;
-  e = cudaMemsetAsync(&c->q[cur ^ 1], 0, sizeof(int), st);
-  if (e) return e;
-  e = cudaMemsetAsync(&c->shadow, 0, sizeof(int), st);
-  if (e) return e;
-  k_extend<STACK, SPH><<<ext_grid, 128, 0, st>>>(sc.sv, rb->ps, rb->q[cur], c, cur, ctx->d_status);
+static int sm_count() {
   static int sms = 0;
   if (!sms) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
   }
-  k_shade<<<sms * 8, 256, 0, st>>>(wp, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1], rb->sh, c, cur, bounce, rb->guide_nd,
-                                   rb->guide_c, rb->guide_jit);
-  if (wp.n_lights > 0)
-    k_connect<STACK, SPH><<<con_grid, 128, 0, st>>>(sc.sv, rb->ps, rb->sh, c, ctx->d_status);
-  return cudaGetLastError();
+  return sms;
 }
+
+static int persistent_grid(const void* fn, int block) {
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, 0);
+  return sm_count() * std::max(1, per);
+}
+
+// Launch shape of one wave; computed before any stream capture.
+struct WaveShape {
+  int gen_grid, ext_grid, con_grid, shade_grid, acc_grid;
+  int bounces;
+  bool lights;
+};
 
 template <int STACK, bool SPH>
-static cudaError_t run_wave(bc_context* ctx, const WaveParams& wp, const ShadeScene& sc) {
+static WaveShape wave_shape(int cap, int bounces, bool lights) {
+  static int ext = 0, con = 0;
+  if (!ext) ext = persistent_grid((const void*)k_extend<STACK, SPH>, 128);
+  if (!con) con = persistent_grid((const void*)k_connect<STACK, SPH>, 128);
+  WaveShape w;
+  w.gen_grid = (cap + 255) / 256;
+  w.ext_grid = ext;
+  w.con_grid = con;
+  w.shade_grid = sm_count() * 8;
+  w.acc_grid = sm_count() * 8;
+  w.bounces = bounces;
+  w.lights = lights;
+  return w;
+}
+
+// Enqueues one wave: generate, the bounces, accumulate, advance.
+template <int STACK, bool SPH>
+static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const ShadeScene& sc, cudaStream_t st) {
   RenderBuffers* rb = ctx->rb;
-  cudaStream_t st = ctx->stream;
-  const int n = wp.npix * wp.S;
   WaveCounters* c = rb->cnt;
-  cudaError_t e = cudaSuccess;
-  k_generate<<<(n + 255) / 256, 256, 0, st>>>(wp, rb->ps, rb->q[0], rb->seqX, rb->seqY, rb->guide_jit, c);
+  k_generate<<<w.gen_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->q[0], rb->seq_xy, rb->guide_jit, c);
   int cur = 0;
-  for (int b = 0; b < wp.bounces; b++) {
-    e = launch_bounce<STACK, SPH>(ctx, wp, sc, b, cur);
+  for (int b = 0; b < w.bounces; b++) {
+    cudaError_t e = cudaMemsetAsync(&c->work_ext, 0, sizeof(int) * 2, st);
+    if (!e) e = cudaMemsetAsync(&c->q[cur ^ 1], 0, sizeof(int), st);
+    if (!e) e = cudaMemsetAsync(&c->shadow, 0, sizeof(int), st);
     if (e) return e;
+    k_extend<STACK, SPH><<<w.ext_grid, 128, 0, st>>>(sc.sv, rb->views, rb->ps, rb->q[cur], c, cur, ctx->d_status);
+    k_shade<<<w.shade_grid, 256, 0, st>>>(rb->views, ctx->ds.n_mats, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1], rb->sh,
+                                          c, cur, b, rb->guide_nd, rb->guide_c, rb->guide_jit);
+    if (w.lights) k_connect<STACK, SPH><<<w.con_grid, 128, 0, st>>>(sc.sv, rb->ps, rb->sh, c, ctx->d_status);
     cur ^= 1;
   }
-  k_accumulate<<<(wp.npix + 255) / 256, 256, 0, st>>>(wp, rb->ps, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr);
+  k_accumulate<<<w.acc_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr);
+  k_advance<<<1, 32, 0, st>>>(rb->bs);
   return cudaGetLastError();
 }
 
-// Renders rows [y0, y0 + rows) into rb->sum (and guides). Returns rays traced.
-static bc_status render_rows_device(bc_context* ctx, const bc_camera& cam, const bc_settings& s, int y0, int rows,
-                                    bool want_guides, int64_t* rays) {
-  if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
-  if (s.width < 1 || s.height < 1 || s.bounces < 1 || s.spp < 1 || y0 < 0 || rows < 1 || y0 + rows > s.height)
+// Runs `n_waves` waves, through one captured CUDA graph when the option allows.
+template <int STACK, bool SPH>
+static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const ShadeScene& sc, int64_t n_waves) {
+  RenderBuffers* rb = ctx->rb;
+  cudaStream_t st = ctx->stream;
+  const WaveShape w = wave_shape<STACK, SPH>(rb->cap, bounces, lights);
+  const bool use_graph = ctx->render_graph != 0 && n_waves > 1;
+  if (use_graph) {
+    // every value the captured launches were given
+    std::vector<uintptr_t> key = {(uintptr_t)STACK, (uintptr_t)SPH, (uintptr_t)bounces, (uintptr_t)lights,
+                                  (uintptr_t)rb->cap, (uintptr_t)w.gen_grid, (uintptr_t)rb->q[0], (uintptr_t)rb->q[1],
+                                  (uintptr_t)rb->cnt, (uintptr_t)rb->bs, (uintptr_t)rb->views, (uintptr_t)rb->seq_xy,
+                                  (uintptr_t)rb->sum, (uintptr_t)(rb->want_sumsq ? rb->sumsq : nullptr),
+                                  (uintptr_t)rb->guide_nd, (uintptr_t)rb->guide_c, (uintptr_t)rb->guide_jit,
+                                  (uintptr_t)ctx->ds.n_mats, (uintptr_t)ctx->d_status};
+    auto add_bytes = [&key](const void* p, size_t n) {
+      const size_t k = key.size();
+      key.resize(k + (n + sizeof(uintptr_t) - 1) / sizeof(uintptr_t), 0);
+      std::memcpy(key.data() + k, p, n);
+    };
+    add_bytes(&rb->ps, sizeof(rb->ps));
+    add_bytes(&rb->sh, sizeof(rb->sh));
+    add_bytes(&sc, sizeof(sc));
+    if (!rb->graph || rb->graph_key != key) {
+      if (rb->graph) cudaGraphExecDestroy(rb->graph);
+      rb->graph = nullptr;
+      rb->graph_key.clear();
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e) return cuda_status(ctx, e, "wave capture");
+      cudaError_t le = enqueue_wave<STACK, SPH>(ctx, w, sc, st);
+      e = cudaStreamEndCapture(st, &g);
+      if (le) e = le;
+      if (!e) e = cudaGraphInstantiate(&rb->graph, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e) {
+        rb->graph = nullptr;
+        return cuda_status(ctx, e, "wave graph");
+      }
+      rb->graph_key = key;
+    }
+  }
+  for (int64_t k = 0; k < n_waves; k++) {
+    if (*(volatile int*)ctx->h_cancel || ctx->cancel.load()) {
+      cudaStreamSynchronize(st);
+      return set_error(ctx, BC_ERR_CANCELLED, "render cancelled");
+    }
+    cudaError_t e = use_graph ? cudaGraphLaunch(rb->graph, st) : enqueue_wave<STACK, SPH>(ctx, w, sc, st);
+    if (e) return cuda_status(ctx, e, "wavefront launch");
+  }
+  return BC_OK;
+}
+
+// One view of a render: what a caller asks for, before packing.
+struct ViewRequest {
+  int scene;
+  bc_camera cam;
+  bc_settings s;
+  int y0, rows;
+  long long pix_off;
+  bool want_guides;
+};
+
+static bc_status check_view(bc_context* ctx, const ViewRequest& r) {
+  const bc_settings& s = r.s;
+  if (r.scene < 0 || r.scene >= (int)ctx->ranges.size())
+    return set_error(ctx, BC_ERR_INVALID_ARG, "view names a scene outside the resident set");
+  if (s.width < 1 || s.height < 1 || s.bounces < 1 || s.spp < 1 || r.y0 < 0 || r.rows < 1 || r.y0 + r.rows > s.height)
     return set_error(ctx, BC_ERR_INVALID_ARG, "invalid render size, rows, spp or bounces");
   if ((int64_t)s.width * s.height > (1 << 26)) return set_error(ctx, BC_ERR_INVALID_ARG, "frame too large");
+  if (s.bounces > kMaxBounces) return set_error(ctx, BC_ERR_INVALID_ARG, "bounces above 1024");
+  return BC_OK;
+}
+
+// Renders the requested views into rb->sum (and guides); `frame_px` pixels of
+// frame buffers are kept. Leaves the per-view table in rb->views.
+static bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, size_t frame_px, int64_t* rays) {
+  if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
+  if (req.empty()) return set_error(ctx, BC_ERR_INVALID_ARG, "no views");
+  bc_status bst;
+  for (const ViewRequest& r : req)
+    if ((bst = check_view(ctx, r))) return bst;
   if (!ctx->rb) ctx->rb = new RenderBuffers();
   RenderBuffers* rb = ctx->rb;
-  const int W = s.width, H = s.height;
-  const int npix = W * rows;
-  const int spp = effective_spp(s);
-  const int cap_target = 1 << 22;
-  int S = std::max(1, std::min(spp, cap_target / std::max(1, npix)));
-  int cap = std::max(npix * S, 1 << 16);
-  bc_status bst = ensure_paths(ctx, std::min(cap, std::max(cap_target, npix)));
-  if (bst) return bst;
-  if ((bst = ensure_frame(ctx, W * H))) return bst;
-  if (npix > rb->cap) return set_error(ctx, BC_ERR_CAPACITY, "row chunk exceeds path capacity");
-  S = std::max(1, std::min(S, rb->cap / npix));
-  cudaError_t e = rb->counters.ensure(sizeof(WaveCounters));
-  if (e) return cuda_status(ctx, e, "counters");
-  rb->cnt = rb->counters.as<WaveCounters>();
+  const int n = (int)req.size();
+  std::vector<ViewGPU> views(n);
   std::vector<double> X, Y;
-  sample_sequence(s, &X, &Y);
-  e = rb->seq.ensure(std::max<size_t>(16, 2 * X.size() * sizeof(double)));
-  if (e) return cuda_status(ctx, e, "sample table");
-  rb->seqX = rb->seq.as<double>();
-  rb->seqY = rb->seqX + X.size();
-  rb->nseq = (int)X.size();
-  if (!X.empty()) {
-    e = cudaMemcpyAsync(rb->seqX, X.data(), X.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
-    if (!e) e = cudaMemcpyAsync(rb->seqY, Y.data(), Y.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+  long long total = 0;
+  int max_bounces = 0;
+  bool lights = false;
+  for (int v = 0; v < n; v++) {
+    const ViewRequest& r = req[v];
+    const SceneRange& sr = ctx->ranges[r.scene];
+    ViewGPU& V = views[v];
+    std::memset(&V, 0, sizeof(V));
+    V.W = r.s.width;
+    V.H = r.s.height;
+    V.y0 = r.y0;
+    V.rows = r.rows;
+    V.npix = r.s.width * r.rows;
+    V.pix_off = r.pix_off;
+    V.spp = effective_spp(r.s);
+    V.bounces = r.s.bounces;
+    V.rr_depth = r.s.rr_depth;
+    V.sampler = r.s.sampler;
+    V.mis = r.s.mis != 0;
+    V.power = r.s.power_light_sampling != 0;
+    V.seq_off = (int)X.size();
+    sample_sequence(r.s, &X, &Y);
+    V.nseq = (int)X.size() - V.seq_off;
+    V.n_lights = sr.n_lights;
+    V.light_off = sr.light_off;
+    V.root = sr.root;
+    V.want_guides = r.want_guides ? 1 : 0;
+    V.clamp = (float)r.s.firefly_clamp;
+    V.seed = r.s.seed;
+    camera_basis(r.cam, (double)V.W / (double)V.H, V.origin, V.lower, V.horiz, V.vert);
+    V.path_off = total;
+    total += (long long)V.npix * V.spp;
+    max_bounces = std::max(max_bounces, V.bounces);
+    lights = lights || sr.n_lights > 0;
   }
-  if (!e) e = cudaMemsetAsync(rb->cnt, 0, sizeof(WaveCounters), ctx->stream);
-  if (!e) e = cudaMemsetAsync(rb->sum + 3 * (size_t)y0 * W, 0, 3 * sizeof(float) * (size_t)npix, ctx->stream);
-  if (!e && rb->want_sumsq)
-    e = cudaMemsetAsync(rb->sumsq + 3 * (size_t)y0 * W, 0, 3 * sizeof(float) * (size_t)npix, ctx->stream);
-  if (!e && want_guides) {  // invalid guides: depth -1, compact words 0
-    k_clear_guides<<<(npix + 255) / 256, 256, 0, ctx->stream>>>(npix, rb->guide_nd + (size_t)y0 * W,
-                                                                rb->guide_c + 3 * (size_t)y0 * W);
-    e = cudaGetLastError();
+  const int cap = (int)std::max<long long>(1, std::min<long long>(total, ctx->render_wave_cap));
+  if ((bst = ensure_paths(ctx, cap))) return bst;
+  if ((bst = ensure_frame(ctx, frame_px))) return bst;
+  BatchState bsh;
+  bsh.w0 = 0;
+  bsh.total = total;
+  bsh.cap = std::min(cap, rb->cap);
+  bsh.n_views = n;
+  // device tables: views, batch cursor, counters; the sample tables
+  // device tables at fixed offsets (a captured wave keeps these addresses):
+  // [BatchState | WaveCounters | views], and the (x, y) sample pairs
+  const size_t tbytes = 512 + n * sizeof(ViewGPU);
+  const size_t sbytes = std::max<size_t>(16, X.size() * sizeof(double2));
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);  // the staging buffer may still be in flight
+  if (!e) e = rb->table.ensure(tbytes);
+  if (!e) e = rb->seq.ensure(sbytes);
+  if (!e) e = rb->staging.ensure(tbytes + 16 + sbytes);
+  if (e) return cuda_status(ctx, e, "render tables");
+  rb->bs = rb->table.as<BatchState>();
+  rb->cnt = reinterpret_cast<WaveCounters*>((char*)rb->table.p + 256);
+  rb->views = reinterpret_cast<ViewGPU*>((char*)rb->table.p + 512);
+  rb->seq_xy = rb->seq.as<double2>();
+  char* hs = (char*)rb->staging.p;
+  std::memset(hs, 0, 512);
+  std::memcpy(hs, &bsh, sizeof(bsh));
+  std::memcpy(hs + 512, views.data(), n * sizeof(ViewGPU));
+  double* hq = reinterpret_cast<double*>(hs + tbytes + ((16 - (tbytes & 15)) & 15));
+  for (size_t i = 0; i < X.size(); i++) {
+    hq[2 * i] = X[i];
+    hq[2 * i + 1] = Y[i];
+  }
+  e = cudaMemcpyAsync(rb->table.p, hs, tbytes, cudaMemcpyHostToDevice, ctx->stream);
+  if (!e && !X.empty())
+    e = cudaMemcpyAsync(rb->seq.p, hq, X.size() * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream);
+  for (int v = 0; v < n && !e; v++) {
+    const ViewGPU& V = views[v];
+    e = cudaMemsetAsync(rb->sum + 3 * (size_t)V.pix_off, 0, 3 * sizeof(float) * (size_t)V.npix, ctx->stream);
+    if (!e && rb->want_sumsq)
+      e = cudaMemsetAsync(rb->sumsq + 3 * (size_t)V.pix_off, 0, 3 * sizeof(float) * (size_t)V.npix, ctx->stream);
+    if (!e && V.want_guides) {  // invalid guides: depth -1, compact words 0
+      k_clear_guides<<<(V.npix + 255) / 256, 256, 0, ctx->stream>>>(V.npix, rb->guide_nd + V.pix_off,
+                                                                    rb->guide_c + 3 * (size_t)V.pix_off);
+      e = cudaGetLastError();
+    }
   }
   if (e) return cuda_status(ctx, e, "render setup");
 
-  WaveParams wp;
-  std::memset(&wp, 0, sizeof(wp));
-  wp.W = W; wp.H = H; wp.y0 = y0; wp.rows = rows; wp.npix = npix;
-  wp.bounces = s.bounces;
-  wp.rr_depth = s.rr_depth;
-  wp.mis = s.mis != 0;
-  wp.power = s.power_light_sampling != 0;
-  wp.sampler = s.sampler;
-  wp.nseq = rb->nseq;
-  wp.n_mats = ctx->ds.n_mats;
-  wp.n_lights = ctx->ds.n_lights;
-  wp.want_guides = want_guides ? 1 : 0;
-  wp.clamp = (float)s.firefly_clamp;
-  wp.seed = s.seed;
-  camera_basis(cam, (double)W / (double)H, wp.origin, wp.lower, wp.horiz, wp.vert);
   ShadeScene sc;
   sc.sv.nodes = ctx->ds.nodes;
   sc.sv.tri = ctx->ds.tri;
@@ -776,26 +982,43 @@ static bc_status render_rows_device(bc_context* ctx, const bc_camera& cam, const
   sc.mats = ctx->ds.mats;
   sc.lights = ctx->ds.lights;
   sc.lpdf_by_prim = ctx->ds.light_pdf_by_prim;
+  const int64_t n_waves = (total + bsh.cap - 1) / bsh.cap;
   const int stack = stack_variant(ctx->ds.stack_need);
-  for (int s0 = 0; s0 < spp; s0 += S) {
-    if (*(volatile int*)ctx->h_cancel || ctx->cancel.load()) {
-      cudaStreamSynchronize(ctx->stream);
-      return set_error(ctx, BC_ERR_CANCELLED, "render cancelled");
-    }
-    wp.s0 = s0;
-    wp.S = std::min(S, spp - s0);
-    const bool sph = ctx->ds.has_spheres;
-    if (stack == 64) e = sph ? run_wave<64, true>(ctx, wp, sc) : run_wave<64, false>(ctx, wp, sc);
-    else if (stack == 128) e = sph ? run_wave<128, true>(ctx, wp, sc) : run_wave<128, false>(ctx, wp, sc);
-    else e = sph ? run_wave<256, true>(ctx, wp, sc) : run_wave<256, false>(ctx, wp, sc);
-    if (e) return cuda_status(ctx, e, "wavefront launch");
-  }
+  const bool sph = ctx->ds.has_spheres;
+  if (stack == 64)
+    bst = sph ? run_waves<64, true>(ctx, max_bounces, lights, sc, n_waves)
+              : run_waves<64, false>(ctx, max_bounces, lights, sc, n_waves);
+  else if (stack == 128)
+    bst = sph ? run_waves<128, true>(ctx, max_bounces, lights, sc, n_waves)
+              : run_waves<128, false>(ctx, max_bounces, lights, sc, n_waves);
+  else
+    bst = sph ? run_waves<256, true>(ctx, max_bounces, lights, sc, n_waves)
+              : run_waves<256, false>(ctx, max_bounces, lights, sc, n_waves);
+  if (bst) return bst;
+  k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sum, rb->out);
+  if (rb->want_sumsq) k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sumsq, rb->post_tmp);
+  e = cudaGetLastError();
   unsigned long long r = 0;
-  e = cudaMemcpyAsync(&r, &rb->cnt->rays, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream);
+  if (!e) e = cudaMemcpyAsync(&r, &rb->cnt->rays, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream);
   if (!e) e = cudaStreamSynchronize(ctx->stream);
   if (e) return cuda_status(ctx, e, "render");
   if (rays) *rays = (int64_t)r;
   return check_kernel_status(ctx);
+}
+
+static bc_status render_rows_device(bc_context* ctx, const bc_camera& cam, const bc_settings& s, int y0, int rows,
+                                    bool want_guides, int64_t* rays) {
+  ViewRequest r;
+  r.scene = 0;
+  r.cam = cam;
+  r.s = s;
+  r.y0 = y0;
+  r.rows = rows;
+  r.pix_off = (long long)y0 * s.width;
+  r.want_guides = want_guides;
+  if (s.width < 1 || s.height < 1 || (int64_t)s.width * s.height > (1 << 26))
+    return set_error(ctx, BC_ERR_INVALID_ARG, "invalid render size, rows, spp or bounces");
+  return render_views(ctx, std::vector<ViewRequest>{r}, (size_t)s.width * s.height, rays);
 }
 
 bc_status run_post(bc_context* ctx, const bc_settings& s);  // post.cu
@@ -815,7 +1038,7 @@ PostTargets post_targets(bc_context* ctx) {
 
 bc_status ensure_post_scratch(bc_context* ctx, int px, PostTargets* t) {
   if (!ctx->rb) ctx->rb = new RenderBuffers();
-  bc_status st = ensure_frame(ctx, px);
+  bc_status st = ensure_frame(ctx, (size_t)px);
   if (st) return st;
   *t = post_targets(ctx);
   return BC_OK;
@@ -836,12 +1059,8 @@ bc_status bc_render_rows(bc_context* ctx, const bc_camera* cam, const bc_setting
   if (st) return st;
   RenderBuffers* rb = ctx->rb;
   const int W = settings->width, npix = W * rows;
-  const int spp = effective_spp(*settings);
-  k_finish<<<(3 * npix + 255) / 256, 256, 0, ctx->stream>>>(npix, spp, rb->sum + 3 * (size_t)y0 * W,
-                                                            rb->out + 3 * (size_t)y0 * W);
-  cudaError_t e = cudaGetLastError();
-  if (!e) e = cudaMemcpyAsync(linear_out, rb->out + 3 * (size_t)y0 * W, 3 * sizeof(float) * (size_t)npix,
-                              cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaMemcpyAsync(linear_out, rb->out + 3 * (size_t)y0 * W, 3 * sizeof(float) * (size_t)npix,
+                                  cudaMemcpyDeviceToHost, ctx->stream);
   if (!e && guide_out)
     e = cudaMemcpyAsync(guide_out, rb->guide_c + 3 * (size_t)y0 * W, 3 * sizeof(uint32_t) * (size_t)npix,
                         cudaMemcpyDeviceToHost, ctx->stream);
@@ -861,11 +1080,8 @@ bc_status bc_render_frame(bc_context* ctx, const bc_camera* cam, const bc_settin
   if (st) return st;
   RenderBuffers* rb = ctx->rb;
   const int npix = settings->width * settings->height;
-  const int spp = effective_spp(*settings);
-  k_finish<<<(3 * npix + 255) / 256, 256, 0, ctx->stream>>>(npix, spp, rb->sum, rb->out);
-  cudaError_t e = cudaGetLastError();
-  if (e) return cuda_status(ctx, e, "finish");
   if ((st = run_post(ctx, *settings))) return st;
+  cudaError_t e = cudaSuccess;
   if (linear_out)
     e = cudaMemcpyAsync(linear_out, rb->out, 3 * sizeof(float) * (size_t)npix, cudaMemcpyDeviceToHost, ctx->stream);
   if (!e && guide_out)
@@ -892,15 +1108,48 @@ bc_status bc_render_moments(bc_context* ctx, const bc_camera* cam, const bc_sett
   if (st) return st;
   RenderBuffers* rb = ctx->rb;
   const int npix = settings->width * settings->height;
-  const int spp = effective_spp(*settings);
-  k_finish<<<(3 * npix + 255) / 256, 256, 0, ctx->stream>>>(npix, spp, rb->sum, rb->out);
-  k_finish<<<(3 * npix + 255) / 256, 256, 0, ctx->stream>>>(npix, spp, rb->sumsq, rb->post_tmp);
-  cudaError_t e = cudaGetLastError();
-  if (!e) e = cudaMemcpyAsync(mean_out, rb->out, 3 * sizeof(float) * (size_t)npix, cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e =
+      cudaMemcpyAsync(mean_out, rb->out, 3 * sizeof(float) * (size_t)npix, cudaMemcpyDeviceToHost, ctx->stream);
   if (!e)
     e = cudaMemcpyAsync(meansq_out, rb->post_tmp, 3 * sizeof(float) * (size_t)npix, cudaMemcpyDeviceToHost, ctx->stream);
   if (!e) e = cudaStreamSynchronize(ctx->stream);
   if (e) return cuda_status(ctx, e, "moments readback");
+  if (rays_out) *rays_out = rays;
+  return BC_OK;
+}
+
+bc_status bc_render_batch(bc_context* ctx, const bc_view* views, int32_t n_views, float* const* linear_out,
+                          int64_t* rays_out) {
+  if (!ctx || !views || n_views < 1) return set_error(ctx, BC_ERR_INVALID_ARG, "NULL argument or no views");
+  cudaSetDevice(ctx->device);
+  std::vector<ViewRequest> req(n_views);
+  long long px = 0;
+  for (int v = 0; v < n_views; v++) {
+    ViewRequest& r = req[v];
+    r.scene = views[v].scene;
+    r.cam = views[v].camera;
+    r.s = views[v].settings;
+    r.y0 = 0;
+    r.rows = r.s.height;
+    r.pix_off = px;
+    r.want_guides = false;
+    if (r.s.width < 1 || r.s.height < 1 || (int64_t)r.s.width * r.s.height > (1 << 26))
+      return set_error(ctx, BC_ERR_INVALID_ARG, "invalid render size in view " + std::to_string(v));
+    px += (long long)r.s.width * r.s.height;
+  }
+  if (px > (1LL << 30)) return set_error(ctx, BC_ERR_INVALID_ARG, "batch holds more than 2^30 pixels");
+  int64_t rays = 0;
+  bc_status st = render_views(ctx, req, (size_t)px, &rays);
+  if (st) return st;
+  RenderBuffers* rb = ctx->rb;
+  cudaError_t e = cudaSuccess;
+  for (int v = 0; v < n_views && !e; v++)
+    if (linear_out && linear_out[v])
+      e = cudaMemcpyAsync(linear_out[v], rb->out + 3 * (size_t)req[v].pix_off,
+                          3 * sizeof(float) * (size_t)req[v].s.width * req[v].s.height, cudaMemcpyDeviceToHost,
+                          ctx->stream);
+  if (!e) e = cudaStreamSynchronize(ctx->stream);
+  if (e) return cuda_status(ctx, e, "batch readback");
   if (rays_out) *rays_out = rays;
   return BC_OK;
 }

@@ -371,9 +371,9 @@ struct Walker {
   int sp;
   uint32_t ref;
   uint32_t pending;
-  __device__ __forceinline__ void reset() {
+  __device__ __forceinline__ void reset(uint32_t root = 0) {  // root: Node8 index of the scene's root
     sp = 0;
-    ref = 0;
+    ref = root;
     pending = 0;
   }
   __device__ __forceinline__ uint32_t pop(float tlim) {

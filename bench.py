@@ -348,18 +348,134 @@ def run_render(args):
             "e2e": {"value": e2e_r / e2e_t / 1e6, "unit": METRIC, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": st.width * st.height * 16},
             "gpu_launches": None, "clocks": clk}
+    cpu_img = None
     if not args.no_cpu_baseline:
         import oracle
         ref = oracle.OracleScene.from_spec(spec)
         cst = st.copy()
-        if args.workload == "ultra":  # bounded sample: the same camera at 1/16 of the pixels, 4 spp
-            cst.width, cst.height, cst.spp = st.width // 4, st.height // 4, 4
+        if args.workload == "ultra":  # bounded sample: the full frame at 4 spp
+            cst.spp = 4
+        else:  # the Cornell frame is tiny: several frames' worth of samples
+            cst.spp = 512
         t0 = time.perf_counter()
         out = ref.render(cam, cst, seed=7, threads=0)
         dt = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": out["stats"]["segments"] / dt / 1e6, "unit": METRIC,
                                 "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"{cst.width}x{cst.height} at {cst.spp} spp, {dt:.1f} s"}
+        if args.rmse and args.workload == "cornell":
+            c16 = st.copy()
+            cpu_img = ref.render(cam, c16, seed=11, threads=0)["linear"]
+    if args.rmse:
+        # converged reference: the parity-validated GPU forward at many samples
+        conv = st.copy()
+        conv.denoise, conv.bloom = False, 0
+        plain = conv.copy()
+        if args.workload == "cornell":
+            conv.spp = 16384
+            ref_img = ctx.render_frame(cam, conv, want_guides=False, want_rgba=False)["linear"].astype(np.float64)
+            gpu_img = ctx.render_frame(cam, plain, want_guides=False, want_rgba=False)["linear"].astype(np.float64)
+            r = {"reference": "GPU, 16384 spp, full frame", "gpu_16spp": float(np.sqrt(np.mean((gpu_img - ref_img) ** 2)))}
+            if cpu_img is not None:
+                r["cpu_16spp"] = float(np.sqrt(np.mean((cpu_img - ref_img) ** 2)))
+        else:
+            y0, rows = st.height // 2 - 90, 180
+            conv.spp = 2048
+            ref_rows = ctx.render_rows(cam, conv, y0, rows)[0].astype(np.float64)
+            gpu_rows = ctx.render_rows(cam, plain, y0, rows)[0].astype(np.float64)
+            r = {"reference": f"GPU, 2048 spp, rows {y0}-{y0 + rows} of the frame (2560x180 crop)",
+                 f"gpu_{plain.spp}spp": float(np.sqrt(np.mean((gpu_rows - ref_rows) ** 2)))}
+        line["rmse"] = r
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+def run_batch(args):
+    """Batching workload: 4 resident scenes (10k / 50k / 200k / 500k random
+    triangles + one emissive quad each), 64 views (log-uniform 128x128 ..
+    1920x1080, spp U{4..64}, 8 bounces). Batched form = one bc_render_batch
+    call over all 64 views (one wave engine, captured wave graph); plain form =
+    64 sequential one-view calls of the same engine. Both render the same
+    samples, so their images are bit-identical (equal RMSE by construction).
+    value = path segments / wall time of the batched call without readback
+    (the call returns after the device is idle); e2e = the batched call with
+    every view's linear image read back to host memory."""
+    import numpy as np
+    import bcgx
+    from bcgx import scenes
+    n_views = args.views
+    specs, views = scenes.batch_views(n_views=n_views)
+    t0 = time.perf_counter()
+    built = [scenes.to_scene(s) for s in specs]
+    build_s = time.perf_counter() - t0
+    ctx = bcgx.Context(0)
+    ctx.upload_set(built)
+    px = sum(st.width * st.height for _, _, st in views)
+    paths = sum(st.width * st.height * st.spp for _, _, st in views)
+
+    def batched(readback=False):
+        t = time.perf_counter()
+        _, r = ctx.render_batch(views, readback=readback)
+        return time.perf_counter() - t, r
+
+    def plain():
+        t = time.perf_counter()
+        r = 0
+        for v in views:
+            r += ctx.render_batch([v], readback=False)[1]
+        return time.perf_counter() - t, r
+
+    for _ in range(args.warmup):
+        batched()
+    plain()
+    clocks = ClockSampler(0)
+    clocks.start()
+    bt, br = [], 0
+    for _ in range(args.steps):
+        dt, r = batched()
+        bt.append(dt)
+        br += r
+    pt, pr = [], 0
+    for _ in range(args.steps):
+        dt, r = plain()
+        pt.append(dt)
+        pr += r
+    e2e_t, e2e_r = batched(readback=True)
+    clk = clocks.stop()
+    value = br / sum(bt) / 1e6
+    plain_v = pr / sum(pt) / 1e6
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(bt) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 primary rays)",
+            "data": "synthetic, seeded (seed 0xBEAC0004)",
+            "config": {"workload": f"batch: {n_views} views over 4 resident scenes (10k/50k/200k/500k tris), "
+                                   "128x128..1920x1080, spp U{4..64}, 8 bounces",
+                       "pixels": px, "paths": paths, "segments_per_step": br // max(1, args.steps),
+                       "host_bvh_build_s": round(build_s, 2),
+                       "wave_cap": ctx.get_option("render_wave_cap")},
+            "plain": {"value": plain_v, "unit": METRIC, "ms_per_step": 1e3 * sum(pt) / args.steps,
+                      "form": f"{n_views} sequential one-view bc_render_batch calls"},
+            "batched_over_plain": value / plain_v,
+            "e2e": {"value": e2e_r / e2e_t / 1e6, "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": px * 12},
+            "gpu_launches": None, "clocks": clk}
+    if not args.no_cpu_baseline:
+        import oracle
+        t_all, segs = 0.0, 0
+        sample = []
+        for v in range(4):  # one view of each scene, 1 spp
+            k, cam, st = views[v]
+            ref = oracle.OracleScene.from_spec(specs[k])
+            cst = st.copy()
+            cst.spp = 1
+            t0 = time.perf_counter()
+            out = ref.render(cam, cst, seed=7, threads=0)
+            t_all += time.perf_counter() - t0
+            segs += out["stats"]["segments"]
+            sample.append(f"{cst.width}x{cst.height}")
+        line["cpu_baseline"] = {"value": segs / t_all / 1e6, "unit": METRIC, "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"views 0-3 (one per scene: {', '.join(sample)}) at 1 spp, {t_all:.1f} s"}
     print(json.dumps(line), flush=True)
     ctx.close()
     return 0
@@ -377,15 +493,19 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
     ap.add_argument("--minblocks", type=int, default=0, help="ray-cast register variant (1, 6, 8; 0 = library default)")
     ap.add_argument("--fast", action="store_true", help="plain fp32 closest hit instead of the exact contract")
-    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra"],
+    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch"],
                     help="raycast (default, the headline line) or a render workload")
     ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
+    ap.add_argument("--rmse", action="store_true", help="render workloads: RMSE against a converged image")
+    ap.add_argument("--views", type=int, default=64, help="batch workload: number of views")
     args = ap.parse_args()
     N_TRIS, N_RAYS = args.tris, args.rays
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
     if args.workload != "raycast":
         return run_render(args)
     return run_gpu(args)

@@ -141,6 +141,18 @@ bc_status bc_device_name(const bc_context* ctx, char* buf, size_t len);
 bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t scene_id, uint64_t topology_rev,
                           uint64_t geometry_rev);
 
+/*
+ * Upload a resident scene set for batched rendering (bc_render_batch): scenes[k]
+ * becomes scene k of the set, with its own BVH root, materials and lights in one
+ * set of device arrays. No reference counterpart (the reference keeps one scene
+ * resident, gpu_opencl_windows.go:94-131); this is the batching entry point's
+ * scene side. set_id names the caller's set: an upload with the set_id, count
+ * and revision of the resident set is a no-op. A set replaces the resident
+ * scene; the single-view calls (bc_raycast, bc_render_frame, ...) use scene 0.
+ */
+bc_status bc_scene_set_upload(bc_context* ctx, const bc_scene_desc* scenes, int32_t n_scenes, uint64_t set_id,
+                              uint64_t revision);
+
 /* Statistics of the resident scene: out[0] BVH8 nodes, out[1] primitive slots,
  * out[2] binary nodes, out[3] BVH8 depth, out[4] traversal stack entries needed,
  * out[5] device bytes held by the scene. */
@@ -202,6 +214,31 @@ bc_status bc_render_moments(bc_context* ctx, const bc_camera* cam, const bc_sett
                             float* meansq_out, int64_t* rays_out);
 
 /*
+ * One view of a batch: a camera and settings over scene `scene` of the resident
+ * set. The settings fields read are those bc_render_frame reads for the linear
+ * image (no post stack, no guides).
+ */
+typedef struct bc_view {
+  int32_t scene;
+  int32_t reserved;  /* 0 */
+  bc_camera camera;
+  bc_settings settings;
+} bc_view;
+
+/*
+ * Render n_views views in one pass of the wave engine: every view's (sample,
+ * pixel) paths are scheduled in one index space, so small views share waves
+ * and the device stays full; one wave is a captured CUDA graph replayed until
+ * the batch is done. linear_out[v] (array and entries may be NULL) receives
+ * views[v]'s width*height RGB floats, the same mean radiance bc_render_frame
+ * returns for that view with post off. rays_out: extension rays over all views.
+ * No reference counterpart: the reference renders one view per call
+ * (renderOpenCL, gpu_opencl_windows.go:565).
+ */
+bc_status bc_render_batch(bc_context* ctx, const bc_view* views, int32_t n_views, float* const* linear_out,
+                          int64_t* rays_out);
+
+/*
  * The post stack alone, on caller buffers (the part of RenderState.Start that
  * follows the render call, renderer.go:2844-2854 and 2890-2895): a-trous denoise
  * with `2 + min(3, max(taa, txaa))` passes when settings->denoise, bloom when
@@ -243,6 +280,10 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *   "raycast_exact"      1 (default): bc_raycast is exact as documented there;
  *                        0: plain fp32 closest hit, t = the fp32 distance, with no
  *                        exactness contract near edges and ties.
+ *   "render_wave_cap"    paths in flight per wave of the renderer, 4096 .. 2^25
+ *                        (default 2^22); images do not depend on it.
+ *   "render_graph"       1 (default): a render of several waves replays one
+ *                        captured CUDA graph per wave; 0: plain stream launches.
  * Unknown names or values return BC_ERR_INVALID_ARG.
  */
 bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value);

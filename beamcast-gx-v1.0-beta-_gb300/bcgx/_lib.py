@@ -53,6 +53,12 @@ class ViewC(C.Structure):
     _fields_ = [("scene", C.c_int32), ("reserved", C.c_int32), ("camera", CameraC), ("settings", SettingsC)]
 
 
+class DiffDescC(C.Structure):
+    _fields_ = [("camera", CameraC), ("settings", SettingsC), ("n_albedo", C.c_int32),
+                ("albedo_materials", P(C.c_int32)), ("n_emission", C.c_int32),
+                ("emission_materials", P(C.c_int32))]
+
+
 # (name, restype, argtypes) for every exported symbol of the two headers.
 SIGNATURES = [
     ("bc_gpu_available", C.c_int, [C.c_char_p, C.c_size_t]),
@@ -71,6 +77,10 @@ SIGNATURES = [
     ("bc_render_frame", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, u32p, u32p, i64p]),
     ("bc_render_moments", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, f32p, i64p]),
     ("bc_render_batch", C.c_int, [C.c_void_p, P(ViewC), C.c_int32, P(f32p), i64p]),
+    ("bc_diff_configure", C.c_int, [C.c_void_p, P(DiffDescC)]),
+    ("bc_diff_set_target", C.c_int, [C.c_void_p, f32p]),
+    ("bc_forward", C.c_int, [C.c_void_p, f32p, C.c_uint64, f32p, f64p]),
+    ("bc_backward", C.c_int, [C.c_void_p, f32p, f32p, f32p]),
     ("bc_post_process", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, f32p, f32p, P(SettingsC), f32p, u32p]),
     ("bc_post_process_noalloc", C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, P(SettingsC), C.c_void_p,
                                           C.c_void_p, C.c_void_p]),

@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import SceneDesc, ViewC, check, lib, ptr
+from ._lib import DiffDescC, SceneDesc, ViewC, check, lib, ptr
 from .scene import Scene, SceneArrays
 from .settings import Camera, RenderSettings
 
@@ -170,6 +170,52 @@ class Context:
         rays = C.c_int64(0)
         check(lib().bc_render_batch(self._h, vc, n, ptrs if readback else None, C.byref(rays)), self._h)
         return outs, rays.value
+
+    # -- differentiable rendering --
+    def diff_configure(self, cam: Camera, settings: RenderSettings, albedo_materials, emission_materials=()):
+        """Parameters: albedo RGB of each diffuse material in albedo_materials, then
+        emission RGB of each emissive material in emission_materials."""
+        a = np.ascontiguousarray(albedo_materials, dtype=np.int32)
+        e = np.ascontiguousarray(emission_materials, dtype=np.int32)
+        d = DiffDescC()
+        d.camera = cam.c()
+        d.settings = settings.c()
+        d.n_albedo, d.albedo_materials = len(a), ptr(a, C.c_int32) if len(a) else None
+        d.n_emission, d.emission_materials = len(e), ptr(e, C.c_int32) if len(e) else None
+        check(lib().bc_diff_configure(self._h, C.byref(d)), self._h)
+        self._diff_shape = (settings.height, settings.width, len(a), len(e))
+        self._diff_has_target = False
+
+    def diff_set_target(self, target: np.ndarray):
+        H, W, _, _ = self._diff_shape
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        assert t.shape == (H, W, 3)
+        check(lib().bc_diff_set_target(self._h, ptr(t, C.c_float)), self._h)
+        self._diff_has_target = True
+
+    def forward(self, params: np.ndarray, seed: int, want_image: bool = True, want_loss: bool | None = None):
+        """params: (n_albedo + n_emission, 3) float32. Returns (image or None, loss or None);
+        the loss is computed when a target is set."""
+        H, W, na, ne = self._diff_shape
+        if want_loss is None:
+            want_loss = self._diff_has_target
+        p = np.ascontiguousarray(params, dtype=np.float32).reshape(-1)
+        assert p.size == 3 * (na + ne)
+        img = np.empty((H, W, 3), np.float32) if want_image else None
+        loss = C.c_double(0)
+        check(lib().bc_forward(self._h, ptr(p, C.c_float), int(seed), ptr(img, C.c_float),
+                               C.byref(loss) if want_loss else None), self._h)
+        return img, (loss.value if want_loss else None)
+
+    def backward(self, dloss_dimage: np.ndarray | None = None):
+        """Gradient at the last forward: (grad_albedo (n_albedo, 3), grad_emission (n_emission, 3))."""
+        H, W, na, ne = self._diff_shape
+        dd = None if dloss_dimage is None else np.ascontiguousarray(dloss_dimage, dtype=np.float32)
+        ga = np.zeros((na, 3), np.float32)
+        ge = np.zeros((ne, 3), np.float32)
+        check(lib().bc_backward(self._h, ptr(dd, C.c_float), ptr(ga, C.c_float) if na else None,
+                                ptr(ge, C.c_float) if ne else None), self._h)
+        return ga, ge
 
     def post_process(self, linear: np.ndarray, guide_nd: np.ndarray | None, settings: RenderSettings,
                      want_rgba: bool = True):

@@ -16,6 +16,10 @@ checker. Seeds and shapes:
                    500k tris, one emissive quad each) and 64 views with
                    log-uniform sizes 128x128 .. 1920x1080, spp U{4..64},
                    8 bounces, cameras orbiting the unit cube.
+  diff_scene       seed 0xBEAC0005: random triangles with 256 diffuse material
+                   slots (true albedo U[0.2, 0.8]^3, start = true +- U[-0.1, 0.1])
+                   and 8 emissive quads (true emission U[2, 10]^3); 512^2,
+                   64 spp, 8 bounces, Russian roulette off.
 The reference's own scenes (renderer.go:2944-2994) are test inputs only.
 """
 from __future__ import annotations
@@ -372,3 +376,48 @@ def batch_views(seed: int = SEED_C4, n_views: int = 64, sizes=(10_000, 50_000, 2
         st.seed = seed + 0x100 + v
         views.append((v % len(sizes), cam, st))
     return specs, views
+
+
+# ---------------------------------------------------------------------------
+# Workload 5: inverse rendering of material parameters.
+@dataclass
+class DiffProblem:
+    spec: SceneSpec
+    cam: Camera
+    settings: RenderSettings
+    albedo_materials: np.ndarray   # (n_slots,) material indices
+    emission_materials: np.ndarray  # (n_lights,)
+    true_params: np.ndarray         # (n_slots + n_lights, 3) float32
+    init_params: np.ndarray         # (n_slots + n_lights, 3) float32
+
+
+def diff_scene(seed: int = SEED_C5, n_tris: int = 200_000, n_slots: int = 256, n_lights: int = 8,
+               width: int = 512, height: int = 512, spp: int = 64, bounces: int = 8) -> DiffProblem:
+    """Random triangles in the unit cube, each on one of n_slots diffuse
+    materials, lit by n_lights emissive quads above the cube and the sky."""
+    rng = np.random.default_rng(seed)
+    sp = SceneSpec(name=f"diff-tris-{n_tris}", bvh_mode="SAH", bvh_bins=32, bvh_leaf=4)
+    true_alb = rng.uniform(0.2, 0.8, (n_slots, 3))
+    init_alb = np.clip(true_alb + rng.uniform(-0.1, 0.1, (n_slots, 3)), 0.02, 0.98)
+    alb_mats = np.array([sp.material(Material(MAT_DIFFUSE, tuple(c))) for c in init_alb], dtype=np.int32)
+    true_em = rng.uniform(2.0, 10.0, (n_lights, 3))
+    init_em = true_em + rng.uniform(-1.0, 1.0, (n_lights, 3))
+    em_mats = np.array([sp.material(Material(MAT_EMISSIVE, emission=tuple(e))) for e in init_em], dtype=np.int32)
+    verts = random_triangle_verts(n_tris, seed + 1)
+    sp.triangles(verts, alb_mats[rng.integers(0, n_slots, n_tris)])
+    for k in range(n_lights):
+        x, z = 0.125 + 0.25 * (k % 4), 0.25 + 0.5 * (k // 4) if n_lights > 4 else 0.5
+        s = 0.09
+        sp.triangles(quad((x - s, 1.25, z - s), (x + s, 1.25, z - s), (x + s, 1.25, z + s), (x - s, 1.25, z + s)),
+                     em_mats[k])
+    cam = Camera((0.5, 1.1, -1.1), (0.5, 0.45, 0.5), (0, 1, 0), 45.0)
+    st = quality("Draft")
+    st.width, st.height, st.spp, st.bounces = width, height, spp, bounces
+    st.msaa, st.tsaa = 1, 0
+    st.sampler, st.mis, st.power_light_sampling = "Halton", True, True
+    st.firefly_clamp, st.rr_depth, st.adaptive_sampling = 0.0, bounces, False
+    st.denoise, st.bloom = False, 0
+    st.seed = seed
+    true_p = np.concatenate([true_alb, true_em]).astype(np.float32)
+    init_p = np.concatenate([init_alb, init_em]).astype(np.float32)
+    return DiffProblem(sp, cam, st, alb_mats, em_mats, true_p, init_p)

@@ -130,6 +130,7 @@ void bc_destroy(bc_context* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   destroy_render_buffers(ctx);
+  destroy_diff_state(ctx);
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_tri, &ctx->d_slot64, &ctx->d_snorm, &ctx->d_slot_prim, &ctx->d_mats,
                     &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ})
     b->release();
@@ -206,6 +207,21 @@ static bc_status install_scene(bc_context* ctx, const PackedScene& ps, const std
                             ps.slot64.size() * sizeof(double) + ps.snorm.size() * sizeof(F4) +
                             slots * sizeof(int32_t) + ps.mats.size() * sizeof(MatGPU) +
                             ps.lights.size() * sizeof(LightGPU) + ps.light_pdf_by_prim.size() * sizeof(float));
+  ctx->mat_kind.assign(ps.mats.size(), 0);
+  for (size_t i = 0; i < ps.mats.size(); i++) ctx->mat_kind[i] = (int8_t)ps.mats[i].kind;
+  ctx->mat_is_light.assign(ps.mats.size(), 0);
+  if (!ps.lights.empty()) {
+    std::vector<int32_t> slot_of(ps.n_prims, -1);
+    for (int32_t sl = 0; sl < ps.n_prims; sl++)
+      if (ps.slot_prim[sl] >= 0 && ps.slot_prim[sl] < ps.n_prims) slot_of[ps.slot_prim[sl]] = sl;
+    for (const LightGPU& L : ps.lights) {
+      const int32_t sl = (L.prim >= 0 && L.prim < ps.n_prims) ? slot_of[L.prim] : -1;
+      if (sl < 0) continue;
+      int32_t m;
+      std::memcpy(&m, &ps.snorm[sl].w, 4);
+      if (m >= 0 && m < (int32_t)ps.mats.size()) ctx->mat_is_light[m] = 1;
+    }
+  }
   ctx->ranges = ranges;
   ctx->has_scene = true;
   return BC_OK;

@@ -69,6 +69,8 @@ struct bc_context {
   bcgx::DevBuf d_nodes, d_tri, d_slot64, d_snorm, d_slot_prim, d_mats, d_lights, d_lpdf;
   std::vector<bcgx::SceneRange> ranges;  // scenes of the resident set (one for bc_scene_upload)
   bool is_set = false;                    // resident scenes came from bc_scene_set_upload
+  std::vector<int8_t> mat_kind;           // host copy of the resident materials' kinds
+  std::vector<int8_t> mat_is_light;       // 1: material of a sphere light (its emission feeds NEE records)
   int64_t stats[6] = {0, 0, 0, 0, 0, 0};
   int raycast_minblocks = 6;  // register budget of the exact ray-cast kernels (bc_set_option)
   int raycast_exact = 1;      // 0: plain fp32 closest hit (bc_set_option "raycast_exact")
@@ -81,6 +83,7 @@ struct bc_context {
   unsigned long long* d_work = nullptr;
   long long render_wave_cap = 1 << 22;  // paths per wave (bc_set_option "render_wave_cap")
   int render_graph = 1;                 // replay a captured wave graph (bc_set_option "render_graph")
+  struct DiffState* diff = nullptr;  // differentiable rendering (diff.cu)
   // rendering state (render.cu)
   struct RenderBuffers* rb = nullptr;
   std::atomic<int> cancel{0};
@@ -93,4 +96,5 @@ bc_status set_error(bc_context* ctx, bc_status st, const std::string& msg);
 bc_status cuda_status(bc_context* ctx, cudaError_t e, const char* what);
 bc_status check_kernel_status(bc_context* ctx);
 void destroy_render_buffers(bc_context* ctx);
+void destroy_diff_state(bc_context* ctx);
 }  // namespace bcgx

@@ -31,6 +31,7 @@
 #include "context.h"
 #include "sampling.cuh"
 #include "trace_core.cuh"
+#include "wave.h"
 
 namespace bcgx {
 
@@ -54,6 +55,18 @@ struct ShadowSoA {
   float4* d;  // direction
   float4* c;  // contribution (already multiplied by the path throughput)
   int32_t* path;
+};
+
+// Path replay records of a gradient render: for every path and bounce, the
+// material whose parameter the vertex depends on and the value the adjoint
+// needs (diffuse: radiance gathered before the albedo multiplied the
+// throughput; emitter: throughput times MIS weight). m < 0: no record.
+constexpr int kEmitTag = 1 << 30;
+struct GradRec {
+  int32_t* m;   // [bounce * cap + path]
+  float4* v;    // [bounce * cap + path]
+  int32_t* nb;  // bounces shaded per path
+  int cap;
 };
 
 // Device counters of a wave. cur/next alternate between [0] and [1].
@@ -240,7 +253,7 @@ __global__ void __launch_bounds__(256) k_shade(const ViewGPU* __restrict__ views
                                                  PathSoA ps, const int* __restrict__ qcur, int* __restrict__ qnext,
                                                  ShadowSoA sh, WaveCounters* cnt, int cur, int bounce,
                                                  float4* __restrict__ guide_nd, uint32_t* __restrict__ guide_c,
-                                                 const uint32_t* __restrict__ guide_jit) {
+                                                 const uint32_t* __restrict__ guide_jit, GradRec rec) {
   const int n = *((volatile int*)&cnt->q[cur]);
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -257,6 +270,8 @@ __global__ void __launch_bounds__(256) k_shade(const ViewGPU* __restrict__ views
       float3 L = f3(ps.lx[path], ps.ly[path], ps.lz[path]);
       const float t = ps.hit_t[path];
       const int slot = ps.hit_slot[path];
+      int rec_m = -1;
+      float3 rec_v = f3(0, 0, 0);
       if (slot < 0) {
         L = L + had(tp, background(d));
       } else {
@@ -321,10 +336,14 @@ __global__ void __launch_bounds__(256) k_shade(const ViewGPU* __restrict__ views
               w = power_heuristic(ppdf, lpdf);
             }
             L = L + had(tp, f3(M.er, M.eg, M.eb)) * w;
+            rec_m = m | kEmitTag;
+            rec_v = tp * w;
           } else {
             bool cont = true;
             float3 nd_dir = d, no = o;
             if (kind == BC_MAT_DIFFUSE) {
+              rec_m = m;
+              rec_v = L;  // everything added from here on carries this albedo once more
               if (wp.n_lights > 0) {  // directLight (renderer.go:1427-1465)
                 int li;
                 float sel;
@@ -424,6 +443,12 @@ __global__ void __launch_bounds__(256) k_shade(const ViewGPU* __restrict__ views
         }
       }
       ps.lx[path] = L.x; ps.ly[path] = L.y; ps.lz[path] = L.z;
+      if (rec.m) {
+        const size_t r = (size_t)bounce * rec.cap + path;
+        rec.m[r] = rec_m;
+        rec.v[r] = make_float4(rec_v.x, rec_v.y, rec_v.z, 0.0f);
+        rec.nb[path] = bounce + 1;
+      }
     }
     const int qn = warp_reserve(&cnt->q[cur ^ 1], alive);
     if (alive) qnext[qn] = path;
@@ -534,6 +559,60 @@ __global__ void k_accumulate(const BatchState* __restrict__ bs, const ViewGPU* _
   }
 }
 
+// ---- gradient (path replay) --------------------------------------------------------
+// After the last bounce of a wave every path knows its final radiance Lf. With
+// the adjoint d = dLoss/dImage(pixel) / spp of its pixel:
+//   diffuse vertex on material m : dL/d albedo_m = (Lf - L_before) / albedo_m
+//   emitter hit on material e    : dL/d emission_e = throughput * MIS weight
+// (everything a path gathers after the albedo of m multiplied its throughput is
+// linear in that albedo; Russian roulette probabilities are held fixed).
+// Per block sums in fp64 shared memory, one row of `partial` per block.
+__global__ void __launch_bounds__(256) k_gradient(const BatchState* __restrict__ bs, const ViewGPU* __restrict__ views,
+                                                  PathSoA ps, GradRec rec, GradArgs ga,
+                                                  const MatGPU* __restrict__ mats) {
+  extern __shared__ double sg[];
+  const int np3 = 3 * ga.n_params;
+  for (int k = threadIdx.x; k < np3; k += blockDim.x) sg[k] = 0.0;
+  __syncthreads();
+  const long long w0 = bs->w0;
+  const int n = (int)min((long long)bs->cap, bs->total - w0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const ViewGPU& V = views[ps.view[i]];
+    const float* dp = ga.dimg + 3 * (size_t)(V.pix_off + ps.pix[i]);
+    const float inv = 1.0f / (float)V.spp;
+    const float3 dl = f3(dp[0] * inv, dp[1] * inv, dp[2] * inv);
+    if (dl.x == 0.0f && dl.y == 0.0f && dl.z == 0.0f) continue;
+    const float3 Lf = f3(ps.lx[i], ps.ly[i], ps.lz[i]);
+    const int nb = rec.nb[i];
+    for (int b = 0; b < nb; b++) {
+      const size_t r = (size_t)b * rec.cap + i;
+      const int m = rec.m[r];
+      if (m < 0) continue;
+      const int mm = m & ~kEmitTag;
+      const int k = ga.mat2param[mm];
+      if (k < 0) continue;
+      const float4 v = rec.v[r];
+      float gx, gy, gz;
+      if (m & kEmitTag) {
+        gx = dl.x * v.x;
+        gy = dl.y * v.y;
+        gz = dl.z * v.z;
+      } else {
+        const MatGPU M = mats[mm];
+        gx = M.cr > 0.0f ? dl.x * ((Lf.x - v.x) / M.cr) : 0.0f;
+        gy = M.cg > 0.0f ? dl.y * ((Lf.y - v.y) / M.cg) : 0.0f;
+        gz = M.cb > 0.0f ? dl.z * ((Lf.z - v.z) / M.cb) : 0.0f;
+      }
+      atomicAdd(&sg[3 * k], (double)gx);
+      atomicAdd(&sg[3 * k + 1], (double)gy);
+      atomicAdd(&sg[3 * k + 2], (double)gz);
+    }
+  }
+  __syncthreads();
+  double* row = ga.partial + (size_t)blockIdx.x * np3;
+  for (int k = threadIdx.x; k < np3; k += blockDim.x) row[k] += sg[k];
+}
+
 __global__ void k_advance(BatchState* bs) {
   if (threadIdx.x == 0 && blockIdx.x == 0) bs->w0 = min(bs->total, bs->w0 + (long long)bs->cap);
 }
@@ -591,6 +670,10 @@ struct RenderBuffers {
   uint32_t* guide_c = nullptr; // compact guide
   uint32_t* guide_jit = nullptr;
   uint32_t* rgba = nullptr;
+  // path replay records (gradient renders)
+  bcgx::DevBuf rec;
+  bcgx::GradRec grec{};
+  int rec_bounces = 0, rec_cap = 0;
   // one wave as an instantiated CUDA graph, and the launch arguments it was captured with
   cudaGraphExec_t graph = nullptr;
   std::vector<uintptr_t> graph_key;
@@ -610,6 +693,7 @@ void destroy_render_buffers(bc_context* ctx) {
   rb->frame.release();
   rb->table.release();
   rb->staging.release();
+  rb->rec.release();
   delete rb;
   ctx->rb = nullptr;
 }
@@ -752,6 +836,8 @@ static int sm_count() {
   return sms;
 }
 
+int gradient_grid() { return sm_count() * 2; }
+
 static int persistent_grid(const void* fn, int block) {
   int per = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, 0);
@@ -763,10 +849,11 @@ struct WaveShape {
   int gen_grid, ext_grid, con_grid, shade_grid, acc_grid;
   int bounces;
   bool lights;
+  const GradArgs* grad;  // non-null: gradient render
 };
 
 template <int STACK, bool SPH>
-static WaveShape wave_shape(int cap, int bounces, bool lights) {
+static WaveShape wave_shape(int cap, int bounces, bool lights, const GradArgs* grad) {
   static int ext = 0, con = 0;
   if (!ext) ext = persistent_grid((const void*)k_extend<STACK, SPH>, 128);
   if (!con) con = persistent_grid((const void*)k_connect<STACK, SPH>, 128);
@@ -778,6 +865,7 @@ static WaveShape wave_shape(int cap, int bounces, bool lights) {
   w.acc_grid = sm_count() * 8;
   w.bounces = bounces;
   w.lights = lights;
+  w.grad = grad;
   return w;
 }
 
@@ -794,11 +882,15 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
     if (!e) e = cudaMemsetAsync(&c->shadow, 0, sizeof(int), st);
     if (e) return e;
     k_extend<STACK, SPH><<<w.ext_grid, 128, 0, st>>>(sc.sv, rb->views, rb->ps, rb->q[cur], c, cur, ctx->d_status);
+    const GradRec rec = w.grad ? rb->grec : GradRec{nullptr, nullptr, nullptr, 0};
     k_shade<<<w.shade_grid, 256, 0, st>>>(rb->views, ctx->ds.n_mats, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1], rb->sh,
-                                          c, cur, b, rb->guide_nd, rb->guide_c, rb->guide_jit);
+                                          c, cur, b, rb->guide_nd, rb->guide_c, rb->guide_jit, rec);
     if (w.lights) k_connect<STACK, SPH><<<w.con_grid, 128, 0, st>>>(sc.sv, rb->ps, rb->sh, c, ctx->d_status);
     cur ^= 1;
   }
+  if (w.grad)
+    k_gradient<<<gradient_grid(), 256, 3 * w.grad->n_params * sizeof(double), st>>>(rb->bs, rb->views, rb->ps,
+                                                                                  rb->grec, *w.grad, sc.mats);
   k_accumulate<<<w.acc_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr);
   k_advance<<<1, 32, 0, st>>>(rb->bs);
   return cudaGetLastError();
@@ -806,10 +898,11 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
 
 // Runs `n_waves` waves, through one captured CUDA graph when the option allows.
 template <int STACK, bool SPH>
-static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const ShadeScene& sc, int64_t n_waves) {
+static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const ShadeScene& sc, int64_t n_waves,
+                           const GradArgs* grad) {
   RenderBuffers* rb = ctx->rb;
   cudaStream_t st = ctx->stream;
-  const WaveShape w = wave_shape<STACK, SPH>(rb->cap, bounces, lights);
+  const WaveShape w = wave_shape<STACK, SPH>(rb->cap, bounces, lights, grad);
   const bool use_graph = ctx->render_graph != 0 && n_waves > 1;
   if (use_graph) {
     // every value the captured launches were given
@@ -827,6 +920,11 @@ static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const Shad
     add_bytes(&rb->ps, sizeof(rb->ps));
     add_bytes(&rb->sh, sizeof(rb->sh));
     add_bytes(&sc, sizeof(sc));
+    key.push_back((uintptr_t)(grad != nullptr));
+    if (grad) {
+      add_bytes(grad, sizeof(*grad));
+      add_bytes(&rb->grec, sizeof(rb->grec));
+    }
     if (!rb->graph || rb->graph_key != key) {
       if (rb->graph) cudaGraphExecDestroy(rb->graph);
       rb->graph = nullptr;
@@ -857,16 +955,6 @@ static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const Shad
   return BC_OK;
 }
 
-// One view of a render: what a caller asks for, before packing.
-struct ViewRequest {
-  int scene;
-  bc_camera cam;
-  bc_settings s;
-  int y0, rows;
-  long long pix_off;
-  bool want_guides;
-};
-
 static bc_status check_view(bc_context* ctx, const ViewRequest& r) {
   const bc_settings& s = r.s;
   if (r.scene < 0 || r.scene >= (int)ctx->ranges.size())
@@ -880,7 +968,8 @@ static bc_status check_view(bc_context* ctx, const ViewRequest& r) {
 
 // Renders the requested views into rb->sum (and guides); `frame_px` pixels of
 // frame buffers are kept. Leaves the per-view table in rb->views.
-static bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, size_t frame_px, int64_t* rays) {
+bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, size_t frame_px, int64_t* rays,
+                       const GradArgs* grad) {
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
   if (req.empty()) return set_error(ctx, BC_ERR_INVALID_ARG, "no views");
   bc_status bst;
@@ -929,6 +1018,24 @@ static bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& r
   const int cap = (int)std::max<long long>(1, std::min<long long>(total, ctx->render_wave_cap));
   if ((bst = ensure_paths(ctx, cap))) return bst;
   if ((bst = ensure_frame(ctx, frame_px))) return bst;
+  if (grad) {  // path replay records: one per path and bounce
+    if (max_bounces > kMaxGradBounces) return set_error(ctx, BC_ERR_INVALID_ARG, "gradient renders allow 64 bounces");
+    if (rb->rec_bounces < max_bounces || rb->rec_cap < rb->cap) {
+      const size_t per = sizeof(int32_t) + sizeof(float4);
+      cudaError_t e = rb->rec.ensure((size_t)max_bounces * rb->cap * per + rb->cap * sizeof(int32_t) + 4 * 256);
+      if (e) {
+        rb->rec_bounces = rb->rec_cap = 0;
+        return cuda_status(ctx, e, "path replay records");
+      }
+      char* p = (char*)rb->rec.p;
+      rb->grec.v = carve<float4>(p, (size_t)max_bounces * rb->cap);
+      rb->grec.m = carve<int32_t>(p, (size_t)max_bounces * rb->cap);
+      rb->grec.nb = carve<int32_t>(p, rb->cap);
+      rb->grec.cap = rb->cap;
+      rb->rec_bounces = max_bounces;
+      rb->rec_cap = rb->cap;
+    }
+  }
   BatchState bsh;
   bsh.w0 = 0;
   bsh.total = total;
@@ -986,14 +1093,14 @@ static bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& r
   const int stack = stack_variant(ctx->ds.stack_need);
   const bool sph = ctx->ds.has_spheres;
   if (stack == 64)
-    bst = sph ? run_waves<64, true>(ctx, max_bounces, lights, sc, n_waves)
-              : run_waves<64, false>(ctx, max_bounces, lights, sc, n_waves);
+    bst = sph ? run_waves<64, true>(ctx, max_bounces, lights, sc, n_waves, grad)
+              : run_waves<64, false>(ctx, max_bounces, lights, sc, n_waves, grad);
   else if (stack == 128)
-    bst = sph ? run_waves<128, true>(ctx, max_bounces, lights, sc, n_waves)
-              : run_waves<128, false>(ctx, max_bounces, lights, sc, n_waves);
+    bst = sph ? run_waves<128, true>(ctx, max_bounces, lights, sc, n_waves, grad)
+              : run_waves<128, false>(ctx, max_bounces, lights, sc, n_waves, grad);
   else
-    bst = sph ? run_waves<256, true>(ctx, max_bounces, lights, sc, n_waves)
-              : run_waves<256, false>(ctx, max_bounces, lights, sc, n_waves);
+    bst = sph ? run_waves<256, true>(ctx, max_bounces, lights, sc, n_waves, grad)
+              : run_waves<256, false>(ctx, max_bounces, lights, sc, n_waves, grad);
   if (bst) return bst;
   k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sum, rb->out);
   if (rb->want_sumsq) k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sumsq, rb->post_tmp);
@@ -1018,8 +1125,10 @@ static bc_status render_rows_device(bc_context* ctx, const bc_camera& cam, const
   r.want_guides = want_guides;
   if (s.width < 1 || s.height < 1 || (int64_t)s.width * s.height > (1 << 26))
     return set_error(ctx, BC_ERR_INVALID_ARG, "invalid render size, rows, spp or bounces");
-  return render_views(ctx, std::vector<ViewRequest>{r}, (size_t)s.width * s.height, rays);
+  return render_views(ctx, std::vector<ViewRequest>{r}, (size_t)s.width * s.height, rays, nullptr);
 }
+
+float* render_mean(bc_context* ctx) { return ctx->rb ? ctx->rb->out : nullptr; }
 
 bc_status run_post(bc_context* ctx, const bc_settings& s);  // post.cu
 
@@ -1139,7 +1248,7 @@ bc_status bc_render_batch(bc_context* ctx, const bc_view* views, int32_t n_views
   }
   if (px > (1LL << 30)) return set_error(ctx, BC_ERR_INVALID_ARG, "batch holds more than 2^30 pixels");
   int64_t rays = 0;
-  bc_status st = render_views(ctx, req, (size_t)px, &rays);
+  bc_status st = render_views(ctx, req, (size_t)px, &rays, nullptr);
   if (st) return st;
   RenderBuffers* rb = ctx->rb;
   cudaError_t e = cudaSuccess;

@@ -481,6 +481,83 @@ def run_batch(args):
     return 0
 
 
+def run_diff(args):
+    """Differentiation workload: 200k random triangles on 256 diffuse material
+    slots + 8 emissive quads, 512x512, 64 spp, 8 bounces (Russian roulette
+    off). Target = the true parameters at 1024 spp (rendered once, untimed).
+    A step is one iteration: bc_forward (parameters in, image + L2 loss) and
+    bc_backward (path replay, 256x3 albedo + 8x3 emission gradients out), plus a
+    sign-descent update on the host. value = seconds per iteration."""
+    import numpy as np
+    import bcgx
+    from bcgx import scenes
+    pb = scenes.diff_scene()
+    t0 = time.perf_counter()
+    scene = scenes.to_scene(pb.spec)
+    build_s = time.perf_counter() - t0
+    ctx = bcgx.Context(0)
+    ctx.upload(scene)
+    st_t = pb.settings.copy()
+    st_t.spp = 1024
+    ctx.diff_configure(pb.cam, st_t, pb.albedo_materials, pb.emission_materials)
+    target, _ = ctx.forward(pb.true_params, 0xBEAC0005)
+    ctx.diff_configure(pb.cam, pb.settings, pb.albedo_materials, pb.emission_materials)
+    ctx.diff_set_target(target)
+    params = pb.init_params.copy()
+    na = len(pb.albedo_materials)
+
+    def iteration(it):
+        t = time.perf_counter()
+        _, loss = ctx.forward(params, 0xBEAC0005 + 1 + it, want_image=False)
+        tf = time.perf_counter()
+        ga, ge = ctx.backward()
+        tb = time.perf_counter()
+        params[:na] = np.clip(params[:na] - 0.01 * np.sign(ga), 0.01, 0.99)
+        params[na:] = np.maximum(params[na:] - 0.1 * np.sign(ge), 0.0)
+        return tb - t, tf - t, tb - tf, loss
+
+    for it in range(args.warmup):
+        iteration(it)
+    clocks = ClockSampler(0)
+    clocks.start()
+    times, tfs, tbs, losses = [], [], [], []
+    for it in range(args.steps):
+        dt, tf, tb, loss = iteration(args.warmup + it)
+        times.append(dt)
+        tfs.append(tf)
+        tbs.append(tb)
+        losses.append(loss)
+    clk = clocks.stop()
+    s_iter = sum(times) / args.steps
+    line = {"metric": "adjoint s/iter", "value": s_iter, "unit": "s/iter", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * s_iter, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 paths, f64 gradient sums", "data": "synthetic, seeded (seed 0xBEAC0005)",
+            "config": {"workload": "differentiation: 200k tris, 256 albedo slots + 8 emitters, 512x512, 64 spp, "
+                                   "8 bounces, RR off, L2 loss vs 1024-spp target",
+                       "host_bvh_build_s": round(build_s, 2)},
+            "forward_s": sum(tfs) / args.steps, "backward_s": sum(tbs) / args.steps,
+            "loss_first_last": [losses[0], losses[-1]],
+            "e2e": {"value": s_iter, "unit": "s/iter", "h2d_bytes_per_step": 4 * params.size,
+                    "d2h_bytes_per_step": 4 * params.size + 8},
+            "gpu_launches": None, "clocks": clk}
+    if not args.no_cpu_baseline:
+        import oracle
+        ref = oracle.OracleScene.from_spec(pb.spec)
+        cst = pb.settings.copy()
+        cst.spp = 4
+        t0 = time.perf_counter()
+        out = ref.render(pb.cam, cst, seed=7, threads=0)
+        dt = time.perf_counter() - t0
+        fwd_s = dt * pb.settings.spp / cst.spp
+        line["cpu_baseline"] = {"value": 2 * fwd_s, "unit": "s/iter", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"oracle forward 512x512 at 4 spp ({dt:.1f} s, "
+                                          f"{out['stats']['segments'] / dt / 1e6:.1f} Mseg/s), scaled to 64 spp; "
+                                          "an iteration counted as two forwards (forward + replay)"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     global N_TRIS, N_RAYS
     ap = argparse.ArgumentParser()
@@ -493,7 +570,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
     ap.add_argument("--minblocks", type=int, default=0, help="ray-cast register variant (1, 6, 8; 0 = library default)")
     ap.add_argument("--fast", action="store_true", help="plain fp32 closest hit instead of the exact contract")
-    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch"],
+    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch", "diff"],
                     help="raycast (default, the headline line) or a render workload")
     ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
     ap.add_argument("--rmse", action="store_true", help="render workloads: RMSE against a converged image")
@@ -506,6 +583,8 @@ def main():
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "diff":
+        return run_diff(args)
     if args.workload != "raycast":
         return run_render(args)
     return run_gpu(args)

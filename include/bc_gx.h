@@ -238,6 +238,52 @@ typedef struct bc_view {
 bc_status bc_render_batch(bc_context* ctx, const bc_view* views, int32_t n_views, float* const* linear_out,
                           int64_t* rays_out);
 
+/* ---- differentiable rendering ------------------------------------------ */
+
+/*
+ * Gradient of an image loss with respect to material parameters by path
+ * replay: bc_backward re-traces the paths of the last bc_forward (same seed,
+ * same random streams) and, once each path's radiance is known, adds for every
+ * diffuse vertex on an albedo parameter d * (L_path - L_before) / albedo and
+ * for every emitter hit on an emission parameter d * throughput * MIS weight,
+ * d being dLoss/dImage of the path's pixel over spp. Russian roulette
+ * probabilities are held fixed (set rr_depth >= bounces for the exact
+ * derivative of the sample estimator). No reference counterpart: the
+ * reference renders forward only (renderer.go:1484-1563).
+ *
+ * Parameters, in order: n_albedo albedo RGB triples (diffuse materials
+ * albedo_materials[i]), then n_emission emission RGB triples (emissive
+ * materials emission_materials[i], not used by sphere lights). At most 1024.
+ * The view renders scene 0 of the resident set; settings->firefly_clamp must
+ * be 0 and settings->bounces at most 64.
+ */
+typedef struct bc_diff_desc {
+  bc_camera camera;
+  bc_settings settings;
+  int32_t n_albedo;
+  const int32_t* albedo_materials;
+  int32_t n_emission;
+  const int32_t* emission_materials;
+} bc_diff_desc;
+
+bc_status bc_diff_configure(bc_context* ctx, const bc_diff_desc* desc);
+/* Target image of the L2 loss, width*height RGB floats:
+ * loss = sum over pixels and channels of (image - target)^2 / (3 * width * height). */
+bc_status bc_diff_set_target(bc_context* ctx, const float* target);
+/*
+ * Writes `params` (3 * (n_albedo + n_emission) floats) into the resident
+ * materials and renders the configured view with path seed `seed`.
+ * image_out (may be NULL): width*height RGB mean radiance. loss_out (may be
+ * NULL; needs a target): the L2 loss.
+ */
+bc_status bc_forward(bc_context* ctx, const float* params, uint64_t seed, float* image_out, double* loss_out);
+/*
+ * Gradient of the loss at the last bc_forward. dloss_dimage: width*height RGB
+ * floats, or NULL for the L2 loss against the target. grad_albedo:
+ * 3 * n_albedo floats, grad_emission: 3 * n_emission floats (either may be NULL).
+ */
+bc_status bc_backward(bc_context* ctx, const float* dloss_dimage, float* grad_albedo, float* grad_emission);
+
 /*
  * The post stack alone, on caller buffers (the part of RenderState.Start that
  * follows the render call, renderer.go:2844-2854 and 2890-2895): a-trous denoise

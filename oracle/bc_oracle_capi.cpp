@@ -59,6 +59,16 @@ int orc_add_material(void* sp, int kind, const double* color, double rough, doub
   m.emission = ld3(emission);
   return ((Scene*)sp)->add_material(m);
 }
+// Replaces the color and/or emission of material idx in place (the Go Scene's
+// Materials slice is mutable, renderer.go:94-101, 242-245). The sphere-light CDF
+// of build() is not recomputed. Returns 0, or -1 for an index out of range.
+int orc_set_material(void* sp, int idx, const double* color, const double* emission) {
+  Scene* s = (Scene*)sp;
+  if (idx < 0 || idx >= (int)s->materials.size()) return -1;
+  if (color) s->materials[idx].color = ld3(color);
+  if (emission) s->materials[idx].emission = ld3(emission);
+  return 0;
+}
 void orc_add_sphere(void* sp, const double* c, double r, int mat) { ((Scene*)sp)->add_sphere(ld3(c), r, mat); }
 void orc_add_triangles(void* sp, int64_t n, const double* v9, const int32_t* mats) {
   Scene* s = (Scene*)sp;

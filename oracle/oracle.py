@@ -29,6 +29,7 @@ _SIG = [
     ("orc_scene_new", C.c_void_p, []), ("orc_scene_free", None, [C.c_void_p]),
     ("orc_scene_set_bvh", None, [C.c_void_p, C.c_char_p, C.c_int, C.c_int]),
     ("orc_add_material", C.c_int, [C.c_void_p, C.c_int, f64p, C.c_double, C.c_double, f64p]),
+    ("orc_set_material", C.c_int, [C.c_void_p, C.c_int, f64p, f64p]),
     ("orc_add_sphere", None, [C.c_void_p, f64p, C.c_double, C.c_int]),
     ("orc_add_triangles", None, [C.c_void_p, C.c_int64, f64p, i32p]),
     ("orc_build", None, [C.c_void_p]), ("orc_refit", None, [C.c_void_p]),
@@ -125,6 +126,14 @@ class OracleScene:
     def add_material(self, kind, color, rough, ior, emission):
         return lib().orc_add_material(self.h, int(kind), _p(_f64(color), C.c_double), float(rough), float(ior),
                                       _p(_f64(emission), C.c_double))
+
+    def set_material(self, idx, color=None, emission=None):
+        """In-place color / emission change (the light CDF of build() is kept)."""
+        c = _f64(color) if color is not None else None
+        e = _f64(emission) if emission is not None else None
+        rc = lib().orc_set_material(self.h, int(idx), _p(c, C.c_double), _p(e, C.c_double))
+        if rc != 0:
+            raise IndexError(f"material {idx} out of range")
 
     def add_sphere(self, c, r, mat):
         lib().orc_add_sphere(self.h, _p(_f64(c), C.c_double), float(r), int(mat))

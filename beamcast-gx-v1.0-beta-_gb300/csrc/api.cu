@@ -388,6 +388,11 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     ctx->render_graph = (int)value;
     return BC_OK;
   }
+  if (n == "render_engine") {
+    if (value != 0 && value != 1) return set_error(ctx, BC_ERR_INVALID_ARG, "render_engine must be 0 or 1");
+    ctx->render_engine = (int)value;
+    return BC_OK;
+  }
   return set_error(ctx, BC_ERR_INVALID_ARG, "unknown option " + n);
 }
 
@@ -398,6 +403,7 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
   if (n == "raycast_exact") { *value = ctx->raycast_exact; return BC_OK; }
   if (n == "render_wave_cap") { *value = ctx->render_wave_cap; return BC_OK; }
   if (n == "render_graph") { *value = ctx->render_graph; return BC_OK; }
+  if (n == "render_engine") { *value = ctx->render_engine; return BC_OK; }
   return BC_ERR_INVALID_ARG;
 }
 

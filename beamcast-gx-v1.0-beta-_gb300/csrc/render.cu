@@ -128,6 +128,38 @@ __device__ __forceinline__ int view_of(const ViewGPU* __restrict__ views, int n_
 }
 
 // ---- generate --------------------------------------------------------------
+// Primary ray of sample s of pixel (x, y) and the path's stream (adaptivePixel's
+// sample loop, renderer.go:1940-1950): Halton / R2 jitter rotated per pixel, or
+// random jitter; fp64 camera arithmetic, rounded to fp32 once.
+__device__ __forceinline__ void primary_ray(const ViewGPU& V, int x, int y, int s, const double2* __restrict__ seq,
+                                            float3* o, float3* d, Pcg32* rng, double* jx, double* jy) {
+  *rng = make_path_rng(V.seed, (uint64_t)y * (uint64_t)V.W + (uint64_t)x, (uint64_t)s);
+  if (V.sampler != BC_SAMPLER_RANDOM && s < V.nseq) {
+    double rx, ry;
+    pixel_rotation(x, y, &rx, &ry);
+    const double2 q = seq[V.seq_off + s];
+    double a = q.x + rx, b = q.y + ry;
+    *jx = a - floor(a);
+    *jy = b - floor(b);
+  } else {
+    *jx = (double)rng->uniform();
+    *jy = (double)rng->uniform();
+  }
+  const double u = ((double)x + *jx) / (double)max(V.W - 1, 1);
+  const double vv = ((double)(V.H - 1 - y) + *jy) / (double)max(V.H - 1, 1);
+  float dd[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) dd[k] = (float)(((V.lower[k] + V.horiz[k] * u) + V.vert[k] * vv) - V.origin[k]);
+  *o = f3((float)V.origin[0], (float)V.origin[1], (float)V.origin[2]);
+  *d = f3(dd[0], dd[1], dd[2]);
+}
+
+__device__ __forceinline__ uint32_t jitter_word(double jx, double jy) {
+  uint32_t a = (uint32_t)rintf(fminf(fmaxf((float)jx, 0.0f), 1.0f) * 65535.0f);
+  uint32_t b = (uint32_t)rintf(fminf(fmaxf((float)jy, 0.0f), 1.0f) * 65535.0f);
+  return (b << 16) | a;
+}
+
 // seq: the views' sample tables, (x, y) pairs
 __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __restrict__ views, PathSoA ps,
                            int* __restrict__ queue, const double2* __restrict__ seq,
@@ -143,26 +175,12 @@ __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __r
   const long long local = g - V.path_off;
   const int s = (int)(local / V.npix), p = (int)(local - (long long)s * V.npix);
   const int x = p % V.W, y = V.y0 + p / V.W;
-  Pcg32 rng = make_path_rng(V.seed, (uint64_t)y * (uint64_t)V.W + (uint64_t)x, (uint64_t)s);
+  float3 o, d;
+  Pcg32 rng;
   double jx, jy;
-  if (V.sampler != BC_SAMPLER_RANDOM && s < V.nseq) {
-    double rx, ry;
-    pixel_rotation(x, y, &rx, &ry);
-    const double2 q = seq[V.seq_off + s];
-    double a = q.x + rx, b = q.y + ry;
-    jx = a - floor(a);
-    jy = b - floor(b);
-  } else {
-    jx = (double)rng.uniform();
-    jy = (double)rng.uniform();
-  }
-  const double u = ((double)x + jx) / (double)max(V.W - 1, 1);
-  const double vv = ((double)(V.H - 1 - y) + jy) / (double)max(V.H - 1, 1);
-  float d[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) d[k] = (float)(((V.lower[k] + V.horiz[k] * u) + V.vert[k] * vv) - V.origin[k]);
-  ps.ox[i] = (float)V.origin[0]; ps.oy[i] = (float)V.origin[1]; ps.oz[i] = (float)V.origin[2];
-  ps.dx[i] = d[0]; ps.dy[i] = d[1]; ps.dz[i] = d[2];
+  primary_ray(V, x, y, s, seq, &o, &d, &rng, &jx, &jy);
+  ps.ox[i] = o.x; ps.oy[i] = o.y; ps.oz[i] = o.z;
+  ps.dx[i] = d.x; ps.dy[i] = d.y; ps.dz[i] = d.z;
   ps.tx[i] = 1.0f; ps.ty[i] = 1.0f; ps.tz[i] = 1.0f;
   ps.lx[i] = 0.0f; ps.ly[i] = 0.0f; ps.lz[i] = 0.0f;
   ps.ppdf[i] = 0.0f;
@@ -173,11 +191,7 @@ __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __r
   ps.pix[i] = p;
   ps.samp[i] = s;
   queue[i] = i;
-  if (s == 0 && V.want_guides) {
-    uint32_t a = (uint32_t)rintf(fminf(fmaxf((float)jx, 0.0f), 1.0f) * 65535.0f);
-    uint32_t b = (uint32_t)rintf(fminf(fmaxf((float)jy, 0.0f), 1.0f) * 65535.0f);
-    guide_jit[V.pix_off + p] = (b << 16) | a;
-  }
+  if (s == 0 && V.want_guides) guide_jit[V.pix_off + p] = jitter_word(jx, jy);
 }
 
 // ---- extend ----------------------------------------------------------------
@@ -249,214 +263,288 @@ __device__ __forceinline__ float light_dir_pdf(const ShadeScene& sc, int n_light
   return sel * dist2 / (cosL * area);
 }
 
+// Path state between bounces as the shading step sees it. The wavefront
+// kernels keep it in the SoA arrays (SoAPath loads what a vertex needs and
+// stores what changes); the one-kernel renderer keeps it in registers (RegPath).
+struct SoAPath {
+  const PathSoA& ps;
+  int path;
+  float3 o, d, tp, L;
+  Pcg32 rng;
+  uint32_t flags;
+  float ppdf;
+  __device__ SoAPath(const PathSoA& p, int i) : ps(p), path(i) {
+    o = f3(ps.ox[i], ps.oy[i], ps.oz[i]);
+    d = f3(ps.dx[i], ps.dy[i], ps.dz[i]);
+    tp = f3(ps.tx[i], ps.ty[i], ps.tz[i]);
+    L = f3(ps.lx[i], ps.ly[i], ps.lz[i]);
+  }
+  __device__ __forceinline__ void load_vertex() {  // only a path that hit a valid material needs these
+    rng.state = ps.rs[path];
+    rng.inc = ps.ri[path];
+    flags = ps.flags[path];
+    ppdf = ps.ppdf[path];
+  }
+  __device__ __forceinline__ float3 prev() const { return f3(ps.px[path], ps.py[path], ps.pz[path]); }
+  __device__ __forceinline__ void set_prev(float3 p) { ps.px[path] = p.x; ps.py[path] = p.y; ps.pz[path] = p.z; }
+  __device__ __forceinline__ void store_continuation(float3 no, float3 nd) {
+    ps.ox[path] = no.x; ps.oy[path] = no.y; ps.oz[path] = no.z;
+    ps.dx[path] = nd.x; ps.dy[path] = nd.y; ps.dz[path] = nd.z;
+    ps.tx[path] = tp.x; ps.ty[path] = tp.y; ps.tz[path] = tp.z;
+    ps.flags[path] = flags;
+    ps.ppdf[path] = ppdf;
+    ps.rs[path] = rng.state;
+  }
+};
+
+struct RegPath {
+  float3 o, d, tp, L, pv;
+  Pcg32 rng;
+  uint32_t flags;
+  float ppdf;
+  __device__ __forceinline__ void load_vertex() {}
+  __device__ __forceinline__ float3 prev() const { return pv; }
+  __device__ __forceinline__ void set_prev(float3 p) { pv = p; }
+  __device__ __forceinline__ void store_continuation(float3 no, float3 nd) {
+    o = no;
+    d = nd;
+  }
+};
+
+// What a vertex asks of the caller: continue (state already advanced), trace
+// a shadow ray, keep a path replay record.
+struct VertexOut {
+  bool alive, shadow;
+  float4 so, sd, scon;  // shadow ray: origin + tmax, direction + scene root, contribution
+  int rec_m;
+  float3 rec_v;
+};
+
+// Guide outputs of a path's first vertex (sample 0 only).
+struct GuideOut {
+  float4* nd;
+  uint32_t* c;
+  const uint32_t* jit;
+  long long px;  // frame pixel, < 0: no guide
+};
+
+// One vertex of trace() (renderer.go:1497-1560) for a path whose extension ray
+// hit `slot` at fp32 distance t (slot < 0: miss). Updates s.L / s.tp and, when
+// the path continues, its next ray (store_continuation).
+template <class P>
+__device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, const ShadeScene& sc, P& s, float t,
+                                             int slot, int bounce, const GuideOut& gd, VertexOut& out) {
+  out.alive = false;
+  out.shadow = false;
+  out.rec_m = -1;
+  out.rec_v = f3(0, 0, 0);
+  const int rr_depth = wp.rr_depth < 1 ? 4 : wp.rr_depth;
+  const float3 o = s.o, d = s.d;
+  float3 tp = s.tp;
+  float3 L = s.L;
+  if (slot < 0) {
+    L = L + had(tp, background(d));
+  } else {
+    const float4 nrm = __ldg(sc.sv.snorm + slot);
+    const int m = __float_as_int(nrm.w);
+    if (m >= 0 && m < n_mats) {
+      s.load_vertex();
+      Pcg32 rng = s.rng;
+      uint32_t flags = s.flags;
+      float ppdf = s.ppdf;
+      const float3 p = o + d * t;
+      const float4 r2 = __ldg(sc.sv.tri + 3 * slot + 2);
+      const bool sphere = r2.w < 0.0f;
+      float3 N;
+      bool front;
+      float radius = 0.0f;
+      if (sphere) {  // sphereHitAccel normal (renderer.go:670-676)
+        const float4 c = __ldg(sc.sv.tri + 3 * slot);
+        radius = c.w;
+        float3 outward = (p - f3(c.x, c.y, c.z)) * (1.0f / c.w);
+        front = dot3(d, outward) < 0.0f;
+        N = front ? outward : outward * -1.0f;
+      } else {
+        N = f3(nrm.x, nrm.y, nrm.z);
+        front = dot3(d, N) < 0.0f;
+        if (!front) N = N * -1.0f;
+      }
+      const MatGPU M = sc.mats[m];
+      const int kind = (int)M.kind;
+      if (gd.px >= 0) {
+        gd.nd[gd.px] = make_float4(N.x, N.y, N.z, t);
+        // compact guide (gpu_opencl_windows.go:791-797): Euclidean depth,
+        // octahedral normal 10:10, material 11 bits, valid bit, jitter
+        const float dl = sqrtf(dot3(d, d));
+        float3 q = N * (1.0f / (fabsf(N.x) + fabsf(N.y) + fabsf(N.z) + 1e-20f));
+        float px = q.x, py = q.y;
+        if (q.z < 0.0f) {
+          float ax = 1.0f - fabsf(q.y), ay = 1.0f - fabsf(q.x);
+          px = copysignf(ax, q.x);
+          py = copysignf(ay, q.y);
+        }
+        px = fminf(fmaxf(px * 0.5f + 0.5f, 0.0f), 1.0f);
+        py = fminf(fmaxf(py * 0.5f + 0.5f, 0.0f), 1.0f);
+        const uint32_t qx = (uint32_t)rintf(px * 1023.0f), qy = (uint32_t)rintf(py * 1023.0f);
+        const uint32_t mm = (uint32_t)min(max(m, 0), 2047);
+        uint32_t* g = gd.c + 3 * (size_t)gd.px;
+        g[0] = __float_as_uint(t * dl);
+        g[1] = 0x80000000u | (mm << 20) | (qy << 10) | qx;
+        g[2] = gd.jit[gd.px];
+      }
+      if (kind == BC_MAT_EMISSIVE) {
+        float w = 1.0f;
+        if (wp.mis && (flags & 1u)) {  // lightDirectionalPDF is 0 for triangles
+          float lpdf = 0.0f;
+          if (sphere) {
+            const int prim = __ldg(sc.sv.slot_prim + slot);
+            lpdf = light_dir_pdf(sc, wp.n_lights, wp.power, prim, radius, s.prev(), p, N);
+          }
+          w = power_heuristic(ppdf, lpdf);
+        }
+        L = L + had(tp, f3(M.er, M.eg, M.eb)) * w;
+        out.rec_m = m | kEmitTag;
+        out.rec_v = tp * w;
+      } else {
+        bool cont = true;
+        float3 nd_dir = d, no = o;
+        if (kind == BC_MAT_DIFFUSE) {
+          out.rec_m = m;
+          out.rec_v = L;  // everything added from here on carries this albedo once more
+          if (wp.n_lights > 0) {  // directLight (renderer.go:1427-1465)
+            int li;
+            float sel;
+            if (!wp.power) {  // rng.Intn (in fp64 so the index matches the CPU draw)
+              li = min((int)((double)rng.uniform() * (double)wp.n_lights), wp.n_lights - 1);
+              sel = 1.0f / (float)wp.n_lights;
+            } else {  // sort.Search over LightCDF
+              const double r = (double)rng.uniform();
+              int lo = 0, hi = wp.n_lights;
+              while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (!(__ldg(&sc.lights[wp.light_off + mid].cdf) >= r)) lo = mid + 1; else hi = mid;
+              }
+              li = min(lo, wp.n_lights - 1);
+              sel = __ldg(&sc.lights[wp.light_off + li].select_pdf);
+            }
+            const LightGPU Lg = sc.lights[wp.light_off + li];
+            const float3 ln = sel > 0.0f ? rand_unit_vector(rng) : f3(0, 0, 1);
+            const float3 q = f3(Lg.cx, Lg.cy, Lg.cz) + ln * Lg.r;
+            const float3 to = q - p;
+            const float dist2 = dot3(to, to);
+            if (dist2 >= 1e-8f && sel > 0.0f) {
+              const float3 ld = unit3(to);
+              const float ndl = fmaxf(0.0f, dot3(N, ld));
+              const float cosL = fmaxf(0.0f, dot3(ln * -1.0f, ld));
+              if (ndl > 0.0f && cosL > 0.0f) {
+                const float area = 4.0f * kPi * Lg.r * Lg.r;
+                const float lightPDF = sel * dist2 / (cosL * area);
+                if (lightPDF > 0.0f) {
+                  const float bsdfPDF = ndl / kPi;
+                  const float w = wp.mis ? power_heuristic(lightPDF, bsdfPDF) : 1.0f;
+                  const float3 f = f3(M.cr, M.cg, M.cb) * (1.0f / kPi);
+                  const float3 contrib = had(tp, had(f, f3(Lg.er, Lg.eg, Lg.eb)) * (ndl * w / lightPDF));
+                  const float3 from = p + N * 2e-4f;  // visible (renderer.go:1333-1341)
+                  const float3 sdv = q - from;
+                  const float sd2 = dot3(sdv, sdv);
+                  if (sd2 < 1e-12f) {
+                    L = L + contrib;
+                  } else {
+                    const float dist = sqrtf(sd2);
+                    const float3 dirn = sdv * (1.0f / dist);
+                    out.shadow = true;
+                    out.so = make_float4(from.x, from.y, from.z, dist - 1e-4f);
+                    out.sd = make_float4(dirn.x, dirn.y, dirn.z, __int_as_float(wp.root));
+                    out.scon = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
+                  }
+                }
+              }
+            }
+          }
+          tp = had(tp, f3(M.cr, M.cg, M.cb));
+          nd_dir = rand_cos_hemisphere(N, rng);
+          flags |= 1u;
+          ppdf = fmaxf(0.0f, dot3(N, nd_dir)) / kPi;
+          s.set_prev(p);
+          no = p + N * 2e-4f;
+        } else if (kind == BC_MAT_METAL) {
+          const float rough = fminf(fmaxf(M.rough, 0.0f), 1.0f);
+          nd_dir = unit3(reflect3(unit3(d), N) + rand_in_unit_sphere(rng) * rough);
+          if (dot3(nd_dir, N) <= 0.0f) {
+            cont = false;
+          } else {
+            flags &= ~1u;
+            tp = had(tp, f3(M.cr, M.cg, M.cb));
+            no = p + N * 2e-4f;
+          }
+        } else {  // glass
+          float eta = M.ior;
+          if (eta <= 1.0f) eta = 1.5f;
+          const float ratio = front ? 1.0f / eta : eta;
+          const float3 un = unit3(d);
+          const float cosT = fminf(dot3(un * -1.0f, N), 1.0f);
+          const float sinT = sqrtf(fmaxf(0.0f, 1.0f - cosT * cosT));
+          if (ratio * sinT > 1.0f || schlick(cosT, ratio) > rng.uniform())
+            nd_dir = reflect3(un, N);
+          else
+            nd_dir = refract3(un, N, ratio);
+          flags &= ~1u;
+          tp = had(tp, f3(M.cr, M.cg, M.cb));
+          no = p + nd_dir * 2e-4f;
+        }
+        if (cont && bounce >= rr_depth) {  // Russian roulette (renderer.go:1550-1560)
+          const float pr = fminf(fmaxf(maxcomp(tp), 0.08f), 0.95f);
+          if (rng.uniform() > pr) cont = false;
+          else tp = tp * (1.0f / pr);
+        }
+        if (cont && bounce + 1 < wp.bounces) {
+          out.alive = true;
+          s.tp = tp;
+          s.flags = flags;
+          s.ppdf = ppdf;
+          s.rng = rng;
+          s.store_continuation(no, nd_dir);
+        }
+      }
+    }
+  }
+  s.L = L;
+}
+
 __global__ void __launch_bounds__(256) k_shade(const ViewGPU* __restrict__ views, int n_mats, ShadeScene sc,
-                                                 PathSoA ps, const int* __restrict__ qcur, int* __restrict__ qnext,
-                                                 ShadowSoA sh, WaveCounters* cnt, int cur, int bounce,
-                                                 float4* __restrict__ guide_nd, uint32_t* __restrict__ guide_c,
-                                                 const uint32_t* __restrict__ guide_jit, GradRec rec) {
+                                               PathSoA ps, const int* __restrict__ qcur, int* __restrict__ qnext,
+                                               ShadowSoA sh, WaveCounters* cnt, int cur, int bounce,
+                                               float4* __restrict__ guide_nd, uint32_t* __restrict__ guide_c,
+                                               const uint32_t* __restrict__ guide_jit, GradRec rec) {
   const int n = *((volatile int*)&cnt->q[cur]);
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
     const int idx = base + threadIdx.x;
     const int path = idx < n ? qcur[idx] : -1;
-    bool alive = false, shadow = false;
-    float4 so = make_float4(0, 0, 0, 0), sd = so, scon = so;
+    VertexOut out;
+    out.alive = false;
+    out.shadow = false;
     if (path >= 0) {
       const ViewGPU& wp = views[ps.view[path]];
-      const int rr_depth = wp.rr_depth < 1 ? 4 : wp.rr_depth;
-      float3 o = f3(ps.ox[path], ps.oy[path], ps.oz[path]);
-      float3 d = f3(ps.dx[path], ps.dy[path], ps.dz[path]);
-      float3 tp = f3(ps.tx[path], ps.ty[path], ps.tz[path]);
-      float3 L = f3(ps.lx[path], ps.ly[path], ps.lz[path]);
-      const float t = ps.hit_t[path];
-      const int slot = ps.hit_slot[path];
-      int rec_m = -1;
-      float3 rec_v = f3(0, 0, 0);
-      if (slot < 0) {
-        L = L + had(tp, background(d));
-      } else {
-        const float4 nrm = __ldg(sc.sv.snorm + slot);
-        const int m = __float_as_int(nrm.w);
-        if (m >= 0 && m < n_mats) {
-          Pcg32 rng;
-          rng.state = ps.rs[path];
-          rng.inc = ps.ri[path];
-          uint32_t flags = ps.flags[path];
-          float ppdf = ps.ppdf[path];
-          const float3 p = o + d * t;
-          const float4 r2 = __ldg(sc.sv.tri + 3 * slot + 2);
-          const bool sphere = r2.w < 0.0f;
-          float3 N;
-          bool front;
-          float radius = 0.0f;
-          if (sphere) {  // sphereHitAccel normal (renderer.go:670-676)
-            const float4 c = __ldg(sc.sv.tri + 3 * slot);
-            radius = c.w;
-            float3 outward = (p - f3(c.x, c.y, c.z)) * (1.0f / c.w);
-            front = dot3(d, outward) < 0.0f;
-            N = front ? outward : outward * -1.0f;
-          } else {
-            N = f3(nrm.x, nrm.y, nrm.z);
-            front = dot3(d, N) < 0.0f;
-            if (!front) N = N * -1.0f;
-          }
-          const MatGPU M = sc.mats[m];
-          const int kind = (int)M.kind;
-          if (bounce == 0 && wp.want_guides && ps.samp[path] == 0) {
-            const int gp = ps.pix[path];
-            guide_nd[wp.pix_off + gp] = make_float4(N.x, N.y, N.z, t);
-            // compact guide (gpu_opencl_windows.go:791-797): Euclidean depth,
-            // octahedral normal 10:10, material 11 bits, valid bit, jitter
-            const float dl = sqrtf(dot3(d, d));
-            float3 q = N * (1.0f / (fabsf(N.x) + fabsf(N.y) + fabsf(N.z) + 1e-20f));
-            float px = q.x, py = q.y;
-            if (q.z < 0.0f) {
-              float ax = 1.0f - fabsf(q.y), ay = 1.0f - fabsf(q.x);
-              px = copysignf(ax, q.x);
-              py = copysignf(ay, q.y);
-            }
-            px = fminf(fmaxf(px * 0.5f + 0.5f, 0.0f), 1.0f);
-            py = fminf(fmaxf(py * 0.5f + 0.5f, 0.0f), 1.0f);
-            const uint32_t qx = (uint32_t)rintf(px * 1023.0f), qy = (uint32_t)rintf(py * 1023.0f);
-            const uint32_t mm = (uint32_t)min(max(m, 0), 2047);
-            uint32_t* g = guide_c + 3 * (size_t)(wp.pix_off + gp);
-            g[0] = __float_as_uint(t * dl);
-            g[1] = 0x80000000u | (mm << 20) | (qy << 10) | qx;
-            g[2] = guide_jit[wp.pix_off + gp];
-          }
-          if (kind == BC_MAT_EMISSIVE) {
-            float w = 1.0f;
-            if (wp.mis && (flags & 1u)) {  // lightDirectionalPDF is 0 for triangles
-              float lpdf = 0.0f;
-              if (sphere) {
-                const int prim = __ldg(sc.sv.slot_prim + slot);
-                lpdf = light_dir_pdf(sc, wp.n_lights, wp.power, prim, radius,
-                                     f3(ps.px[path], ps.py[path], ps.pz[path]), p, N);
-              }
-              w = power_heuristic(ppdf, lpdf);
-            }
-            L = L + had(tp, f3(M.er, M.eg, M.eb)) * w;
-            rec_m = m | kEmitTag;
-            rec_v = tp * w;
-          } else {
-            bool cont = true;
-            float3 nd_dir = d, no = o;
-            if (kind == BC_MAT_DIFFUSE) {
-              rec_m = m;
-              rec_v = L;  // everything added from here on carries this albedo once more
-              if (wp.n_lights > 0) {  // directLight (renderer.go:1427-1465)
-                int li;
-                float sel;
-                if (!wp.power) {  // rng.Intn (in fp64 so the index matches the CPU draw)
-                  li = min((int)((double)rng.uniform() * (double)wp.n_lights), wp.n_lights - 1);
-                  sel = 1.0f / (float)wp.n_lights;
-                } else {  // sort.Search over LightCDF
-                  const double r = (double)rng.uniform();
-                  int lo = 0, hi = wp.n_lights;
-                  while (lo < hi) {
-                    int mid = (lo + hi) >> 1;
-                    if (!(__ldg(&sc.lights[wp.light_off + mid].cdf) >= r)) lo = mid + 1; else hi = mid;
-                  }
-                  li = min(lo, wp.n_lights - 1);
-                  sel = __ldg(&sc.lights[wp.light_off + li].select_pdf);
-                }
-                const LightGPU Lg = sc.lights[wp.light_off + li];
-                const float3 ln = sel > 0.0f ? rand_unit_vector(rng) : f3(0, 0, 1);
-                const float3 q = f3(Lg.cx, Lg.cy, Lg.cz) + ln * Lg.r;
-                const float3 to = q - p;
-                const float dist2 = dot3(to, to);
-                if (dist2 >= 1e-8f && sel > 0.0f) {
-                  const float3 ld = unit3(to);
-                  const float ndl = fmaxf(0.0f, dot3(N, ld));
-                  const float cosL = fmaxf(0.0f, dot3(ln * -1.0f, ld));
-                  if (ndl > 0.0f && cosL > 0.0f) {
-                    const float area = 4.0f * kPi * Lg.r * Lg.r;
-                    const float lightPDF = sel * dist2 / (cosL * area);
-                    if (lightPDF > 0.0f) {
-                      const float bsdfPDF = ndl / kPi;
-                      const float w = wp.mis ? power_heuristic(lightPDF, bsdfPDF) : 1.0f;
-                      const float3 f = f3(M.cr, M.cg, M.cb) * (1.0f / kPi);
-                      const float3 contrib = had(tp, had(f, f3(Lg.er, Lg.eg, Lg.eb)) * (ndl * w / lightPDF));
-                      const float3 from = p + N * 2e-4f;  // visible (renderer.go:1333-1341)
-                      const float3 sdv = q - from;
-                      const float sd2 = dot3(sdv, sdv);
-                      if (sd2 < 1e-12f) {
-                        L = L + contrib;
-                      } else {
-                        const float dist = sqrtf(sd2);
-                        const float3 dirn = sdv * (1.0f / dist);
-                        shadow = true;
-                        so = make_float4(from.x, from.y, from.z, dist - 1e-4f);
-                        sd = make_float4(dirn.x, dirn.y, dirn.z, __int_as_float(wp.root));
-                        scon = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
-                      }
-                    }
-                  }
-                }
-              }
-              tp = had(tp, f3(M.cr, M.cg, M.cb));
-              nd_dir = rand_cos_hemisphere(N, rng);
-              flags |= 1u;
-              ppdf = fmaxf(0.0f, dot3(N, nd_dir)) / kPi;
-              ps.px[path] = p.x; ps.py[path] = p.y; ps.pz[path] = p.z;
-              no = p + N * 2e-4f;
-            } else if (kind == BC_MAT_METAL) {
-              const float rough = fminf(fmaxf(M.rough, 0.0f), 1.0f);
-              nd_dir = unit3(reflect3(unit3(d), N) + rand_in_unit_sphere(rng) * rough);
-              if (dot3(nd_dir, N) <= 0.0f) {
-                cont = false;
-              } else {
-                flags &= ~1u;
-                tp = had(tp, f3(M.cr, M.cg, M.cb));
-                no = p + N * 2e-4f;
-              }
-            } else {  // glass
-              float eta = M.ior;
-              if (eta <= 1.0f) eta = 1.5f;
-              const float ratio = front ? 1.0f / eta : eta;
-              const float3 un = unit3(d);
-              const float cosT = fminf(dot3(un * -1.0f, N), 1.0f);
-              const float sinT = sqrtf(fmaxf(0.0f, 1.0f - cosT * cosT));
-              if (ratio * sinT > 1.0f || schlick(cosT, ratio) > rng.uniform())
-                nd_dir = reflect3(un, N);
-              else
-                nd_dir = refract3(un, N, ratio);
-              flags &= ~1u;
-              tp = had(tp, f3(M.cr, M.cg, M.cb));
-              no = p + nd_dir * 2e-4f;
-            }
-            if (cont && bounce >= rr_depth) {  // Russian roulette (renderer.go:1550-1560)
-              const float pr = fminf(fmaxf(maxcomp(tp), 0.08f), 0.95f);
-              if (rng.uniform() > pr) cont = false;
-              else tp = tp * (1.0f / pr);
-            }
-            if (cont && bounce + 1 < wp.bounces) {
-              alive = true;
-              ps.ox[path] = no.x; ps.oy[path] = no.y; ps.oz[path] = no.z;
-              ps.dx[path] = nd_dir.x; ps.dy[path] = nd_dir.y; ps.dz[path] = nd_dir.z;
-              ps.tx[path] = tp.x; ps.ty[path] = tp.y; ps.tz[path] = tp.z;
-              ps.flags[path] = flags;
-              ps.ppdf[path] = ppdf;
-              ps.rs[path] = rng.state;
-            }
-          }
-        }
-      }
-      ps.lx[path] = L.x; ps.ly[path] = L.y; ps.lz[path] = L.z;
+      SoAPath s(ps, path);
+      GuideOut gd{guide_nd, guide_c, guide_jit, -1};
+      if (bounce == 0 && wp.want_guides && ps.samp[path] == 0) gd.px = wp.pix_off + ps.pix[path];
+      shade_vertex(wp, n_mats, sc, s, ps.hit_t[path], ps.hit_slot[path], bounce, gd, out);
+      ps.lx[path] = s.L.x; ps.ly[path] = s.L.y; ps.lz[path] = s.L.z;
       if (rec.m) {
         const size_t r = (size_t)bounce * rec.cap + path;
-        rec.m[r] = rec_m;
-        rec.v[r] = make_float4(rec_v.x, rec_v.y, rec_v.z, 0.0f);
+        rec.m[r] = out.rec_m;
+        rec.v[r] = make_float4(out.rec_v.x, out.rec_v.y, out.rec_v.z, 0.0f);
         rec.nb[path] = bounce + 1;
       }
     }
-    const int qn = warp_reserve(&cnt->q[cur ^ 1], alive);
-    if (alive) qnext[qn] = path;
-    const int qs = warp_reserve(&cnt->shadow, shadow);
-    if (shadow) {
-      sh.o[qs] = so;
-      sh.d[qs] = sd;
-      sh.c[qs] = scon;
+    const int qn = warp_reserve(&cnt->q[cur ^ 1], out.alive);
+    if (out.alive) qnext[qn] = path;
+    const int qs = warp_reserve(&cnt->shadow, out.shadow);
+    if (out.shadow) {
+      sh.o[qs] = out.so;
+      sh.d[qs] = out.sd;
+      sh.c[qs] = out.scon;
       sh.path[qs] = path;
     }
   }
@@ -511,6 +599,15 @@ __global__ void __launch_bounds__(128) k_connect(SceneView sv, PathSoA ps, Shado
   }
 }
 
+// clampFirefly (renderer.go:1917-1926)
+__device__ __forceinline__ float3 clamp_sample(float3 c, float limit) {
+  if (limit > 0.0f) {
+    const float mx = maxcomp(c);
+    if (!(mx <= limit || mx <= 0.0f)) c = c * (limit / mx);
+  }
+  return c;
+}
+
 // ---- accumulate --------------------------------------------------------------
 // For every view the wave touches, each pixel adds its samples of the wave in
 // sample order (path = view.path_off + s * npix + p): no atomics, and the sum
@@ -539,11 +636,7 @@ __global__ void k_accumulate(const BatchState* __restrict__ bs, const ViewGPU* _
       float3 acc2 = qp ? f3(qp[0], qp[1], qp[2]) : f3(0, 0, 0);
       for (int s = s_lo; s < s_hi; s++) {
         const long long i = V.path_off + (long long)s * V.npix + p - w0;
-        float3 c = f3(ps.lx[i], ps.ly[i], ps.lz[i]);
-        if (V.clamp > 0.0f) {  // clampFirefly (renderer.go:1917-1926)
-          const float mx = maxcomp(c);
-          if (!(mx <= V.clamp || mx <= 0.0f)) c = c * (V.clamp / mx);
-        }
+        const float3 c = clamp_sample(f3(ps.lx[i], ps.ly[i], ps.lz[i]), V.clamp);
         acc = acc + c;
         acc2 = acc2 + had(c, c);
       }
@@ -635,6 +728,86 @@ __global__ void k_finish_views(const ViewGPU* __restrict__ views, int n_views, c
     const float inv = 1.0f / (float)V.spp;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * V.npix; k += stride)
       out[3 * (size_t)V.pix_off + k] = sum[3 * (size_t)V.pix_off + k] * inv;
+  }
+}
+
+// ---- one-kernel form ----------------------------------------------------------------
+// The reference's OpenCL design (one work-item per pixel looping over samples
+// and bounces, gpu_opencl_windows.go:800-822), on the same primary rays,
+// traversal, shading and accumulation code as the wave engine: the plain
+// one-view-per-launch form the wave engine is measured against. Shadow rays are
+// traced in place; a lane idles once its path ends until the warp's longest
+// path of that sample is done.
+template <int STACK, bool SPH>
+__global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict__ views, int v, int n_mats,
+                                                      ShadeScene sc, const double2* __restrict__ seq,
+                                                      float* __restrict__ sum, float* __restrict__ sumsq,
+                                                      float4* __restrict__ guide_nd, uint32_t* __restrict__ guide_c,
+                                                      uint32_t* __restrict__ guide_jit, WaveCounters* cnt,
+                                                      unsigned* status) {
+  const ViewGPU& V = views[v];
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long segs = 0, shadows = 0;
+  if (p < V.npix) {
+    const int x = p % V.W, y = V.y0 + p / V.W;
+    float* sp = sum + 3 * (size_t)(V.pix_off + p);
+    float* qp = sumsq ? sumsq + 3 * (size_t)(V.pix_off + p) : nullptr;
+    float3 acc = f3(sp[0], sp[1], sp[2]);
+    float3 acc2 = qp ? f3(qp[0], qp[1], qp[2]) : f3(0, 0, 0);
+    Walker<STACK> w;
+    for (int s = 0; s < V.spp; s++) {
+      RegPath st;
+      double jx, jy;
+      primary_ray(V, x, y, s, seq, &st.o, &st.d, &st.rng, &jx, &jy);
+      st.tp = f3(1.0f, 1.0f, 1.0f);
+      st.L = f3(0.0f, 0.0f, 0.0f);
+      st.pv = f3(0.0f, 0.0f, 0.0f);
+      st.flags = 0u;
+      st.ppdf = 0.0f;
+      const bool guide = s == 0 && V.want_guides;
+      if (guide) guide_jit[V.pix_off + p] = jitter_word(jx, jy);
+      for (int b = 0; b < V.bounces; b++) {
+        const Ray32 r = make_ray(st.o.x, st.o.y, st.o.z, st.d.x, st.d.y, st.d.z, 1e-4f);
+        FastClosestLeaf<SPH> leaf(sc.sv, r, 1e30f);
+        w.reset(V.root);
+        while (!w.step(sc.sv, r, leaf, status)) {
+        }
+        segs++;
+        const GuideOut gd{guide_nd, guide_c, guide_jit, (b == 0 && guide) ? V.pix_off + p : -1};
+        VertexOut out;
+        shade_vertex(V, n_mats, sc, st, leaf.best_t, leaf.best_slot, b, gd, out);
+        if (out.shadow) {
+          shadows++;
+          const Ray32 sr = make_ray(out.so.x, out.so.y, out.so.z, out.sd.x, out.sd.y, out.sd.z, 1e-4f);
+          FastAnyLeaf<SPH> any(sc.sv, sr, out.so.w);
+          w.reset(V.root);
+          while (!w.step(sc.sv, sr, any, status)) {
+          }
+          if (!any.done) st.L = st.L + f3(out.scon.x, out.scon.y, out.scon.z);
+        }
+        if (!out.alive) break;
+      }
+      const float3 c = clamp_sample(st.L, V.clamp);
+      acc = acc + c;
+      acc2 = acc2 + had(c, c);
+    }
+    sp[0] = acc.x;
+    sp[1] = acc.y;
+    sp[2] = acc.z;
+    if (qp) {
+      qp[0] = acc2.x;
+      qp[1] = acc2.y;
+      qp[2] = acc2.z;
+    }
+  }
+  // one atomic per warp for the ray counters
+  for (int o = 16; o > 0; o >>= 1) {
+    segs += __shfl_down_sync(0xffffffffu, segs, o);
+    shadows += __shfl_down_sync(0xffffffffu, shadows, o);
+  }
+  if ((threadIdx.x & 31u) == 0) {
+    if (segs) atomicAdd(&cnt->rays, segs);
+    if (shadows) atomicAdd(&cnt->shadow_rays, shadows);
   }
 }
 
@@ -968,6 +1141,25 @@ static bc_status check_view(bc_context* ctx, const ViewRequest& r) {
 
 // Renders the requested views into rb->sum (and guides); `frame_px` pixels of
 // frame buffers are kept. Leaves the per-view table in rb->views.
+// The one-kernel form: one launch per view.
+template <int STACK, bool SPH>
+static bc_status run_plain(bc_context* ctx, const ShadeScene& sc, const std::vector<ViewGPU>& views) {
+  RenderBuffers* rb = ctx->rb;
+  for (int v = 0; v < (int)views.size(); v++) {
+    if (*(volatile int*)ctx->h_cancel || ctx->cancel.load()) {
+      cudaStreamSynchronize(ctx->stream);
+      return set_error(ctx, BC_ERR_CANCELLED, "render cancelled");
+    }
+    const int grid = (views[v].npix + 127) / 128;
+    k_render_plain<STACK, SPH><<<grid, 128, 0, ctx->stream>>>(
+        rb->views, v, ctx->ds.n_mats, sc, rb->seq_xy, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr, rb->guide_nd,
+        rb->guide_c, rb->guide_jit, rb->cnt, ctx->d_status);
+    cudaError_t e = cudaGetLastError();
+    if (e) return cuda_status(ctx, e, "one-kernel render launch");
+  }
+  return BC_OK;
+}
+
 bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, size_t frame_px, int64_t* rays,
                        const GradArgs* grad) {
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
@@ -1092,7 +1284,11 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
   const int64_t n_waves = (total + bsh.cap - 1) / bsh.cap;
   const int stack = stack_variant(ctx->ds.stack_need);
   const bool sph = ctx->ds.has_spheres;
-  if (stack == 64)
+  if (ctx->render_engine == 1 && !grad) {
+    if (stack == 64) bst = sph ? run_plain<64, true>(ctx, sc, views) : run_plain<64, false>(ctx, sc, views);
+    else if (stack == 128) bst = sph ? run_plain<128, true>(ctx, sc, views) : run_plain<128, false>(ctx, sc, views);
+    else bst = sph ? run_plain<256, true>(ctx, sc, views) : run_plain<256, false>(ctx, sc, views);
+  } else if (stack == 64)
     bst = sph ? run_waves<64, true>(ctx, max_bounces, lights, sc, n_waves, grad)
               : run_waves<64, false>(ctx, max_bounces, lights, sc, n_waves, grad);
   else if (stack == 128)

@@ -339,6 +339,20 @@ def run_render(args):
         times.append(dt)
         rays += r
     e2e_t, e2e_r, lin = frame(True)
+    plain = None
+    if args.plain_steps > 0:
+        # the plain form: one kernel per view, a thread per pixel looping over
+        # samples and bounces (the reference's OpenCL kernel shape), same samples
+        ctx.set_option("render_engine", 1)
+        frame(False)
+        pt, pr = [], 0
+        for _ in range(args.plain_steps):
+            dt, r, _ = frame(False)
+            pt.append(dt)
+            pr += r
+        ctx.set_option("render_engine", 0)
+        plain = {"value": pr / sum(pt) / 1e6, "unit": METRIC, "ms_per_step": 1e3 * sum(pt) / len(pt),
+                 "steps": len(pt), "form": "one kernel launch per view, thread per pixel (same samples)"}
     clk = clocks.stop()
     value = rays / sum(times) / 1e6
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -348,6 +362,9 @@ def run_render(args):
             "e2e": {"value": e2e_r / e2e_t / 1e6, "unit": METRIC, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": st.width * st.height * 16},
             "gpu_launches": None, "clocks": clk}
+    if plain:
+        line["plain"] = plain
+        line["wave_over_plain"] = value / plain["value"]
     cpu_img = None
     if not args.no_cpu_baseline:
         import oracle
@@ -442,6 +459,18 @@ def run_batch(args):
         pt.append(dt)
         pr += r
     e2e_t, e2e_r = batched(readback=True)
+    kernel_form = None
+    if args.plain_steps > 0:  # one kernel launch per view (thread per pixel), same samples
+        ctx.set_option("render_engine", 1)
+        batched()
+        kt, kr = [], 0
+        for _ in range(args.plain_steps):
+            dt, r = batched()
+            kt.append(dt)
+            kr += r
+        ctx.set_option("render_engine", 0)
+        kernel_form = {"value": kr / sum(kt) / 1e6, "unit": METRIC, "ms_per_step": 1e3 * sum(kt) / len(kt),
+                       "form": f"{n_views} one-kernel launches (thread per pixel looping samples and bounces)"}
     clk = clocks.stop()
     value = br / sum(bt) / 1e6
     plain_v = pr / sum(pt) / 1e6
@@ -457,6 +486,8 @@ def run_batch(args):
             "plain": {"value": plain_v, "unit": METRIC, "ms_per_step": 1e3 * sum(pt) / args.steps,
                       "form": f"{n_views} sequential one-view bc_render_batch calls"},
             "batched_over_plain": value / plain_v,
+            "plain_one_kernel": kernel_form,
+            "batched_over_one_kernel": (value / kernel_form["value"]) if kernel_form else None,
             "e2e": {"value": e2e_r / e2e_t / 1e6, "unit": METRIC, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": px * 12},
             "gpu_launches": None, "clocks": clk}
@@ -575,6 +606,8 @@ def main():
     ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
     ap.add_argument("--rmse", action="store_true", help="render workloads: RMSE against a converged image")
     ap.add_argument("--views", type=int, default=64, help="batch workload: number of views")
+    ap.add_argument("--plain-steps", type=int, default=2,
+                    help="render workloads: frames timed with the one-kernel form (0 = skip)")
     args = ap.parse_args()
     N_TRIS, N_RAYS = args.tris, args.rays
     if args.warmup < 3 and args.impl == "gb300":

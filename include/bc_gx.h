@@ -330,6 +330,10 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *                        (default 2^22); images do not depend on it.
  *   "render_graph"       1 (default): a render of several waves replays one
  *                        captured CUDA graph per wave; 0: plain stream launches.
+ *   "render_engine"      0 (default): the wave engine; 1: one kernel launch per
+ *                        view, one thread per pixel looping over samples and
+ *                        bounces (the reference OpenCL kernel's shape, kept as the
+ *                        measured baseline; gradient renders always use the wave engine).
  * Unknown names or values return BC_ERR_INVALID_ARG.
  */
 bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value);

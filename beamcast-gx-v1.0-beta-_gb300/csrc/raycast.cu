@@ -206,8 +206,8 @@ __global__ void __launch_bounds__(128) k_closest_fast_persistent(SceneView sv, c
   bool exhausted = false;
   Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
   FastClosestLeaf<false> leaf(sv, r, 0.0f);
-  Walker<STACK> w;
-  w.reset();
+  FastWalker<STACK> w;
+  w.reset(r);
   for (;;) {
     const bool need = idx < 0 && !exhausted;
     const unsigned m = __ballot_sync(0xffffffffu, need);
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(128) k_closest_fast_persistent(SceneView sv, c
           const float4 a = __ldg(rays + 2 * idx), b = __ldg(rays + 2 * idx + 1);
           r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
           leaf.reset(b.w);
-          w.reset();
+          w.reset(r);
         } else {
           exhausted = true;
         }

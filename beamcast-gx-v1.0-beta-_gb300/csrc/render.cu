@@ -167,7 +167,10 @@ __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __r
   const long long w0 = bs->w0;
   const int n = (int)min((long long)bs->cap, bs->total - w0);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) cnt->q[0] = max(n, 0);  // the first bounce's queue holds every path of the wave
+  if (i == 0) {
+    cnt->q[0] = max(n, 0);  // the first bounce's queue holds every path of the wave
+    cnt->work_ext = 0;
+  }
   if (i >= n) return;
   const long long g = w0 + i;
   const int v = view_of(views, bs->n_views, g);
@@ -202,15 +205,19 @@ __global__ void __launch_bounds__(128) k_extend(SceneView sv, const ViewGPU* __r
                                                 const int* __restrict__ queue, WaveCounters* cnt, int cur,
                                                 unsigned* status) {
   const int n = *((volatile int*)&cnt->q[cur]);
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->rays, (unsigned long long)n);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&cnt->rays, (unsigned long long)n);
+    cnt->q[cur ^ 1] = 0;  // the queue and shadow list this bounce's shade fills
+    cnt->shadow = 0;
+  }
   const unsigned lane = threadIdx.x & 31u;
   const unsigned below = (1u << lane) - 1u;
   int path = -1;
   bool exhausted = false;
   Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
   FastClosestLeaf<SPH> leaf(sv, r, 1e30f);
-  Walker<STACK> w;
-  w.reset();
+  FastWalker<STACK> w;
+  w.reset(r);
   for (;;) {
     const bool need = path < 0 && !exhausted;
     const unsigned m = __ballot_sync(0xffffffffu, need);
@@ -225,7 +232,7 @@ __global__ void __launch_bounds__(128) k_extend(SceneView sv, const ViewGPU* __r
           path = queue[my];
           r = make_ray(ps.ox[path], ps.oy[path], ps.oz[path], ps.dx[path], ps.dy[path], ps.dz[path], 1e-4f);
           leaf.reset(1e30f);
-          w.reset(views[ps.view[path]].root);
+          w.reset(r, views[ps.view[path]].root);
         } else {
           exhausted = true;
         }
@@ -511,12 +518,16 @@ __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, cons
   s.L = L;
 }
 
-__global__ void __launch_bounds__(256) k_shade(const ViewGPU* __restrict__ views, int n_mats, ShadeScene sc,
+__global__ void __launch_bounds__(256, 3) k_shade(const ViewGPU* __restrict__ views, int n_mats, ShadeScene sc,
                                                PathSoA ps, const int* __restrict__ qcur, int* __restrict__ qnext,
                                                ShadowSoA sh, WaveCounters* cnt, int cur, int bounce,
                                                float4* __restrict__ guide_nd, uint32_t* __restrict__ guide_c,
                                                const uint32_t* __restrict__ guide_jit, GradRec rec) {
   const int n = *((volatile int*)&cnt->q[cur]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cnt->work_ext = 0;  // the next bounce's extend and this bounce's connect start from zero
+    cnt->work_con = 0;
+  }
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
     const int idx = base + threadIdx.x;
@@ -562,8 +573,8 @@ __global__ void __launch_bounds__(128) k_connect(SceneView sv, PathSoA ps, Shado
   bool exhausted = false;
   Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
   FastAnyLeaf<SPH> leaf(sv, r, 0.0f);
-  Walker<STACK> w;
-  w.reset();
+  FastWalker<STACK> w;
+  w.reset(r);
   for (;;) {
     const bool need = i < 0 && !exhausted;
     const unsigned m = __ballot_sync(0xffffffffu, need);
@@ -579,7 +590,7 @@ __global__ void __launch_bounds__(128) k_connect(SceneView sv, PathSoA ps, Shado
           const float4 o = sh.o[i], d = sh.d[i];
           r = make_ray(o.x, o.y, o.z, d.x, d.y, d.z, 1e-4f);
           leaf.reset(o.w);
-          w.reset((uint32_t)__float_as_int(d.w));  // the scene root rides in d.w
+          w.reset(r, (uint32_t)__float_as_int(d.w));  // the scene root rides in d.w
         } else {
           exhausted = true;
         }
@@ -754,7 +765,7 @@ __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict_
     float* qp = sumsq ? sumsq + 3 * (size_t)(V.pix_off + p) : nullptr;
     float3 acc = f3(sp[0], sp[1], sp[2]);
     float3 acc2 = qp ? f3(qp[0], qp[1], qp[2]) : f3(0, 0, 0);
-    Walker<STACK> w;
+    FastWalker<STACK> w;
     for (int s = 0; s < V.spp; s++) {
       RegPath st;
       double jx, jy;
@@ -769,7 +780,7 @@ __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict_
       for (int b = 0; b < V.bounces; b++) {
         const Ray32 r = make_ray(st.o.x, st.o.y, st.o.z, st.d.x, st.d.y, st.d.z, 1e-4f);
         FastClosestLeaf<SPH> leaf(sc.sv, r, 1e30f);
-        w.reset(V.root);
+        w.reset(r, V.root);
         while (!w.step(sc.sv, r, leaf, status)) {
         }
         segs++;
@@ -780,7 +791,7 @@ __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict_
           shadows++;
           const Ray32 sr = make_ray(out.so.x, out.so.y, out.so.z, out.sd.x, out.sd.y, out.sd.z, 1e-4f);
           FastAnyLeaf<SPH> any(sc.sv, sr, out.so.w);
-          w.reset(V.root);
+          w.reset(sr, V.root);
           while (!w.step(sc.sv, sr, any, status)) {
           }
           if (!any.done) st.L = st.L + f3(out.scon.x, out.scon.y, out.scon.z);
@@ -1049,11 +1060,10 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
   WaveCounters* c = rb->cnt;
   k_generate<<<w.gen_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->q[0], rb->seq_xy, rb->guide_jit, c);
   int cur = 0;
+  // Counter resets ride in the kernels: generate zeroes the first extend's work
+  // counter, extend zeroes the queue and shadow list its shade fills, shade
+  // zeroes the work counters of the next extend and of its connect.
   for (int b = 0; b < w.bounces; b++) {
-    cudaError_t e = cudaMemsetAsync(&c->work_ext, 0, sizeof(int) * 2, st);
-    if (!e) e = cudaMemsetAsync(&c->q[cur ^ 1], 0, sizeof(int), st);
-    if (!e) e = cudaMemsetAsync(&c->shadow, 0, sizeof(int), st);
-    if (e) return e;
     k_extend<STACK, SPH><<<w.ext_grid, 128, 0, st>>>(sc.sv, rb->views, rb->ps, rb->q[cur], c, cur, ctx->d_status);
     const GradRec rec = w.grad ? rb->grec : GradRec{nullptr, nullptr, nullptr, 0};
     k_shade<<<w.shade_grid, 256, 0, st>>>(rb->views, ctx->ds.n_mats, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1], rb->sh,

@@ -65,6 +65,11 @@ __device__ __forceinline__ float slab_near(float lox, float hix, float loy, floa
   return tn <= tf ? tn : __int_as_float(0x7f800000);
 }
 
+// 1 + b 2^-15 for byte j of word (bit pattern 0x3f80bb00, exact).
+__device__ __forceinline__ float byte_v(uint32_t word, int j) {
+  return __uint_as_float(__byte_perm(word, 0x3f800000u, 0x7604u | ((uint32_t)j << 4)));
+}
+
 // Exact float of an unsigned byte: 2^23 + b built in the bit pattern, minus 2^23.
 __device__ __forceinline__ float byte_f(uint32_t word, int j) {
   return __uint_as_float(__byte_perm(word, 0x4b000000u, 0x7540u | (uint32_t)j)) - 8388608.0f;
@@ -389,6 +394,117 @@ struct Walker {
       float nr[8];
       uint32_t ch[8];
       node_children(sv.nodes + ref, r, leaf.tlim, nr, ch);
+      sort8(nr, ch);
+      if (nr[0] == __int_as_float(0x7f800000)) {
+        ref = pop(leaf.tlim);
+      } else {
+#pragma unroll
+        for (int k = 7; k >= 1; k--) {
+          if (nr[k] != __int_as_float(0x7f800000)) {
+            if (sp < STACK) st[sp++] = make_uint2(ch[k], __float_as_uint(nr[k]));
+            else atomicOr(status, kStatusStackOverflow);
+          }
+        }
+        ref = ch[0];
+      }
+      if (ref != kEnd && (ref & kLeafBit)) {
+        if (pending != 0) break;
+        pending = ref;
+        ref = pop(leaf.tlim);
+      }
+      if (__all_sync(__activemask(), pending != 0)) break;
+    }
+    while (pending != 0) {
+      leaf(pending);
+      if (leaf.done) return true;
+      pending = 0;
+      if (ref != kEnd && (ref & kLeafBit)) {
+        pending = ref;
+        ref = pop(leaf.tlim);
+      }
+    }
+    return ref == kEnd;
+  }
+};
+
+// ---- lean walk for the fast (rendering) precision -------------------------------
+// Same while-while structure and stack as Walker, with a cheaper node test:
+//  * decode and slab in one FMA per bound: per node and axis A = (p - o)/d and
+//    B = 2^e/d, then t(q) = q*B + A (q enters as 1 + q 2^-15, one byte
+//    permute, with A and B rescaled to match); the near and far byte of each axis are
+//    chosen once per node from the sign of 1/d, so no per-axis min/max;
+//  * zero direction components use a finite 1/(+-1e-15) instead of infinity
+//    (q*B would be 0*inf);
+// The decode is not outward-rounded, so a box can lose a few ulps of its
+// quantization margin: fine for rendering, not for the exact ray cast.
+template <int STACK>
+struct FastWalker {
+  uint2 st[STACK];
+  int sp;
+  uint32_t ref;
+  uint32_t pending;
+  float ivx, ivy, ivz;  // finite 1/d
+  float nox, noy, noz;  // -o/d
+  __device__ __forceinline__ void reset(const Ray32& r, uint32_t root = 0) {
+    sp = 0;
+    ref = root;
+    pending = 0;
+    ivx = 1.0f / (fabsf(r.dx) < 1e-15f ? copysignf(1e-15f, r.dx) : r.dx);
+    ivy = 1.0f / (fabsf(r.dy) < 1e-15f ? copysignf(1e-15f, r.dy) : r.dy);
+    ivz = 1.0f / (fabsf(r.dz) < 1e-15f ? copysignf(1e-15f, r.dz) : r.dz);
+    nox = -r.ox * ivx;
+    noy = -r.oy * ivy;
+    noz = -r.oz * ivz;
+  }
+  __device__ __forceinline__ uint32_t pop(float tlim) {
+    while (sp > 0) {
+      const uint2 e = st[--sp];
+      if (__uint_as_float(e.y) <= tlim) return e.x;
+    }
+    return kEnd;
+  }
+  // Entry distances of the eight children (+inf: missed or empty slot).
+  __device__ __forceinline__ void children(const Node8* __restrict__ node, float tmin, float tlim, float near[8],
+                                           uint32_t child[8]) const {
+    const float4* p = reinterpret_cast<const float4*>(node);
+    const float4 w0 = __ldg(p + 0);
+    const uint4 c0 = __ldg(reinterpret_cast<const uint4*>(p + 1));
+    const uint4 c1 = __ldg(reinterpret_cast<const uint4*>(p + 2));
+    const uint4 qx = __ldg(reinterpret_cast<const uint4*>(p + 3));
+    const uint4 qy = __ldg(reinterpret_cast<const uint4*>(p + 4));
+    const uint4 qz = __ldg(reinterpret_cast<const uint4*>(p + 5));
+    const uint32_t meta = __float_as_uint(w0.w);
+    // A byte q becomes v = 1 + q 2^-15 with one byte permute (bits 0x3f80qq00);
+    // q*B + A = v*B' + (A - B') with B' = 2^15 B. The subtraction rounds at the
+    // scale of 2^15 steps: ~1e-3 of a grid step.
+    const float bx = __uint_as_float((meta & 0xffu) << 23) * ivx * 32768.0f;
+    const float by = __uint_as_float(((meta >> 8) & 0xffu) << 23) * ivy * 32768.0f;
+    const float bz = __uint_as_float(((meta >> 16) & 0xffu) << 23) * ivz * 32768.0f;
+    const float ax = fmaf(w0.x, ivx, nox) - bx, ay = fmaf(w0.y, ivy, noy) - by, az = fmaf(w0.z, ivz, noz) - bz;
+    // near / far byte words (children 0-3, 4-7) per axis
+    const bool fx = ivx < 0.0f, fy = ivy < 0.0f, fz = ivz < 0.0f;
+    const uint32_t nx0 = fx ? qx.z : qx.x, nx1 = fx ? qx.w : qx.y, gx0 = fx ? qx.x : qx.z, gx1 = fx ? qx.y : qx.w;
+    const uint32_t ny0 = fy ? qy.z : qy.x, ny1 = fy ? qy.w : qy.y, gy0 = fy ? qy.x : qy.z, gy1 = fy ? qy.y : qy.w;
+    const uint32_t nz0 = fz ? qz.z : qz.x, nz1 = fz ? qz.w : qz.y, gz0 = fz ? qz.x : qz.z, gz1 = fz ? qz.y : qz.w;
+    child[0] = c0.x; child[1] = c0.y; child[2] = c0.z; child[3] = c0.w;
+    child[4] = c1.x; child[5] = c1.y; child[6] = c1.z; child[7] = c1.w;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const int j = k & 3;
+      const float tnx = fmaf(byte_v(k < 4 ? nx0 : nx1, j), bx, ax), tfx = fmaf(byte_v(k < 4 ? gx0 : gx1, j), bx, ax);
+      const float tny = fmaf(byte_v(k < 4 ? ny0 : ny1, j), by, ay), tfy = fmaf(byte_v(k < 4 ? gy0 : gy1, j), by, ay);
+      const float tnz = fmaf(byte_v(k < 4 ? nz0 : nz1, j), bz, az), tfz = fmaf(byte_v(k < 4 ? gz0 : gz1, j), bz, az);
+      const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+      const float tf = fminf(fminf(fminf(tfx, tfy), tfz) * (1.0f + kFarSlack), tlim);
+      near[k] = tn <= tf ? tn : __int_as_float(0x7f800000);  // empty slots decode inverted: a miss
+    }
+  }
+  template <class Leaf>
+  __device__ __forceinline__ bool step(const SceneView& sv, const Ray32& r, Leaf& leaf, unsigned* status) {
+    while (ref != kEnd && !(ref & kLeafBit)) {
+      float nr[8];
+      uint32_t ch[8];
+      children(sv.nodes + ref, r.tmin, leaf.tlim, nr, ch);
       sort8(nr, ch);
       if (nr[0] == __int_as_float(0x7f800000)) {
         ref = pop(leaf.tlim);

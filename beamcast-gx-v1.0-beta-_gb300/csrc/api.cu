@@ -378,8 +378,8 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     return BC_OK;
   }
   if (n == "render_wave_cap") {
-    if (value < 4096 || value > (1 << 25))
-      return set_error(ctx, BC_ERR_INVALID_ARG, "render_wave_cap must be in [4096, 2^25]");
+    if (value < 4096 || value > (1 << 27))
+      return set_error(ctx, BC_ERR_INVALID_ARG, "render_wave_cap must be in [4096, 2^27]");
     ctx->render_wave_cap = (long long)value;
     return BC_OK;
   }

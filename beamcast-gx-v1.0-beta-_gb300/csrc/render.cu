@@ -1217,25 +1217,29 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
     max_bounces = std::max(max_bounces, V.bounces);
     lights = lights || sr.n_lights > 0;
   }
-  const int cap = (int)std::max<long long>(1, std::min<long long>(total, ctx->render_wave_cap));
+  long long cap_limit = ctx->render_wave_cap;
+  if (grad)  // path replay records cost 20 bytes per path and bounce: keep them under 8 GB
+    cap_limit = std::min<long long>(cap_limit, std::max<long long>(4096, (8LL << 30) / (20LL * max_bounces)));
+  const int cap = (int)std::max<long long>(1, std::min<long long>(total, cap_limit));
   if ((bst = ensure_paths(ctx, cap))) return bst;
   if ((bst = ensure_frame(ctx, frame_px))) return bst;
   if (grad) {  // path replay records: one per path and bounce
     if (max_bounces > kMaxGradBounces) return set_error(ctx, BC_ERR_INVALID_ARG, "gradient renders allow 64 bounces");
-    if (rb->rec_bounces < max_bounces || rb->rec_cap < rb->cap) {
+    // stride: this render's wave size (path slots >= cap are never used by it)
+    if (rb->rec_bounces < max_bounces || rb->rec_cap < cap) {
       const size_t per = sizeof(int32_t) + sizeof(float4);
-      cudaError_t e = rb->rec.ensure((size_t)max_bounces * rb->cap * per + rb->cap * sizeof(int32_t) + 4 * 256);
+      cudaError_t e = rb->rec.ensure((size_t)max_bounces * cap * per + (size_t)cap * sizeof(int32_t) + 4 * 256);
       if (e) {
         rb->rec_bounces = rb->rec_cap = 0;
         return cuda_status(ctx, e, "path replay records");
       }
       char* p = (char*)rb->rec.p;
-      rb->grec.v = carve<float4>(p, (size_t)max_bounces * rb->cap);
-      rb->grec.m = carve<int32_t>(p, (size_t)max_bounces * rb->cap);
-      rb->grec.nb = carve<int32_t>(p, rb->cap);
-      rb->grec.cap = rb->cap;
+      rb->grec.v = carve<float4>(p, (size_t)max_bounces * cap);
+      rb->grec.m = carve<int32_t>(p, (size_t)max_bounces * cap);
+      rb->grec.nb = carve<int32_t>(p, cap);
+      rb->grec.cap = cap;
       rb->rec_bounces = max_bounces;
-      rb->rec_cap = rb->cap;
+      rb->rec_cap = cap;
     }
   }
   BatchState bsh;

@@ -314,6 +314,8 @@ def run_render(args):
         st.spp = args.spp
     scene = scenes.to_scene(spec)
     ctx = bcgx.Context(0)
+    if args.wave_cap:
+        ctx.set_option("render_wave_cap", args.wave_cap)
     ctx.upload(scene)
     L = bcgx.lib()
     import ctypes as C
@@ -427,6 +429,8 @@ def run_batch(args):
     built = [scenes.to_scene(s) for s in specs]
     build_s = time.perf_counter() - t0
     ctx = bcgx.Context(0)
+    if args.wave_cap:
+        ctx.set_option("render_wave_cap", args.wave_cap)
     ctx.upload_set(built)
     px = sum(st.width * st.height for _, _, st in views)
     paths = sum(st.width * st.height * st.spp for _, _, st in views)
@@ -606,6 +610,7 @@ def main():
     ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
     ap.add_argument("--rmse", action="store_true", help="render workloads: RMSE against a converged image")
     ap.add_argument("--views", type=int, default=64, help="batch workload: number of views")
+    ap.add_argument("--wave-cap", type=int, default=0, help="render workloads: paths per wave (0 = library default)")
     ap.add_argument("--plain-steps", type=int, default=2,
                     help="render workloads: frames timed with the one-kernel form (0 = skip)")
     args = ap.parse_args()

@@ -326,8 +326,11 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *   "raycast_exact"      1 (default): bc_raycast is exact as documented there;
  *                        0: plain fp32 closest hit, t = the fp32 distance, with no
  *                        exactness contract near edges and ties.
- *   "render_wave_cap"    paths in flight per wave of the renderer, 4096 .. 2^25
- *                        (default 2^22); images do not depend on it.
+ *   "render_wave_cap"    paths in flight per wave of the renderer, 4096 .. 2^27
+ *                        (default 2^25: ~160 bytes of device memory per path,
+ *                        allocated up to what a render needs); images do not
+ *                        depend on it. Each wave ends in a latency-bound tail of
+ *                        long paths, so larger waves render faster.
  *   "render_graph"       1 (default): a render of several waves replays one
  *                        captured CUDA graph per wave; 0: plain stream launches.
  *   "render_engine"      0 (default): the wave engine; 1: one kernel launch per

@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(128, MINB) k_closest_exact_persistent(SceneVie
   Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
   ExactClosestLeaf<false> leaf(sv, r, 0.0f, status);
   Walker<STACK> w;
-  w.reset();
+  w.reset(r);
   int parked = 0;  // warp-uniform
   for (;;) {
     const bool need = idx < 0 && !exhausted;
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(128, MINB) k_closest_exact_persistent(SceneVie
           const float4 a = __ldg(rays + 2 * idx), b = __ldg(rays + 2 * idx + 1);
           r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
           leaf.reset(b.w);
-          w.reset();
+          w.reset(r);
         } else {
           exhausted = true;
         }

@@ -53,58 +53,9 @@ __device__ __forceinline__ Ray32 make_ray(float ox, float oy, float oz, float dx
 // ignores, and the box would be entered.
 __device__ __forceinline__ float widen(float t) { return t * (t >= 0.0f ? 1.0f + kFarSlack : 1.0f - kFarSlack); }
 
-// Slab test of one child box; returns the entry distance or +inf on a miss.
-__device__ __forceinline__ float slab_near(float lox, float hix, float loy, float hiy, float loz, float hiz,
-                                           const Ray32& r, float tlim) {
-  float t0x = (lox - r.ox) * r.ix, t1x = (hix - r.ox) * r.ix;
-  float t0y = (loy - r.oy) * r.iy, t1y = (hiy - r.oy) * r.iy;
-  float t0z = (loz - r.oz) * r.iz, t1z = (hiz - r.oz) * r.iz;
-  float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), r.tmin));
-  float sf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-  float tf = fminf(widen(sf), tlim);
-  return tn <= tf ? tn : __int_as_float(0x7f800000);
-}
-
 // 1 + b 2^-15 for byte j of word (bit pattern 0x3f80bb00, exact).
 __device__ __forceinline__ float byte_v(uint32_t word, int j) {
   return __uint_as_float(__byte_perm(word, 0x3f800000u, 0x7604u | ((uint32_t)j << 4)));
-}
-
-// Exact float of an unsigned byte: 2^23 + b built in the bit pattern, minus 2^23.
-__device__ __forceinline__ float byte_f(uint32_t word, int j) {
-  return __uint_as_float(__byte_perm(word, 0x4b000000u, 0x7540u | (uint32_t)j)) - 8388608.0f;
-}
-
-// Test all children of a node; near[k] = entry distance or +inf. Child boxes
-// are decoded conservatively (round-down lower, round-up upper bounds).
-__device__ __forceinline__ void node_children(const Node8* __restrict__ node, const Ray32& r, float tlim,
-                                              float near[8], uint32_t child[8]) {
-  const float4* p = reinterpret_cast<const float4*>(node);
-  const float4 w0 = __ldg(p + 0);
-  const uint4 c0 = __ldg(reinterpret_cast<const uint4*>(p + 1));
-  const uint4 c1 = __ldg(reinterpret_cast<const uint4*>(p + 2));
-  const uint4 qx = __ldg(reinterpret_cast<const uint4*>(p + 3));
-  const uint4 qy = __ldg(reinterpret_cast<const uint4*>(p + 4));
-  const uint4 qz = __ldg(reinterpret_cast<const uint4*>(p + 5));
-  const uint32_t meta = __float_as_uint(w0.w);
-  const float sx = __uint_as_float((meta & 0xffu) << 23);
-  const float sy = __uint_as_float(((meta >> 8) & 0xffu) << 23);
-  const float sz = __uint_as_float(((meta >> 16) & 0xffu) << 23);
-  const int nchild = (int)(meta >> 24);
-  child[0] = c0.x; child[1] = c0.y; child[2] = c0.z; child[3] = c0.w;
-  child[4] = c1.x; child[5] = c1.y; child[6] = c1.z; child[7] = c1.w;
-#pragma unroll
-  for (int k = 0; k < 8; k++) {
-    const int j = k & 3;
-    const uint32_t wlx = k < 4 ? qx.x : qx.y, whx = k < 4 ? qx.z : qx.w;
-    const uint32_t wly = k < 4 ? qy.x : qy.y, why = k < 4 ? qy.z : qy.w;
-    const uint32_t wlz = k < 4 ? qz.x : qz.y, whz = k < 4 ? qz.z : qz.w;
-    const float lox = __fmaf_rd(byte_f(wlx, j), sx, w0.x), hix = __fmaf_ru(byte_f(whx, j), sx, w0.x);
-    const float loy = __fmaf_rd(byte_f(wly, j), sy, w0.y), hiy = __fmaf_ru(byte_f(why, j), sy, w0.y);
-    const float loz = __fmaf_rd(byte_f(wlz, j), sz, w0.z), hiz = __fmaf_ru(byte_f(whz, j), sz, w0.z);
-    const float t = slab_near(lox, hix, loy, hiy, loz, hiz, r, tlim);
-    near[k] = k < nchild ? t : __int_as_float(0x7f800000);
-  }
 }
 
 // Sorting network (Batcher odd-even merge, 19 comparators) on (near, child).
@@ -223,14 +174,34 @@ __device__ __forceinline__ TriClass tri_classify(float4 A, float4 E1, float4 E2,
     return c;
   }
   const float R = A.w + fmaxf(fabsf(sx), fmaxf(fabsf(sy), fabsf(sz)));
+  // Quick certain misses before any division, on the numerators u*det, v*det
+  // and t*det: with sd = sign(det) (certain, |det| > 2 errDet), un = s.h
+  // within Eun of its exact value, vn = d.q within Evn, tn = E2.q within Etn
+  // (the numerator terms of eu, ev, et below), u < 0 is certain when
+  // sd un + Eun < 0 and u > 1 when sd un - Eun > |det| + errDet, and so on.
+  // Directed rounding keeps each comparison sound.
+  const float sd = det > 0.0f ? 1.0f : -1.0f;
+  const float un = sd * (sx * hx + sy * hy + sz * hz);
+  const float Eun = 96.0f * kU * R * Mh;
+  const float dhi = __fadd_ru(adet, errDet), dlo = __fsub_rd(adet, errDet);
+  if (__fadd_ru(un, Eun) < 0.0f || __fsub_rd(un, Eun) > dhi) return c;
+  const float qx = sy * E1.z - sz * E1.y;
+  const float qy = sz * E1.x - sx * E1.z;
+  const float qz = sx * E1.y - sy * E1.x;
+  const float vn = sd * (r.dx * qx + r.dy * qy + r.dz * qz);
+  const float Evn = 96.0f * kU * r.dmax * R * E1.w;
+  if (__fadd_ru(vn, Evn) < 0.0f || __fsub_rd(__fsub_rd(__fadd_rd(un, vn), Eun), Evn) > dhi) return c;
+  const float tn = sd * (E2.x * qx + E2.y * qy + E2.z * qz);
+  const float Etn = 112.0f * kU * E2.w * R * E1.w;
+  // bounds of tmin |det| and tlim |det| over |det| in [dlo, dhi] (either may be negative)
+  const float tmin_det = fminf(__fmul_rd(r.tmin, dlo), __fmul_rd(r.tmin, dhi));
+  const float tlim_det = fmaxf(__fmul_ru(tlim, dlo), __fmul_ru(tlim, dhi));
+  if (__fadd_ru(tn, Etn) < tmin_det || __fsub_rd(tn, Etn) > tlim_det) return c;
   const float invd = 1.0f / (adet - errDet);
   const float f = 1.0f / det;
   const float u = f * (sx * hx + sy * hy + sz * hz);
   const float eu = (96.0f * kU * R * Mh + fabsf(u) * errDet) * invd + 4.0f * kU * fabsf(u);
   if (u < -eu || u > 1.0f + eu) return c;
-  const float qx = sy * E1.z - sz * E1.y;
-  const float qy = sz * E1.x - sx * E1.z;
-  const float qz = sx * E1.y - sy * E1.x;
   const float v = f * (r.dx * qx + r.dy * qy + r.dz * qz);
   const float ev = (96.0f * kU * r.dmax * R * E1.w + fabsf(v) * errDet) * invd + 4.0f * kU * fabsf(v);
   const float euv = eu + ev + 4.0f * kU * fabsf(u + v);
@@ -246,23 +217,27 @@ __device__ __forceinline__ TriClass tri_classify(float4 A, float4 E1, float4 E2,
   return c;
 }
 
-// Plain fp32 triangle test for rendering (reference thresholds).
+// Plain fp32 triangle test for rendering (reference thresholds), with the
+// barycentric and distance tests on the numerators (u det, v det, t det
+// against det), so a missed triangle costs no division.
 __device__ __forceinline__ bool tri_hit32(float4 A, float4 E1, float4 E2, const Ray32& r, float tmax, float* t_out) {
   const float hx = r.dy * E2.z - r.dz * E2.y;
   const float hy = r.dz * E2.x - r.dx * E2.z;
   const float hz = r.dx * E2.y - r.dy * E2.x;
   const float det = E1.x * hx + E1.y * hy + E1.z * hz;
   if (fabsf(det) < 1e-10f) return false;
-  const float f = 1.0f / det;
+  const float sd = det > 0.0f ? 1.0f : -1.0f, adet = fabsf(det);
   const float sx = r.ox - A.x, sy = r.oy - A.y, sz = r.oz - A.z;
-  const float u = f * (sx * hx + sy * hy + sz * hz);
-  if (u < 0.0f || u > 1.0f) return false;
+  const float un = sd * (sx * hx + sy * hy + sz * hz);
+  if (un < 0.0f || un > adet) return false;
   const float qx = sy * E1.z - sz * E1.y;
   const float qy = sz * E1.x - sx * E1.z;
   const float qz = sx * E1.y - sy * E1.x;
-  const float v = f * (r.dx * qx + r.dy * qy + r.dz * qz);
-  if (v < 0.0f || u + v > 1.0f) return false;
-  const float t = f * (E2.x * qx + E2.y * qy + E2.z * qz);
+  const float vn = sd * (r.dx * qx + r.dy * qy + r.dz * qz);
+  if (vn < 0.0f || un + vn > adet) return false;
+  const float tn = sd * (E2.x * qx + E2.y * qy + E2.z * qz);
+  if (tn < r.tmin * adet || tn > tmax * adet) return false;
+  const float t = (E2.x * qx + E2.y * qy + E2.z * qz) / det;
   if (t < r.tmin || t > tmax) return false;
   *t_out = t;
   return true;
@@ -304,6 +279,87 @@ struct HitResult {
 
 constexpr uint32_t kEnd = 0x7fffffffu;  // "no node": bit 31 clear and above any node index
 
+// Per-ray constants of the fused node test.
+struct RayPre {
+  float ivx, ivy, ivz;  // finite 1/d (components below 1e-15 in magnitude replaced by +-1e-15)
+  float nox, noy, noz;  // -o/d
+  float mx, my, mz;     // 2|o/d| (rounding-bound term of the conservative test)
+};
+
+__device__ __forceinline__ RayPre ray_pre(const Ray32& r) {
+  RayPre p;
+  p.ivx = 1.0f / (fabsf(r.dx) < 1e-15f ? copysignf(1e-15f, r.dx) : r.dx);
+  p.ivy = 1.0f / (fabsf(r.dy) < 1e-15f ? copysignf(1e-15f, r.dy) : r.dy);
+  p.ivz = 1.0f / (fabsf(r.dz) < 1e-15f ? copysignf(1e-15f, r.dz) : r.dz);
+  p.nox = -r.ox * p.ivx;
+  p.noy = -r.oy * p.ivy;
+  p.noz = -r.oz * p.ivz;
+  p.mx = 2.0f * fabsf(p.nox);
+  p.my = 2.0f * fabsf(p.noy);
+  p.mz = 2.0f * fabsf(p.noz);
+  return p;
+}
+
+// Entry distances of a node's eight children (+inf: missed or empty), decode
+// and slab fused: per axis A = (p - o)/d and B = 2^e/d, a byte q enters as
+// v = 1 + q 2^-15 (one byte permute) and t(q) = v B' + (A - B') with
+// B' = 2^15 B; near and far bytes are picked by the sign of 1/d.
+// CONS: the walk of the exact ray cast must enter every box the fp64 slab
+// test of the reference enters. B' is exact (power-of-two scaling); A, A - B'
+// and the final FMA add at most 4.2u (|p/d| + |o/d|) + 3.1u |B'| of absolute
+// error, so near offsets are lowered and far offsets raised by
+// E = 5u (|fl(p/d - o/d)| + 2|o/d| + |B'|) + 1e-30 per node and axis; the
+// rounding of 1/d itself is relative and covered by the far-distance slack
+// (widen). A zero direction component (|d| < 1e-15, the reference's
+// origin-inside test) gets a finite 1/(+-1e-15): its E is then so large that
+// the axis never rejects, which keeps the test conservative. Empty slots are
+// masked by the child count. Without CONS there is no margin: fine for
+// rendering.
+template <bool CONS>
+__device__ __forceinline__ void node_children_fused(const Node8* __restrict__ node, const RayPre& rp, float tmin,
+                                                    float tlim, float near[8], uint32_t child[8]) {
+  const float4* p = reinterpret_cast<const float4*>(node);
+  const float4 w0 = __ldg(p + 0);
+  const uint4 c0 = __ldg(reinterpret_cast<const uint4*>(p + 1));
+  const uint4 c1 = __ldg(reinterpret_cast<const uint4*>(p + 2));
+  const uint4 qx = __ldg(reinterpret_cast<const uint4*>(p + 3));
+  const uint4 qy = __ldg(reinterpret_cast<const uint4*>(p + 4));
+  const uint4 qz = __ldg(reinterpret_cast<const uint4*>(p + 5));
+  const uint32_t meta = __float_as_uint(w0.w);
+  const int nchild = (int)(meta >> 24);
+  const float bx = __uint_as_float((meta & 0xffu) << 23) * rp.ivx * 32768.0f;
+  const float by = __uint_as_float(((meta >> 8) & 0xffu) << 23) * rp.ivy * 32768.0f;
+  const float bz = __uint_as_float(((meta >> 16) & 0xffu) << 23) * rp.ivz * 32768.0f;
+  const float a1x = fmaf(w0.x, rp.ivx, rp.nox), a1y = fmaf(w0.y, rp.ivy, rp.noy), a1z = fmaf(w0.z, rp.ivz, rp.noz);
+  float anx = a1x - bx, any = a1y - by, anz = a1z - bz;
+  float afx = anx, afy = any, afz = anz;
+  if (CONS) {
+    const float ex = fmaf(fabsf(a1x) + fabsf(bx) + rp.mx, 5.0f * kU, 1e-30f);
+    const float ey = fmaf(fabsf(a1y) + fabsf(by) + rp.my, 5.0f * kU, 1e-30f);
+    const float ez = fmaf(fabsf(a1z) + fabsf(bz) + rp.mz, 5.0f * kU, 1e-30f);
+    anx -= ex; any -= ey; anz -= ez;
+    afx += ex; afy += ey; afz += ez;
+  }
+  const bool fx = rp.ivx < 0.0f, fy = rp.ivy < 0.0f, fz = rp.ivz < 0.0f;
+  const uint32_t nx0 = fx ? qx.z : qx.x, nx1 = fx ? qx.w : qx.y, gx0 = fx ? qx.x : qx.z, gx1 = fx ? qx.y : qx.w;
+  const uint32_t ny0 = fy ? qy.z : qy.x, ny1 = fy ? qy.w : qy.y, gy0 = fy ? qy.x : qy.z, gy1 = fy ? qy.y : qy.w;
+  const uint32_t nz0 = fz ? qz.z : qz.x, nz1 = fz ? qz.w : qz.y, gz0 = fz ? qz.x : qz.z, gz1 = fz ? qz.y : qz.w;
+  child[0] = c0.x; child[1] = c0.y; child[2] = c0.z; child[3] = c0.w;
+  child[4] = c1.x; child[5] = c1.y; child[6] = c1.z; child[7] = c1.w;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int j = k & 3;
+    const float tnx = fmaf(byte_v(k < 4 ? nx0 : nx1, j), bx, anx), tfx = fmaf(byte_v(k < 4 ? gx0 : gx1, j), bx, afx);
+    const float tny = fmaf(byte_v(k < 4 ? ny0 : ny1, j), by, any), tfy = fmaf(byte_v(k < 4 ? gy0 : gy1, j), by, afy);
+    const float tnz = fmaf(byte_v(k < 4 ? nz0 : nz1, j), bz, anz), tfz = fmaf(byte_v(k < 4 ? gz0 : gz1, j), bz, afz);
+    const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+    const float sf = fminf(fminf(tfx, tfy), tfz);
+    const float tf = fminf(CONS ? widen(sf) : sf * (1.0f + kFarSlack), tlim);
+    const bool hit = CONS ? (k < nchild && tn <= tf) : tn <= tf;  // without CONS empty slots decode inverted
+    near[k] = hit ? tn : __int_as_float(0x7f800000);
+  }
+}
+
 // While-while BVH8 walk (Aila and Laine, "Understanding the Efficiency of Ray
 // Traversal on GPUs", HPG 2009): a lane descends inner nodes, postponing the
 // first leaf it reaches, until every active lane of the warp holds a leaf;
@@ -316,11 +372,12 @@ __device__ __forceinline__ void walk(const SceneView& sv, const Ray32& r, Leaf& 
   int sp = 0;
   uint32_t ref = 0;      // root Node8
   uint32_t pending = 0;  // postponed leaf ref, 0 = none
+  const RayPre rp = ray_pre(r);
   for (;;) {
     while (ref != kEnd && !(ref & kLeafBit)) {
       float nr[8];
       uint32_t ch[8];
-      node_children(sv.nodes + ref, r, leaf.tlim, nr, ch);
+      node_children_fused<true>(sv.nodes + ref, rp, r.tmin, leaf.tlim, nr, ch);
       sort8(nr, ch);
       if (nr[0] == __int_as_float(0x7f800000)) {
         ref = kEnd;
@@ -376,10 +433,12 @@ struct Walker {
   int sp;
   uint32_t ref;
   uint32_t pending;
-  __device__ __forceinline__ void reset(uint32_t root = 0) {  // root: Node8 index of the scene's root
+  RayPre rp;
+  __device__ __forceinline__ void reset(const Ray32& r, uint32_t root = 0) {  // root: Node8 index of the scene's root
     sp = 0;
     ref = root;
     pending = 0;
+    rp = ray_pre(r);
   }
   __device__ __forceinline__ uint32_t pop(float tlim) {
     while (sp > 0) {
@@ -393,7 +452,7 @@ struct Walker {
     while (ref != kEnd && !(ref & kLeafBit)) {
       float nr[8];
       uint32_t ch[8];
-      node_children(sv.nodes + ref, r, leaf.tlim, nr, ch);
+      node_children_fused<true>(sv.nodes + ref, rp, r.tmin, leaf.tlim, nr, ch);
       sort8(nr, ch);
       if (nr[0] == __int_as_float(0x7f800000)) {
         ref = pop(leaf.tlim);
@@ -427,34 +486,22 @@ struct Walker {
   }
 };
 
-// ---- lean walk for the fast (rendering) precision -------------------------------
-// Same while-while structure and stack as Walker, with a cheaper node test:
-//  * decode and slab in one FMA per bound: per node and axis A = (p - o)/d and
-//    B = 2^e/d, then t(q) = q*B + A (q enters as 1 + q 2^-15, one byte
-//    permute, with A and B rescaled to match); the near and far byte of each axis are
-//    chosen once per node from the sign of 1/d, so no per-axis min/max;
-//  * zero direction components use a finite 1/(+-1e-15) instead of infinity
-//    (q*B would be 0*inf);
-// The decode is not outward-rounded, so a box can lose a few ulps of its
-// quantization margin: fine for rendering, not for the exact ray cast.
+// ---- walk for the fast (rendering) precision -----------------------------------
+// Walker with the fused node test without rounding margins (see
+// node_children_fused): a box can lose a few ulps of its quantization margin,
+// fine for rendering, not for the exact ray cast.
 template <int STACK>
 struct FastWalker {
   uint2 st[STACK];
   int sp;
   uint32_t ref;
   uint32_t pending;
-  float ivx, ivy, ivz;  // finite 1/d
-  float nox, noy, noz;  // -o/d
+  RayPre rp;
   __device__ __forceinline__ void reset(const Ray32& r, uint32_t root = 0) {
     sp = 0;
     ref = root;
     pending = 0;
-    ivx = 1.0f / (fabsf(r.dx) < 1e-15f ? copysignf(1e-15f, r.dx) : r.dx);
-    ivy = 1.0f / (fabsf(r.dy) < 1e-15f ? copysignf(1e-15f, r.dy) : r.dy);
-    ivz = 1.0f / (fabsf(r.dz) < 1e-15f ? copysignf(1e-15f, r.dz) : r.dz);
-    nox = -r.ox * ivx;
-    noy = -r.oy * ivy;
-    noz = -r.oz * ivz;
+    rp = ray_pre(r);
   }
   __device__ __forceinline__ uint32_t pop(float tlim) {
     while (sp > 0) {
@@ -463,48 +510,12 @@ struct FastWalker {
     }
     return kEnd;
   }
-  // Entry distances of the eight children (+inf: missed or empty slot).
-  __device__ __forceinline__ void children(const Node8* __restrict__ node, float tmin, float tlim, float near[8],
-                                           uint32_t child[8]) const {
-    const float4* p = reinterpret_cast<const float4*>(node);
-    const float4 w0 = __ldg(p + 0);
-    const uint4 c0 = __ldg(reinterpret_cast<const uint4*>(p + 1));
-    const uint4 c1 = __ldg(reinterpret_cast<const uint4*>(p + 2));
-    const uint4 qx = __ldg(reinterpret_cast<const uint4*>(p + 3));
-    const uint4 qy = __ldg(reinterpret_cast<const uint4*>(p + 4));
-    const uint4 qz = __ldg(reinterpret_cast<const uint4*>(p + 5));
-    const uint32_t meta = __float_as_uint(w0.w);
-    // A byte q becomes v = 1 + q 2^-15 with one byte permute (bits 0x3f80qq00);
-    // q*B + A = v*B' + (A - B') with B' = 2^15 B. The subtraction rounds at the
-    // scale of 2^15 steps: ~1e-3 of a grid step.
-    const float bx = __uint_as_float((meta & 0xffu) << 23) * ivx * 32768.0f;
-    const float by = __uint_as_float(((meta >> 8) & 0xffu) << 23) * ivy * 32768.0f;
-    const float bz = __uint_as_float(((meta >> 16) & 0xffu) << 23) * ivz * 32768.0f;
-    const float ax = fmaf(w0.x, ivx, nox) - bx, ay = fmaf(w0.y, ivy, noy) - by, az = fmaf(w0.z, ivz, noz) - bz;
-    // near / far byte words (children 0-3, 4-7) per axis
-    const bool fx = ivx < 0.0f, fy = ivy < 0.0f, fz = ivz < 0.0f;
-    const uint32_t nx0 = fx ? qx.z : qx.x, nx1 = fx ? qx.w : qx.y, gx0 = fx ? qx.x : qx.z, gx1 = fx ? qx.y : qx.w;
-    const uint32_t ny0 = fy ? qy.z : qy.x, ny1 = fy ? qy.w : qy.y, gy0 = fy ? qy.x : qy.z, gy1 = fy ? qy.y : qy.w;
-    const uint32_t nz0 = fz ? qz.z : qz.x, nz1 = fz ? qz.w : qz.y, gz0 = fz ? qz.x : qz.z, gz1 = fz ? qz.y : qz.w;
-    child[0] = c0.x; child[1] = c0.y; child[2] = c0.z; child[3] = c0.w;
-    child[4] = c1.x; child[5] = c1.y; child[6] = c1.z; child[7] = c1.w;
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-      const int j = k & 3;
-      const float tnx = fmaf(byte_v(k < 4 ? nx0 : nx1, j), bx, ax), tfx = fmaf(byte_v(k < 4 ? gx0 : gx1, j), bx, ax);
-      const float tny = fmaf(byte_v(k < 4 ? ny0 : ny1, j), by, ay), tfy = fmaf(byte_v(k < 4 ? gy0 : gy1, j), by, ay);
-      const float tnz = fmaf(byte_v(k < 4 ? nz0 : nz1, j), bz, az), tfz = fmaf(byte_v(k < 4 ? gz0 : gz1, j), bz, az);
-      const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-      const float tf = fminf(fminf(fminf(tfx, tfy), tfz) * (1.0f + kFarSlack), tlim);
-      near[k] = tn <= tf ? tn : __int_as_float(0x7f800000);  // empty slots decode inverted: a miss
-    }
-  }
   template <class Leaf>
   __device__ __forceinline__ bool step(const SceneView& sv, const Ray32& r, Leaf& leaf, unsigned* status) {
     while (ref != kEnd && !(ref & kLeafBit)) {
       float nr[8];
       uint32_t ch[8];
-      children(sv.nodes + ref, r.tmin, leaf.tlim, nr, ch);
+      node_children_fused<false>(sv.nodes + ref, rp, r.tmin, leaf.tlim, nr, ch);
       sort8(nr, ch);
       if (nr[0] == __int_as_float(0x7f800000)) {
         ref = pop(leaf.tlim);

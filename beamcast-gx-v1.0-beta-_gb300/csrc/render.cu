@@ -91,9 +91,38 @@ struct ViewGPU {
   int n_lights, light_off, root;
   int want_guides;
   float clamp;
+  int adaptive;       // adaptivePixel's early stop (renderer.go:1961-1968)
+  float adapt_thr;    // max(1e-8, AdaptiveThreshold)
+  int min_samples;    // min(8, spp)
   int pad;
   unsigned long long seed;
 };
+
+// Per-pixel state of the adaptive stop: samples accumulated, luminance sums.
+struct AdaptState {
+  int32_t* n;       // samples accumulated; bit 31: the pixel has stopped
+  float2* lum;      // (sum of luminance, sum of squared luminance)
+};
+constexpr int32_t kPixDone = int32_t(0x80000000u);
+
+// luminance (renderer.go:2142)
+__device__ __forceinline__ float luminance3(float3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+// One sample of an adaptive pixel: updates the luminance sums and the count;
+// true when the pixel stops after this sample (renderer.go:1957-1968).
+__device__ __forceinline__ bool adaptive_step(const ViewGPU& V, float3 c, int* n, float* sl, float* ssl) {
+  const float l = luminance3(c);
+  *sl += l;
+  *ssl += l * l;
+  *n += 1;
+  if (*n >= V.min_samples && (*n & 1) == 0) {
+    const float nn = (float)*n;
+    const float mean = *sl / nn;
+    const float var = fmaxf(0.0f, *ssl / nn - mean * mean);
+    return var < V.adapt_thr;
+  }
+  return false;
+}
 
 // Device-side wave cursor of a batch.
 struct BatchState {
@@ -161,22 +190,28 @@ __device__ __forceinline__ uint32_t jitter_word(double jx, double jy) {
 }
 
 // seq: the views' sample tables, (x, y) pairs
+// The wave's paths of pixels that have not stopped (adaptive sampling) enter
+// the first queue (warp-aggregated append; cnt->q[0] is zero on entry).
 __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __restrict__ views, PathSoA ps,
                            int* __restrict__ queue, const double2* __restrict__ seq,
-                           uint32_t* __restrict__ guide_jit, WaveCounters* cnt) {
+                           uint32_t* __restrict__ guide_jit, WaveCounters* cnt, AdaptState ad) {
   const long long w0 = bs->w0;
   const int n = (int)min((long long)bs->cap, bs->total - w0);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) {
-    cnt->q[0] = max(n, 0);  // the first bounce's queue holds every path of the wave
-    cnt->work_ext = 0;
+  if (i == 0) cnt->work_ext = 0;
+  int v = 0, s = 0, p = 0;
+  bool live = i < n;
+  if (live) {
+    const long long g = w0 + i;
+    v = view_of(views, bs->n_views, g);
+    const long long local = g - views[v].path_off;
+    s = (int)(local / views[v].npix);
+    p = (int)(local - (long long)s * views[v].npix);
+    if (views[v].adaptive && (ad.n[views[v].pix_off + p] & kPixDone)) live = false;
   }
-  if (i >= n) return;
-  const long long g = w0 + i;
-  const int v = view_of(views, bs->n_views, g);
+  const int slot = warp_reserve(&cnt->q[0], live);
+  if (!live) return;
   const ViewGPU& V = views[v];
-  const long long local = g - V.path_off;
-  const int s = (int)(local / V.npix), p = (int)(local - (long long)s * V.npix);
   const int x = p % V.W, y = V.y0 + p / V.W;
   float3 o, d;
   Pcg32 rng;
@@ -193,7 +228,7 @@ __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __r
   ps.view[i] = v;
   ps.pix[i] = p;
   ps.samp[i] = s;
-  queue[i] = i;
+  queue[slot] = i;
   if (s == 0 && V.want_guides) guide_jit[V.pix_off + p] = jitter_word(jx, jy);
 }
 
@@ -624,7 +659,7 @@ __device__ __forceinline__ float3 clamp_sample(float3 c, float limit) {
 // sample order (path = view.path_off + s * npix + p): no atomics, and the sum
 // does not depend on thread scheduling.
 __global__ void k_accumulate(const BatchState* __restrict__ bs, const ViewGPU* __restrict__ views, PathSoA ps,
-                             float* __restrict__ sum, float* __restrict__ sumsq) {
+                             float* __restrict__ sum, float* __restrict__ sumsq, AdaptState ad) {
   const long long w0 = bs->w0;
   const long long w1 = min(bs->total, w0 + (long long)bs->cap);
   if (w1 <= w0) return;
@@ -643,13 +678,28 @@ __global__ void k_accumulate(const BatchState* __restrict__ bs, const ViewGPU* _
       // that of one pass over samples 0..spp-1, whatever the wave boundaries
       float* sp = sum + 3 * (size_t)(V.pix_off + p);
       float* qp = sumsq ? sumsq + 3 * (size_t)(V.pix_off + p) : nullptr;
+      int an = 0;
+      float sl = 0.0f, ssl = 0.0f;
+      if (V.adaptive) {
+        an = ad.n[V.pix_off + p];
+        if (an & kPixDone) continue;  // stopped in an earlier wave
+        const float2 l = ad.lum[V.pix_off + p];
+        sl = l.x;
+        ssl = l.y;
+      }
       float3 acc = f3(sp[0], sp[1], sp[2]);
       float3 acc2 = qp ? f3(qp[0], qp[1], qp[2]) : f3(0, 0, 0);
-      for (int s = s_lo; s < s_hi; s++) {
+      bool stop = false;
+      for (int s = s_lo; s < s_hi && !stop; s++) {
         const long long i = V.path_off + (long long)s * V.npix + p - w0;
         const float3 c = clamp_sample(f3(ps.lx[i], ps.ly[i], ps.lz[i]), V.clamp);
         acc = acc + c;
         acc2 = acc2 + had(c, c);
+        if (V.adaptive) stop = adaptive_step(V, c, &an, &sl, &ssl);
+      }
+      if (V.adaptive) {
+        ad.n[V.pix_off + p] = stop ? (an | kPixDone) : an;
+        ad.lum[V.pix_off + p] = make_float2(sl, ssl);
       }
       sp[0] = acc.x;
       sp[1] = acc.y;
@@ -717,8 +767,11 @@ __global__ void __launch_bounds__(256) k_gradient(const BatchState* __restrict__
   for (int k = threadIdx.x; k < np3; k += blockDim.x) row[k] += sg[k];
 }
 
-__global__ void k_advance(BatchState* bs) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) bs->w0 = min(bs->total, bs->w0 + (long long)bs->cap);
+__global__ void k_advance(BatchState* bs, WaveCounters* cnt) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    bs->w0 = min(bs->total, bs->w0 + (long long)bs->cap);
+    cnt->q[0] = 0;  // the next wave's generate appends to it
+  }
 }
 
 __global__ void k_clear_guides(int n, float4* __restrict__ nd, uint32_t* __restrict__ c) {
@@ -731,14 +784,22 @@ __global__ void k_clear_guides(int n, float4* __restrict__ nd, uint32_t* __restr
 }
 
 // mean = sum / spp for every pixel of every view
+// mean = sum / spp for every pixel of every view (sum / samples taken for an
+// adaptive view, renderer.go:1965)
 __global__ void k_finish_views(const ViewGPU* __restrict__ views, int n_views, const float* __restrict__ sum,
-                               float* __restrict__ out) {
+                               float* __restrict__ out, const int32_t* __restrict__ pix_n) {
   const int stride = gridDim.x * blockDim.x;
   for (int v = 0; v < n_views; v++) {
     const ViewGPU& V = views[v];
     const float inv = 1.0f / (float)V.spp;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * V.npix; k += stride)
-      out[3 * (size_t)V.pix_off + k] = sum[3 * (size_t)V.pix_off + k] * inv;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * V.npix; k += stride) {
+      float f = inv;
+      if (V.adaptive) {
+        const int n = pix_n[V.pix_off + k / 3] & 0x7fffffff;
+        f = 1.0f / (float)max(n, 1);
+      }
+      out[3 * (size_t)V.pix_off + k] = sum[3 * (size_t)V.pix_off + k] * f;
+    }
   }
 }
 
@@ -755,7 +816,7 @@ __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict_
                                                       float* __restrict__ sum, float* __restrict__ sumsq,
                                                       float4* __restrict__ guide_nd, uint32_t* __restrict__ guide_c,
                                                       uint32_t* __restrict__ guide_jit, WaveCounters* cnt,
-                                                      unsigned* status) {
+                                                      unsigned* status, AdaptState ad) {
   const ViewGPU& V = views[v];
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long segs = 0, shadows = 0;
@@ -766,6 +827,8 @@ __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict_
     float3 acc = f3(sp[0], sp[1], sp[2]);
     float3 acc2 = qp ? f3(qp[0], qp[1], qp[2]) : f3(0, 0, 0);
     FastWalker<STACK> w;
+    int an = 0;
+    float sl = 0.0f, ssl = 0.0f;
     for (int s = 0; s < V.spp; s++) {
       RegPath st;
       double jx, jy;
@@ -801,6 +864,14 @@ __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict_
       const float3 c = clamp_sample(st.L, V.clamp);
       acc = acc + c;
       acc2 = acc2 + had(c, c);
+      if (V.adaptive && adaptive_step(V, c, &an, &sl, &ssl)) {
+        an |= kPixDone;
+        break;
+      }
+    }
+    if (V.adaptive) {
+      ad.n[V.pix_off + p] = an;
+      ad.lum[V.pix_off + p] = make_float2(sl, ssl);
     }
     sp[0] = acc.x;
     sp[1] = acc.y;
@@ -854,6 +925,7 @@ struct RenderBuffers {
   uint32_t* guide_c = nullptr; // compact guide
   uint32_t* guide_jit = nullptr;
   uint32_t* rgba = nullptr;
+  bcgx::AdaptState adapt{};    // per-pixel adaptive-sampling state
   // path replay records (gradient renders)
   bcgx::DevBuf rec;
   bcgx::GradRec grec{};
@@ -920,7 +992,8 @@ static bc_status ensure_paths(bc_context* ctx, int cap) {
 static bc_status ensure_frame(bc_context* ctx, size_t px) {
   RenderBuffers* rb = ctx->rb;
   if (rb->frame_px >= px) return BC_OK;
-  size_t bytes = px * (5 * 3 * sizeof(float) + sizeof(float4) + 5 * sizeof(uint32_t)) + 16 * 256;
+  size_t bytes = px * (5 * 3 * sizeof(float) + sizeof(float4) + 5 * sizeof(uint32_t) + sizeof(int32_t) +
+                       sizeof(float2)) + 16 * 256;
   cudaError_t e = rb->frame.ensure(bytes);
   if (e != cudaSuccess) {
     rb->frame_px = 0;
@@ -936,6 +1009,8 @@ static bc_status ensure_frame(bc_context* ctx, size_t px) {
   rb->guide_c = carve<uint32_t>(p, 3 * px);
   rb->guide_jit = carve<uint32_t>(p, px);
   rb->rgba = carve<uint32_t>(p, px);
+  rb->adapt.n = carve<int32_t>(p, px);
+  rb->adapt.lum = carve<float2>(p, px);
   rb->frame_px = px;
   return BC_OK;
 }
@@ -1058,7 +1133,8 @@ template <int STACK, bool SPH>
 static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const ShadeScene& sc, cudaStream_t st) {
   RenderBuffers* rb = ctx->rb;
   WaveCounters* c = rb->cnt;
-  k_generate<<<w.gen_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->q[0], rb->seq_xy, rb->guide_jit, c);
+  k_generate<<<w.gen_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->q[0], rb->seq_xy, rb->guide_jit, c,
+                                         rb->adapt);
   int cur = 0;
   // Counter resets ride in the kernels: generate zeroes the first extend's work
   // counter, extend zeroes the queue and shadow list its shade fills, shade
@@ -1074,8 +1150,9 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
   if (w.grad)
     k_gradient<<<gradient_grid(), 256, 3 * w.grad->n_params * sizeof(double), st>>>(rb->bs, rb->views, rb->ps,
                                                                                   rb->grec, *w.grad, sc.mats);
-  k_accumulate<<<w.acc_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr);
-  k_advance<<<1, 32, 0, st>>>(rb->bs);
+  k_accumulate<<<w.acc_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr,
+                                           rb->adapt);
+  k_advance<<<1, 32, 0, st>>>(rb->bs, c);
   return cudaGetLastError();
 }
 
@@ -1094,6 +1171,7 @@ static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const Shad
                                   (uintptr_t)rb->cnt, (uintptr_t)rb->bs, (uintptr_t)rb->views, (uintptr_t)rb->seq_xy,
                                   (uintptr_t)rb->sum, (uintptr_t)(rb->want_sumsq ? rb->sumsq : nullptr),
                                   (uintptr_t)rb->guide_nd, (uintptr_t)rb->guide_c, (uintptr_t)rb->guide_jit,
+                                  (uintptr_t)rb->adapt.n, (uintptr_t)rb->adapt.lum,
                                   (uintptr_t)ctx->ds.n_mats, (uintptr_t)ctx->d_status};
     auto add_bytes = [&key](const void* p, size_t n) {
       const size_t k = key.size();
@@ -1163,7 +1241,7 @@ static bc_status run_plain(bc_context* ctx, const ShadeScene& sc, const std::vec
     const int grid = (views[v].npix + 127) / 128;
     k_render_plain<STACK, SPH><<<grid, 128, 0, ctx->stream>>>(
         rb->views, v, ctx->ds.n_mats, sc, rb->seq_xy, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr, rb->guide_nd,
-        rb->guide_c, rb->guide_jit, rb->cnt, ctx->d_status);
+        rb->guide_c, rb->guide_jit, rb->cnt, ctx->d_status, rb->adapt);
     cudaError_t e = cudaGetLastError();
     if (e) return cuda_status(ctx, e, "one-kernel render launch");
   }
@@ -1210,6 +1288,9 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
     V.root = sr.root;
     V.want_guides = r.want_guides ? 1 : 0;
     V.clamp = (float)r.s.firefly_clamp;
+    V.adaptive = (r.s.adaptive_sampling != 0 && !grad) ? 1 : 0;  // gradient renders take every sample
+    V.adapt_thr = (float)std::max(1e-8, r.s.adaptive_threshold);
+    V.min_samples = std::min(8, V.spp);
     V.seed = r.s.seed;
     camera_basis(r.cam, (double)V.W / (double)V.H, V.origin, V.lower, V.horiz, V.vert);
     V.path_off = total;
@@ -1276,6 +1357,9 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
   for (int v = 0; v < n && !e; v++) {
     const ViewGPU& V = views[v];
     e = cudaMemsetAsync(rb->sum + 3 * (size_t)V.pix_off, 0, 3 * sizeof(float) * (size_t)V.npix, ctx->stream);
+    if (!e && V.adaptive) e = cudaMemsetAsync(rb->adapt.n + V.pix_off, 0, sizeof(int32_t) * (size_t)V.npix, ctx->stream);
+    if (!e && V.adaptive)
+      e = cudaMemsetAsync(rb->adapt.lum + V.pix_off, 0, sizeof(float2) * (size_t)V.npix, ctx->stream);
     if (!e && rb->want_sumsq)
       e = cudaMemsetAsync(rb->sumsq + 3 * (size_t)V.pix_off, 0, 3 * sizeof(float) * (size_t)V.npix, ctx->stream);
     if (!e && V.want_guides) {  // invalid guides: depth -1, compact words 0
@@ -1312,8 +1396,9 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
     bst = sph ? run_waves<256, true>(ctx, max_bounces, lights, sc, n_waves, grad)
               : run_waves<256, false>(ctx, max_bounces, lights, sc, n_waves, grad);
   if (bst) return bst;
-  k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sum, rb->out);
-  if (rb->want_sumsq) k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sumsq, rb->post_tmp);
+  k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sum, rb->out, rb->adapt.n);
+  if (rb->want_sumsq)
+    k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sumsq, rb->post_tmp, rb->adapt.n);
   e = cudaGetLastError();
   unsigned long long r = 0;
   if (!e) e = cudaMemcpyAsync(&r, &rb->cnt->rays, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream);

@@ -312,6 +312,8 @@ def run_render(args):
                     "2560x1440, 256 spp, 16 bounces, RR from bounce 6, denoise x3, bloom 1, ACES")
     if args.spp:
         st.spp = args.spp
+    if args.adaptive is not None:  # the preset's own adaptive stop (threshold), off for equal-spp measurement
+        st.adaptive_sampling, st.adaptive_threshold = True, args.adaptive
     scene = scenes.to_scene(spec)
     ctx = bcgx.Context(0)
     if args.wave_cap:
@@ -610,6 +612,8 @@ def main():
     ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
     ap.add_argument("--rmse", action="store_true", help="render workloads: RMSE against a converged image")
     ap.add_argument("--views", type=int, default=64, help="batch workload: number of views")
+    ap.add_argument("--adaptive", type=float, default=None,
+                    help="render workloads: turn the adaptive stop on with this threshold (Ultra preset: 8e-5)")
     ap.add_argument("--wave-cap", type=int, default=0, help="render workloads: paths per wave (0 = library default)")
     ap.add_argument("--plain-steps", type=int, default=2,
                     help="render workloads: frames timed with the one-kernel form (0 = skip)")

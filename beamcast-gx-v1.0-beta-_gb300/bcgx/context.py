@@ -87,9 +87,9 @@ class Context:
         self._desc_keep = list(scenes)
 
     def scene_stats(self) -> dict:
-        out = (C.c_int64 * 6)()
-        check(lib().bc_scene_stats(self._h, out, 6), self._h)
-        keys = ("nodes8", "slots", "binary_nodes", "depth8", "stack_need", "device_bytes")
+        out = (C.c_int64 * 7)()
+        check(lib().bc_scene_stats(self._h, out, 7), self._h)
+        keys = ("nodes8", "slots", "binary_nodes", "depth8", "stack_need", "device_bytes", "geometry_updates")
         return dict(zip(keys, list(out)))
 
     # -- ray casting --

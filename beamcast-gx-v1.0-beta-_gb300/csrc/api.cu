@@ -132,7 +132,8 @@ void bc_destroy(bc_context* ctx) {
   destroy_render_buffers(ctx);
   destroy_diff_state(ctx);
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_tri, &ctx->d_slot64, &ctx->d_snorm, &ctx->d_slot_prim, &ctx->d_mats,
-                    &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ})
+                    &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ,
+                    &ctx->d_kids8, &ctx->d_geom})
     b->release();
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->d_work) cudaFree(ctx->d_work);
@@ -169,6 +170,7 @@ static bc_status install_scene(bc_context* ctx, const PackedScene& ps, const std
   if (e != cudaSuccess) return cuda_status(ctx, e, "scene upload");
   ctx->has_scene = false;
   ctx->ranges.clear();
+  ctx->geom.valid = false;
   const size_t slots = (size_t)ps.n_prims;
   bc_status st;
   if ((st = upload(ctx, ctx->d_nodes, ps.nodes.data(), ps.nodes.size() * sizeof(Node8), "BVH8 upload")) ||
@@ -227,6 +229,24 @@ static bc_status install_scene(bc_context* ctx, const PackedScene& ps, const std
   return BC_OK;
 }
 
+// Keeps what a later geometry-only update of this (single) scene needs.
+static bc_status keep_geometry_map(bc_context* ctx, const bc_scene_desc& d, const PackedScene& ps) {
+  if (ps.kids8.size() != 8 * ps.nodes.size()) return BC_OK;
+  bc_status st = upload(ctx, ctx->d_kids8, ps.kids8.data(), ps.kids8.size() * sizeof(int32_t), "child map upload");
+  if (st) return st;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e) return cuda_status(ctx, e, "child map upload");
+  GeomInfo& g = ctx->geom;
+  g.n_binary = d.n_nodes;
+  g.n_lights = d.n_lights;
+  g.n_materials = d.n_materials;
+  g.n_node8 = (int32_t)ps.nodes.size();
+  g.has_tris = false;
+  for (int32_t i = 0; i < d.n_prims && !g.has_tris; i++) g.has_tris = d.prim_kind[i] == BC_PRIM_TRIANGLE;
+  g.valid = true;
+  return BC_OK;
+}
+
 }  // namespace bcgx
 
 extern "C" {
@@ -238,14 +258,26 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
       ctx->geom_rev == geometry_rev)
     return BC_OK;
   cudaSetDevice(ctx->device);
+  bc_status st;
+  if (ctx->has_scene && !ctx->is_set && ctx->scene_id == scene_id && ctx->topo_rev == topology_rev) {
+    // only the geometry moved: rewrite primitives and node boxes on the device
+    st = update_geometry(ctx, *scene);
+    if (st == BC_OK) {
+      ctx->geom_rev = geometry_rev;
+      ctx->stats[6]++;
+      return BC_OK;
+    }
+    if (st != BC_ERR_INVALID_ARG) return st;  // a device error; the descriptor itself did not fit: full upload
+  }
   PackedScene ps;
   std::string err;
-  bc_status st = pack_scene(*scene, &ps, &err);
+  st = pack_scene(*scene, &ps, &err);
   if (st != BC_OK) return set_error(ctx, st, err);
   SceneRange r;
   r.n_lights = (int32_t)ps.lights.size();
   r.n_slots = ps.n_prims;
   if ((st = install_scene(ctx, ps, std::vector<SceneRange>{r}))) return st;
+  if ((st = keep_geometry_map(ctx, *scene, ps))) return st;
   ctx->is_set = false;
   ctx->scene_id = scene_id;
   ctx->topo_rev = topology_rev;
@@ -276,7 +308,7 @@ bc_status bc_scene_set_upload(bc_context* ctx, const bc_scene_desc* scenes, int3
 bc_status bc_scene_stats(const bc_context* ctx, int64_t* out, int n_out) {
   if (!ctx || !out || n_out < 0) return BC_ERR_INVALID_ARG;
   if (!ctx->has_scene) return BC_ERR_NO_SCENE;
-  for (int i = 0; i < n_out && i < 6; i++) out[i] = ctx->stats[i];
+  for (int i = 0; i < n_out && i < 7; i++) out[i] = ctx->stats[i];
   return BC_OK;
 }
 

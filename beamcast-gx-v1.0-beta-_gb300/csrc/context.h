@@ -54,6 +54,13 @@ struct HostBuf {
   }
 };
 
+// What the geometry-only update needs to know about the resident scene.
+struct GeomInfo {
+  bool valid = false;  // the resident scene came from bc_scene_upload and kept its BVH8 child map
+  int32_t n_binary = 0, n_lights = 0, n_materials = 0, n_node8 = 0;
+  bool has_tris = false;
+};
+
 }  // namespace bcgx
 
 struct bc_context {
@@ -69,9 +76,11 @@ struct bc_context {
   bcgx::DevBuf d_nodes, d_tri, d_slot64, d_snorm, d_slot_prim, d_mats, d_lights, d_lpdf;
   std::vector<bcgx::SceneRange> ranges;  // scenes of the resident set (one for bc_scene_upload)
   bool is_set = false;                    // resident scenes came from bc_scene_set_upload
+  bcgx::GeomInfo geom;                    // geometry-only updates (refit.cu)
+  bcgx::DevBuf d_kids8, d_geom;           // Node8 -> binary child map; fp64 geometry staging
   std::vector<int8_t> mat_kind;           // host copy of the resident materials' kinds
   std::vector<int8_t> mat_is_light;       // 1: material of a sphere light (its emission feeds NEE records)
-  int64_t stats[6] = {0, 0, 0, 0, 0, 0};
+  int64_t stats[7] = {0, 0, 0, 0, 0, 0, 0};  // bc_scene_stats; [6] counts geometry-only updates
   int raycast_minblocks = 6;  // register budget of the exact ray-cast kernels (bc_set_option)
   int raycast_exact = 1;      // 0: plain fp32 closest hit (bc_set_option "raycast_exact")
   int raycast_variant = 6;    // 0 = fast kernel, else the exact kernel's minblocks
@@ -98,4 +107,5 @@ bc_status cuda_status(bc_context* ctx, cudaError_t e, const char* what);
 bc_status check_kernel_status(bc_context* ctx);
 void destroy_render_buffers(bc_context* ctx);
 void destroy_diff_state(bc_context* ctx);
+bc_status update_geometry(bc_context* ctx, const bc_scene_desc& d);  // refit.cu
 }  // namespace bcgx

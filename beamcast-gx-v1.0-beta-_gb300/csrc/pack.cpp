@@ -8,18 +8,12 @@
 #include <cmath>
 #include <cstring>
 
+#include "quantize.h"
+
 namespace bcgx {
 
-float round_down_f32(double x) {
-  float f = (float)x;
-  if ((double)f > x) f = std::nextafterf(f, -INFINITY);
-  return f;
-}
-float round_up_f32(double x) {
-  float f = (float)x;
-  if ((double)f < x) f = std::nextafterf(f, INFINITY);
-  return f;
-}
+float round_down_f32(double x) { return rd_f32(x); }
+float round_up_f32(double x) { return ru_f32(x); }
 
 namespace {
 
@@ -108,81 +102,24 @@ void pack_slots(const bc_scene_desc& d, PackedScene* ps) {
   for (int32_t s = 0; s < n; s++) {
     const int32_t p = d.order[s];
     ps->slot_prim[s] = p;
-    F4* r = &ps->tri[3 * (size_t)s];
-    double* q = &ps->slot64[9 * (size_t)s];
     int32_t mat = d.prim_material[p];
     float matbits;
     std::memcpy(&matbits, &mat, 4);
-    if (d.prim_kind[p] == BC_PRIM_SPHERE) {
-      ps->has_spheres = true;
-      const double* c = d.prim_center + 3 * (size_t)p;
-      double rad = d.prim_radius[p];
-      r[0] = F4{(float)c[0], (float)c[1], (float)c[2], (float)rad};
-      r[1] = F4{(float)(rad * rad), rad > 0 ? (float)(1.0 / rad) : 0.0f, 0.0f, 0.0f};
-      r[2] = F4{0.0f, 0.0f, 0.0f, -1.0f};
-      q[0] = c[0]; q[1] = c[1]; q[2] = c[2]; q[3] = rad;
-      ps->snorm[s] = F4{0.0f, 0.0f, 0.0f, matbits};
-    } else {
-      const double* a = d.prim_a + 3 * (size_t)p;
-      const double* e1 = d.prim_e1 + 3 * (size_t)p;
-      const double* e2 = d.prim_e2 + 3 * (size_t)p;
-      const double* nn = d.prim_normal + 3 * (size_t)p;
-      auto amax = [](const double* v) {
-        return round_up_f32(std::max(std::fabs(v[0]), std::max(std::fabs(v[1]), std::fabs(v[2]))));
-      };
-      r[0] = F4{(float)a[0], (float)a[1], (float)a[2], amax(a)};
-      r[1] = F4{(float)e1[0], (float)e1[1], (float)e1[2], amax(e1)};
-      r[2] = F4{(float)e2[0], (float)e2[1], (float)e2[2], amax(e2)};
-      for (int k = 0; k < 3; k++) { q[k] = a[k]; q[3 + k] = e1[k]; q[6 + k] = e2[k]; }
-      ps->snorm[s] = F4{(float)nn[0], (float)nn[1], (float)nn[2], matbits};
-    }
+    const bool sphere = d.prim_kind[p] == BC_PRIM_SPHERE;
+    ps->has_spheres = ps->has_spheres || sphere;
+    const double zero[3] = {0.0, 0.0, 0.0};
+    const size_t k3 = 3 * (size_t)p;
+    float nrm[3];
+    pack_slot(sphere, sphere ? d.prim_center + k3 : zero, sphere ? d.prim_radius[p] : 0.0,
+              sphere ? zero : d.prim_a + k3, sphere ? zero : d.prim_e1 + k3, sphere ? zero : d.prim_e2 + k3,
+              sphere ? zero : d.prim_normal + k3, &ps->tri[3 * (size_t)s], &ps->slot64[9 * (size_t)s], nrm);
+    ps->snorm[s] = F4{nrm[0], nrm[1], nrm[2], matbits};
   }
 }
 
-// Quantizes the child boxes of one node. Per axis: p = the children's union
-// minimum rounded down to fp32 and stepped one ulp further down, the grid step
-// 2^e the smallest power of two with 254 * 2^e >= extent, qlo = the largest q
-// with p + q 2^e < lo (strict), qhi = the smallest q with p + q 2^e > hi. The
-// device decodes with round-down (lo) and round-up (hi) FMAs, which keeps the
-// strict inequalities, so a ray origin on a face of the fp64 box is strictly
-// inside the decoded box (the reference's zero-direction axes test origins
-// against closed boxes).
 void quantize_node(Node8& n, const double* boxes, int nk) {
-  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (int k = 0; k < nk; k++)
-    for (int a = 0; a < 3; a++) {
-      lo[a] = std::min(lo[a], boxes[6 * k + a]);
-      hi[a] = std::max(hi[a], boxes[6 * k + 3 + a]);
-    }
-  float p[3];
-  uint8_t eb[3];
-  double scale[3];
-  for (int a = 0; a < 3; a++) {
-    p[a] = std::nextafterf(round_down_f32(lo[a]), -INFINITY);
-    const double extent = hi[a] - (double)p[a];
-    int e = -126;
-    while (e < 127 && std::ldexp(254.0, e) < extent) e++;
-    eb[a] = (uint8_t)(e + 127);
-    scale[a] = std::ldexp(1.0, e);
-  }
-  n.px = p[0]; n.py = p[1]; n.pz = p[2];
-  n.ex = eb[0]; n.ey = eb[1]; n.ez = eb[2];
+  quantize_children(n, boxes, nk);
   n.nchild = (uint8_t)nk;
-  uint8_t* qlo[3] = {n.qlox, n.qloy, n.qloz};
-  uint8_t* qhi[3] = {n.qhix, n.qhiy, n.qhiz};
-  for (int k = 0; k < 8; k++)
-    for (int a = 0; a < 3; a++) {
-      if (k >= nk) { qlo[a][k] = 255; qhi[a][k] = 0; continue; }
-      const double bl = boxes[6 * k + a], bh = boxes[6 * k + 3 + a];
-      double ql = std::floor((bl - (double)p[a]) / scale[a]);
-      ql = std::max(0.0, std::min(255.0, ql));
-      while (ql > 0 && (double)p[a] + ql * scale[a] >= bl) ql -= 1;
-      double qh = std::ceil((bh - (double)p[a]) / scale[a]);
-      qh = std::max(0.0, std::min(255.0, qh));
-      while (qh < 255 && (double)p[a] + qh * scale[a] <= bh) qh += 1;
-      qlo[a][k] = (uint8_t)ql;
-      qhi[a][k] = (uint8_t)qh;
-    }
 }
 
 uint32_t leaf_ref(const bc_scene_desc& d, int32_t i) {
@@ -232,6 +169,8 @@ void collapse(const bc_scene_desc& d, PackedScene* ps) {
     double boxes[48];
     for (int k = 0; k < nk; k++) std::memcpy(boxes + 6 * k, d.node_box + 6 * (size_t)kids[k], 6 * sizeof(double));
     quantize_node(n, boxes, nk);
+    ps->kids8.resize(8 * ps->nodes.size(), -1);
+    for (int k = 0; k < nk; k++) ps->kids8[8 * (size_t)idx + k] = kids[k];
     ps->depth = std::max(ps->depth, j.depth);
     ps->stack_need = std::max(ps->stack_need, j.acc + nk + 1);
     for (int k = nk - 1; k >= 0; k--) {
@@ -375,12 +314,6 @@ bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::v
   return BC_OK;
 }
 
-bc_status repack_geometry(const bc_scene_desc& d, PackedScene* io, std::string* err) {
-  if (d.n_prims != io->n_prims || d.n_nodes != io->n_binary) {
-    if (err) *err = "geometry update changes the topology; a full upload is required";
-    return BC_ERR_BAD_SCENE;
-  }
-  return pack_scene(d, io, err);
-}
+void pack_scene_lights(const bc_scene_desc& d, PackedScene* out) { pack_lights(d, out); }
 
 }  // namespace bcgx

@@ -16,6 +16,7 @@ struct PackedScene {
   std::vector<double> slot64;    // 9 per slot
   std::vector<F4> snorm;         // 1 per slot
   std::vector<int32_t> slot_prim;
+  std::vector<int32_t> kids8;    // 8 per node: binary node index of each child (-1: empty slot)
   std::vector<MatGPU> mats;
   std::vector<LightGPU> lights;
   std::vector<float> light_pdf_by_prim;
@@ -42,8 +43,8 @@ bc_status pack_scene(const bc_scene_desc& d, PackedScene* out, std::string* err)
 // `ranges[k]` tells where each scene starts. stack_need is the maximum.
 bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::vector<SceneRange>* ranges,
                          std::string* err);
-// Re-packs only geometry (boxes and primitive records) for an unchanged topology.
-bc_status repack_geometry(const bc_scene_desc& d, PackedScene* io, std::string* err);
+// Sphere-light records and per-primitive light selection pdfs of a scene.
+void pack_scene_lights(const bc_scene_desc& d, PackedScene* out);
 
 float round_down_f32(double x);
 float round_up_f32(double x);

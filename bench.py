@@ -595,6 +595,55 @@ def run_diff(args):
     return 0
 
 
+def run_refit(args):
+    """Geometry-only update of the ray-cast scene (1M random triangles): 1% of
+    the triangles move, Scene.Refit (host builder) refits the node boxes, and
+    bc_scene_upload takes the device path (primitives and boxes copied up,
+    slots rewritten, every BVH8 node re-quantized on the GPU). Compared with a
+    full upload of the same scene (host validation, BVH8 collapse, packing).
+    Time per step = wall time of the bc_scene_upload call (host refit excluded)."""
+    import numpy as np
+    import bcgx
+    from bcgx import scenes
+    spec = scenes.random_triangles(N_TRIS)
+    scene = scenes.to_scene(spec)
+    ctx = bcgx.Context(0)
+    ctx.upload(scene)
+    rng = np.random.default_rng(0xBEAC0106)
+    geo, full, refit_s = [], [], []
+    for k in range(args.warmup + args.steps):
+        for i in rng.choice(N_TRIS, N_TRIS // 100, replace=False):
+            scene.translate_primitive(int(i), rng.normal(0.0, 0.002, 3))
+        t0 = time.perf_counter()
+        scene.refit()
+        t1 = time.perf_counter()
+        ctx.upload(scene)
+        t2 = time.perf_counter()
+        ctx.upload(scene, scene_id=0x5EED0000 + k)  # full path
+        t3 = time.perf_counter()
+        ctx.upload(scene)  # back to the tracked id for the next drag (full path again)
+        if k >= args.warmup:
+            refit_s.append(t1 - t0)
+            geo.append(t2 - t1)
+            full.append(t3 - t2)
+    stats = ctx.scene_stats()
+    line = {"metric": "geometry update ms", "value": 1e3 * statistics.median(geo), "unit": "ms",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(geo),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64 in, f32/f64 records",
+            "data": "synthetic, seeded (tris seed 0xBEAC0002)",
+            "config": {"workload": f"refit: {N_TRIS} random tris, 1% moved per step", "bvh8_nodes": stats["nodes8"],
+                       "binary_nodes": stats["binary_nodes"]},
+            "full_upload_ms": 1e3 * statistics.median(full),
+            "host_refit_ms": 1e3 * statistics.median(refit_s),
+            "geometry_updates": stats["geometry_updates"],
+            "e2e": {"value": 1e3 * statistics.median(geo), "unit": "ms",
+                    "h2d_bytes_per_step": 8 * (16 * N_TRIS + 6 * stats["binary_nodes"]), "d2h_bytes_per_step": 0},
+            "gpu_launches": 2 * args.steps}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     global N_TRIS, N_RAYS
     ap = argparse.ArgumentParser()
@@ -607,7 +656,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
     ap.add_argument("--minblocks", type=int, default=0, help="ray-cast register variant (1, 6, 8; 0 = library default)")
     ap.add_argument("--fast", action="store_true", help="plain fp32 closest hit instead of the exact contract")
-    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch", "diff"],
+    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch", "diff", "refit"],
                     help="raycast (default, the headline line) or a render workload")
     ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
     ap.add_argument("--rmse", action="store_true", help="render workloads: RMSE against a converged image")
@@ -627,6 +676,8 @@ def main():
         return run_batch(args)
     if args.workload == "diff":
         return run_diff(args)
+    if args.workload == "refit":
+        return run_refit(args)
     if args.workload != "raycast":
         return run_render(args)
     return run_gpu(args)

@@ -133,8 +133,10 @@ bc_status bc_device_name(const bc_context* ctx, char* buf, size_t len);
  * Upload or update a scene; replaces ensureSceneLocked (gpu_opencl_windows.go:484-495)
  * with uploadFullSceneLocked (379) and updateGeometryLocked (447). scene_id
  * identifies the caller's scene object (Go: the *Scene pointer value). When
- * scene_id and topology_rev match the resident scene, only geometry is
- * re-packed if geometry_rev changed; when all three match, the call is a no-op.
+ * scene_id and topology_rev match the resident scene and only geometry_rev
+ * changed, the primitives and the caller's refit node boxes replace the
+ * resident ones on the device (same primitive and node counts required, else
+ * a full upload); when all three match, the call is a no-op.
  * Leaves with more than 16 primitives or more than 2^27 nodes/primitives are
  * rejected with BC_ERR_BAD_SCENE, as validateGPUSceneEncoding (470-482) does.
  */
@@ -155,7 +157,10 @@ bc_status bc_scene_set_upload(bc_context* ctx, const bc_scene_desc* scenes, int3
 
 /* Statistics of the resident scene: out[0] BVH8 nodes, out[1] primitive slots,
  * out[2] binary nodes, out[3] BVH8 depth, out[4] traversal stack entries needed,
- * out[5] device bytes held by the scene. */
+ * out[5] device bytes held by the scene, out[6] geometry-only updates applied
+ * by this context (the device path of bc_scene_upload when only geometry_rev
+ * moved: new primitives and refit node boxes are copied up, slots rewritten and
+ * every BVH8 node re-quantized on the GPU, the BVH8 topology kept). */
 bc_status bc_scene_stats(const bc_context* ctx, int64_t* out, int n_out);
 
 /* ---- ray casting (closest hit / any hit) -------------------------------- */

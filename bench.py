@@ -293,6 +293,21 @@ def run_gpu(args):
     return 0
 
 
+def _render_roofline(stats, mseg_per_s):
+    """Algorithmic bytes per path segment from the oracle's binary-BVH counters on
+    the CPU sample (32 B per box test, 40 per triangle, 32 per sphere, 32 of ray in
+    and hit out per query incl. shadow rays) plus 160 B of path state read and
+    written and 32 B of material per segment; achieved = that x segments/s."""
+    segs = max(1, stats["segments"])
+    per_seg = (32 * stats["boxes"] + 40 * stats["tris"] + 32 * stats["spheres"] +
+               32 * (stats["segments"] + stats["shadow"])) / segs + 160 + 32
+    peak, kind = _peaks()
+    achieved = per_seg * mseg_per_s * 1e6 / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "peak_kind": kind, "algorithmic_bytes_per_segment": per_seg,
+            "scope": "whole frame (all kernels), not one kernel"}
+
+
 def run_render(args):
     """Render workloads (one JSON line each): `cornell` = the Cornell-box
     configuration (320x240, 16 spp, 5 bounces, RR from 3, Halton, MIS, power
@@ -384,6 +399,7 @@ def run_render(args):
         line["cpu_baseline"] = {"value": out["stats"]["segments"] / dt / 1e6, "unit": METRIC,
                                 "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"{cst.width}x{cst.height} at {cst.spp} spp, {dt:.1f} s"}
+        line["roofline"] = _render_roofline(out["stats"], value)
         if args.rmse and args.workload == "cornell":
             c16 = st.copy()
             cpu_img = ref.render(cam, c16, seed=11, threads=0)["linear"]
@@ -500,6 +516,7 @@ def run_batch(args):
     if not args.no_cpu_baseline:
         import oracle
         t_all, segs = 0.0, 0
+        agg = {"segments": 0, "shadow": 0, "boxes": 0, "tris": 0, "spheres": 0}
         sample = []
         for v in range(4):  # one view of each scene, 1 spp
             k, cam, st = views[v]
@@ -510,9 +527,12 @@ def run_batch(args):
             out = ref.render(cam, cst, seed=7, threads=0)
             t_all += time.perf_counter() - t0
             segs += out["stats"]["segments"]
+            for key in agg:
+                agg[key] += out["stats"][key]
             sample.append(f"{cst.width}x{cst.height}")
         line["cpu_baseline"] = {"value": segs / t_all / 1e6, "unit": METRIC, "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"views 0-3 (one per scene: {', '.join(sample)}) at 1 spp, {t_all:.1f} s"}
+        line["roofline"] = _render_roofline(agg, value)
     print(json.dumps(line), flush=True)
     ctx.close()
     return 0

@@ -565,6 +565,14 @@ struct Contender {
 
 constexpr int kPending = 4;
 
+// A pending contender keeps only what decides whether it is settled later:
+// its slot and the lower end of its distance interval (settlement recomputes
+// the fp64 distance).
+struct PendEntry {
+  int32_t slot;
+  float lo;
+};
+
 template <bool SPHERES>
 struct ExactClosestLeaf {
   const SceneView& sv;
@@ -575,7 +583,7 @@ struct ExactClosestLeaf {
   bool done;
   Contender best;
   int npend;
-  Contender pend[kPending];
+  PendEntry pend[kPending];
 
   __device__ ExactClosestLeaf(const SceneView& s, const Ray32& ray, float tmax, unsigned* st)
       : sv(s), r(ray), status(st) {
@@ -622,7 +630,7 @@ struct ExactClosestLeaf {
   // settle it now when the list is full.
   __device__ __forceinline__ void defer_maybe(Contender c) {
     if (npend < kPending) {
-      pend[npend++] = c;
+      pend[npend++] = PendEntry{c.slot, c.lo};
       return;
     }
     if (resolve(c)) settle_against_best(c);
@@ -636,10 +644,10 @@ struct ExactClosestLeaf {
       return;
     } else if (npend < kPending) {
       if (c.hi < best.hi) {
-        pend[npend++] = best;
+        pend[npend++] = PendEntry{best.slot, best.lo};
         best = c;
       } else {
-        pend[npend++] = c;
+        pend[npend++] = PendEntry{c.slot, c.lo};
       }
     } else {
       if (!resolve(c)) {
@@ -696,7 +704,12 @@ struct ExactClosestLeaf {
 #pragma unroll
     for (int k = 0; k < kPending; k++) {
       if (k < npend && !(best.slot >= 0 && pend[k].lo > best.hi)) {
-        Contender c = pend[k];
+        Contender c;
+        c.slot = pend[k].slot;
+        c.lo = pend[k].lo;
+        c.hi = __int_as_float(0x7f800000);
+        c.t64 = 0.0;
+        c.exact = false;
         if (resolve(c) &&
             (win.slot < 0 || c.t64 < win.t64 || (c.t64 == win.t64 && c.slot > win.slot)))
           win = c;

@@ -68,6 +68,8 @@ SIGNATURES = [
     ("bc_device_name", C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     ("bc_scene_upload", C.c_int, [C.c_void_p, P(SceneDesc), C.c_uint64, C.c_uint64, C.c_uint64]),
     ("bc_scene_set_upload", C.c_int, [C.c_void_p, P(SceneDesc), C.c_int32, C.c_uint64, C.c_uint64]),
+    ("bc_build_sah", C.c_int, [C.c_void_p, C.c_int32, f64p, f64p, C.c_int32, C.c_int32, i32p, f64p, i32p, i32p,
+                               i32p, i32p, i32p]),
     ("bc_scene_stats", C.c_int, [C.c_void_p, i64p, C.c_int]),
     ("bc_raycast", C.c_int, [C.c_void_p, f32p, C.c_int64, f32p, i32p]),
     ("bc_raycast_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -96,6 +98,7 @@ SIGNATURES = [
     ("bc_hscene_translate_prim", C.c_int, [C.c_void_p, C.c_int32, f64p]),
     ("bc_hscene_set_bvh", None, [C.c_void_p, C.c_char_p, C.c_int32, C.c_int32]),
     ("bc_hscene_build", C.c_int, [C.c_void_p]),
+    ("bc_hscene_build_device", C.c_int, [C.c_void_p, C.c_void_p]),
     ("bc_hscene_refit", C.c_int, [C.c_void_p]),
     ("bc_hscene_counts", None, [C.c_void_p, i64p]),
     ("bc_hscene_describe", C.c_int, [C.c_void_p, P(SceneDesc)]),

@@ -83,6 +83,11 @@ class Scene:
         lib().bc_hscene_set_bvh(self._h, self.bvh_mode.encode(), int(self.bvh_bins), int(self.bvh_leaf))
         check(lib().bc_hscene_build(self._h))
 
+    def build_device(self, ctx):
+        """Scene.Build with the SAH tree built on the GPU of `ctx` (same result as build())."""
+        lib().bc_hscene_set_bvh(self._h, self.bvh_mode.encode(), int(self.bvh_bins), int(self.bvh_leaf))
+        check(lib().bc_hscene_build_device(self._h, ctx.handle), ctx.handle)
+
     def refit(self):
         check(lib().bc_hscene_refit(self._h))
 

@@ -133,7 +133,7 @@ void bc_destroy(bc_context* ctx) {
   destroy_diff_state(ctx);
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_tri, &ctx->d_slot64, &ctx->d_snorm, &ctx->d_slot_prim, &ctx->d_mats,
                     &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ,
-                    &ctx->d_kids8, &ctx->d_geom})
+                    &ctx->d_kids8, &ctx->d_geom, &ctx->d_build, &ctx->d_build_out})
     b->release();
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->d_work) cudaFree(ctx->d_work);

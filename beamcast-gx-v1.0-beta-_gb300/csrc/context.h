@@ -78,6 +78,7 @@ struct bc_context {
   bool is_set = false;                    // resident scenes came from bc_scene_set_upload
   bcgx::GeomInfo geom;                    // geometry-only updates (refit.cu)
   bcgx::DevBuf d_kids8, d_geom;           // Node8 -> binary child map; fp64 geometry staging
+  bcgx::DevBuf d_build, d_build_out;      // device SAH build (build.cu)
   std::vector<int8_t> mat_kind;           // host copy of the resident materials' kinds
   std::vector<int8_t> mat_is_light;       // 1: material of a sphere light (its emission feeds NEE records)
   int64_t stats[7] = {0, 0, 0, 0, 0, 0, 0};  // bc_scene_stats; [6] counts geometry-only updates

@@ -457,3 +457,55 @@ bc_status bc_hscene_describe(const bc_hscene* s, bc_scene_desc* d) {
 }
 
 }  // extern "C"
+
+namespace bcgx {
+
+// Scene.Build in SAH mode with the tree produced by an external builder (the
+// device build): the clamps, revisions and light distribution of
+// bc_hscene_build, then `fn` fills the node arrays and Order.
+using TreeBuildFn = bc_status (*)(void* user, int32_t n, const double* pbox, const double* cent, int32_t bins,
+                                  int32_t leaf, int32_t* n_nodes, double* box, int32_t* left, int32_t* right,
+                                  int32_t* start, int32_t* count, int32_t* order);
+bc_status hscene_build_external(bc_hscene* s, TreeBuildFn fn, void* user) {
+  if (!s || !fn) return BC_ERR_INVALID_ARG;
+  std::string lower = s->mode.empty() ? std::string("sah") : s->mode;
+  for (auto& ch : lower) ch = (char)std::tolower((unsigned char)ch);
+  if (lower == "median" || s->nprims() == 0) return bc_hscene_build(s);
+  s->topo++;
+  s->geom++;
+  s->rebuild_lights();
+  if (s->mode.empty()) s->mode = "SAH";  // the clamps of bc_hscene_build (renderer.go:413-427)
+  if (s->bins < 4) s->bins = 16;
+  if (s->bins > 32) s->bins = 32;
+  if (s->leaf < 1) s->leaf = 4;
+  if (s->leaf > 16) s->leaf = 16;
+  const int32_t n = s->nprims();
+  const size_t cap = 2 * (size_t)n - 1;
+  try {
+    s->nbox.assign(6 * cap, 0.0);
+    s->left.assign(cap, -1);
+    s->right.assign(cap, -1);
+    s->start.assign(cap, 0);
+    s->count.assign(cap, 0);
+    s->order.assign(n, 0);
+  } catch (const std::bad_alloc&) {
+    return BC_ERR_OOM;
+  }
+  int32_t nn = 0;
+  const bc_status st = fn(user, n, reinterpret_cast<const double*>(s->pbox.data()), s->cent.data(), s->bins, s->leaf,
+                          &nn, s->nbox.data(), s->left.data(), s->right.data(), s->start.data(), s->count.data(),
+                          s->order.data());
+  if (st != BC_OK) {
+    s->left.clear(); s->right.clear(); s->start.clear(); s->count.clear(); s->nbox.clear();
+    return st;
+  }
+  s->nbox.resize(6 * (size_t)nn);
+  s->left.resize(nn);
+  s->right.resize(nn);
+  s->start.resize(nn);
+  s->count.resize(nn);
+  return BC_OK;
+}
+
+}  // namespace bcgx
+

@@ -664,6 +664,53 @@ def run_refit(args):
     return 0
 
 
+def run_build(args):
+    """Binned SAH build (32 bins, leaf 4) of the ray-cast scene (1M random
+    triangles) and of the Ultra-shaped scene (2,048,130 triangles): the host
+    builder (the reference's buildNodeSAH restated in C++, one thread) vs the
+    device build (bc_build_sah: same nodes and Order, bit for bit; host-side
+    light distribution and array copies included in its time)."""
+    import numpy as np
+    import bcgx
+    from bcgx import scenes
+    ctx = bcgx.Context(0)
+    out = {}
+    for name, spec in (("random_1M", scenes.random_triangles(N_TRIS)), ("ultra_2M", scenes.icosphere_grid()[0])):
+        host = scenes.to_scene(spec, build=False)
+        dev = scenes.to_scene(spec, build=False)
+        for s_ in (host, dev):
+            s_.bvh_mode, s_.bvh_bins, s_.bvh_leaf = "SAH", 32, 4
+        th, td = [], []
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            dev.build_device(ctx)
+            t1 = time.perf_counter()
+            if k >= args.warmup:
+                td.append(t1 - t0)
+        for k in range(max(1, min(args.steps, 2))):
+            t0 = time.perf_counter()
+            host.build()
+            th.append(time.perf_counter() - t0)
+        same = all(np.array_equal(x, y) for x, y in zip(
+            (host.arrays().node_left, host.arrays().order), (dev.arrays().node_left, dev.arrays().order)))
+        out[name] = {"prims": spec.n_triangles(), "device_ms": 1e3 * statistics.median(td),
+                     "host_ms": 1e3 * statistics.median(th), "identical": bool(same)}
+    value = out["ultra_2M"]["device_ms"]
+    line = {"metric": "SAH build ms", "value": value, "unit": "ms", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic, seeded",
+            "config": {"workload": "binned SAH build, 32 bins, leaf 4: Ultra-shaped scene (value) and 1M random tris"},
+            "builds": out,
+            "cpu_baseline": {"value": out["ultra_2M"]["host_ms"], "unit": "ms", "cores": 1, "kind": "port",
+                             "sample": "the host builder (buildNodeSAH restated), whole Ultra-shaped scene"},
+            "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 72 * out["ultra_2M"]["prims"],
+                    "d2h_bytes_per_step": 4 * out["ultra_2M"]["prims"] + 2 * out["ultra_2M"]["prims"] * 64},
+            "gpu_launches": None}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     global N_TRIS, N_RAYS
     ap = argparse.ArgumentParser()
@@ -676,7 +723,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
     ap.add_argument("--minblocks", type=int, default=0, help="ray-cast register variant (1, 6, 8; 0 = library default)")
     ap.add_argument("--fast", action="store_true", help="plain fp32 closest hit instead of the exact contract")
-    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch", "diff", "refit"],
+    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch", "diff", "refit", "build"],
                     help="raycast (default, the headline line) or a render workload")
     ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
     ap.add_argument("--rmse", action="store_true", help="render workloads: RMSE against a converged image")
@@ -698,6 +745,8 @@ def main():
         return run_diff(args)
     if args.workload == "refit":
         return run_refit(args)
+    if args.workload == "build":
+        return run_build(args)
     if args.workload != "raycast":
         return run_render(args)
     return run_gpu(args)

@@ -155,6 +155,21 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
 bc_status bc_scene_set_upload(bc_context* ctx, const bc_scene_desc* scenes, int32_t n_scenes, uint64_t set_id,
                               uint64_t revision);
 
+/*
+ * Binned SAH build on the device with the result of Scene.Build's SAH mode
+ * (buildNodeSAH, renderer.go:526-633): the same nodes in the same pre-order
+ * numbering and the same Scene.Order, bit for bit. prim_box: 6 doubles per
+ * primitive (the padded Primitive.Box: min xyz, max xyz); centroid: 3 doubles
+ * per primitive; bins and leaf_size are clamped as Scene.Build clamps them.
+ * Outputs (host arrays): node arrays of capacity 2 * n_prims - 1, filled up to
+ * *n_nodes_out; node_box 6 doubles per node; left/right -1 for leaves; start
+ * and count 0 for inner nodes; order_out n_prims. No reference counterpart on
+ * the GPU (the reference builds on the host).
+ */
+bc_status bc_build_sah(bc_context* ctx, int32_t n_prims, const double* prim_box, const double* centroid, int32_t bins,
+                       int32_t leaf_size, int32_t* n_nodes_out, double* node_box, int32_t* node_left,
+                       int32_t* node_right, int32_t* node_start, int32_t* node_count, int32_t* order_out);
+
 /* Statistics of the resident scene: out[0] BVH8 nodes, out[1] primitive slots,
  * out[2] binary nodes, out[3] BVH8 depth, out[4] traversal stack entries needed,
  * out[5] device bytes held by the scene, out[6] geometry-only updates applied

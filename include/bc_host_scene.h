@@ -40,6 +40,9 @@ bc_status bc_hscene_translate_prim(bc_hscene* s, int32_t index, const double del
 void bc_hscene_set_bvh(bc_hscene* s, const char* mode, int32_t bins, int32_t leaf_size);
 /* Scene.Build (renderer.go:409-449): light distribution, then the BVH. Bumps both revisions. */
 bc_status bc_hscene_build(bc_hscene* s);
+/* Scene.Build with the BVH built on the device (bc_build_sah): the same result as
+ * bc_hscene_build in SAH mode; the Median mode is built on the host. */
+bc_status bc_hscene_build_device(bc_hscene* s, bc_context* ctx);
 /* Scene.Refit (renderer.go:451-473): bottom-up box refit; bumps the geometry revision. */
 bc_status bc_hscene_refit(bc_hscene* s);
 

@@ -59,6 +59,15 @@ class DiffDescC(C.Structure):
                 ("emission_materials", P(C.c_int32))]
 
 
+class PostDescC(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("render_width", C.c_int32),
+                ("render_height", C.c_int32), ("hbao", C.c_int32), ("hbao_plus", C.c_int32),
+                ("denoise", C.c_int32), ("taa", C.c_int32), ("tsaa", C.c_int32), ("txaa", C.c_int32),
+                ("bloom", C.c_int32), ("fxaa", C.c_int32), ("upscale", C.c_int32), ("debug_view", C.c_int32),
+                ("hdr", C.c_int32), ("reserved", C.c_int32), ("exposure", C.c_double), ("gamma", C.c_double),
+                ("camera", CameraC)]
+
+
 # (name, restype, argtypes) for every exported symbol of the two headers.
 SIGNATURES = [
     ("bc_gpu_available", C.c_int, [C.c_char_p, C.c_size_t]),
@@ -83,6 +92,8 @@ SIGNATURES = [
     ("bc_diff_set_target", C.c_int, [C.c_void_p, f32p]),
     ("bc_forward", C.c_int, [C.c_void_p, f32p, C.c_uint64, f32p, f64p]),
     ("bc_backward", C.c_int, [C.c_void_p, f32p, f32p, f32p]),
+    ("bc_post_stack", C.c_int, [C.c_void_p, P(PostDescC), f32p, f32p, f32p, u32p]),
+    ("bc_post_history_reset", C.c_int, [C.c_void_p]),
     ("bc_post_process", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, f32p, f32p, P(SettingsC), f32p, u32p]),
     ("bc_post_process_noalloc", C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, P(SettingsC), C.c_void_p,
                                           C.c_void_p, C.c_void_p]),

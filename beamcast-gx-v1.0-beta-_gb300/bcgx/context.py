@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import DiffDescC, SceneDesc, ViewC, check, lib, ptr
+from ._lib import DiffDescC, PostDescC, SceneDesc, ViewC, check, lib, ptr
 from .scene import Scene, SceneArrays
 from .settings import Camera, RenderSettings
 
@@ -216,6 +216,32 @@ class Context:
         check(lib().bc_backward(self._h, ptr(dd, C.c_float), ptr(ga, C.c_float) if na else None,
                                 ptr(ge, C.c_float) if ne else None), self._h)
         return ga, ge
+
+    def post_stack(self, linear: np.ndarray, guides12: np.ndarray | None, cam: Camera, width: int, height: int,
+                   want_rgba: bool = True, **levels):
+        """RenderState.Start's whole post stack on caller buffers. linear: (rh, rw, 3);
+        guides12: (rh, rw, 12) = P xyz, depth, N xyz, valid, albedo xyz, 0. levels: hbao,
+        hbao_plus, denoise, taa, tsaa, txaa, bloom, fxaa, upscale (0-3), debug_view (0-5),
+        hdr, exposure, gamma. Returns (linear (height, width, 3), rgba or None)."""
+        lin = np.ascontiguousarray(linear, dtype=np.float32)
+        rh, rw = lin.shape[:2]
+        g = None if guides12 is None else np.ascontiguousarray(guides12, dtype=np.float32)
+        d = PostDescC()
+        d.width, d.height, d.render_width, d.render_height = int(width), int(height), rw, rh
+        for k in ("hbao", "hbao_plus", "denoise", "taa", "tsaa", "txaa", "bloom", "fxaa", "upscale", "debug_view"):
+            setattr(d, k, int(levels.get(k, 0)))
+        d.hdr = int(levels.get("hdr", 2))
+        d.exposure = float(levels.get("exposure", 0.0))
+        d.gamma = float(levels.get("gamma", 2.2))
+        d.camera = cam.c()
+        out = np.empty((height, width, 3), np.float32)
+        rgba = np.empty((height, width), np.uint32) if want_rgba else None
+        check(lib().bc_post_stack(self._h, C.byref(d), ptr(lin, C.c_float), ptr(g, C.c_float), ptr(out, C.c_float),
+                                  ptr(rgba, C.c_uint32)), self._h)
+        return out, rgba
+
+    def post_history_reset(self):
+        check(lib().bc_post_history_reset(self._h), self._h)
 
     def post_process(self, linear: np.ndarray, guide_nd: np.ndarray | None, settings: RenderSettings,
                      want_rgba: bool = True):

@@ -131,6 +131,7 @@ void bc_destroy(bc_context* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   destroy_render_buffers(ctx);
   destroy_diff_state(ctx);
+  destroy_post_state(ctx);
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_tri, &ctx->d_slot64, &ctx->d_snorm, &ctx->d_slot_prim, &ctx->d_mats,
                     &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ,
                     &ctx->d_kids8, &ctx->d_geom, &ctx->d_build, &ctx->d_build_out})

@@ -79,6 +79,8 @@ struct bc_context {
   bcgx::GeomInfo geom;                    // geometry-only updates (refit.cu)
   bcgx::DevBuf d_kids8, d_geom;           // Node8 -> binary child map; fp64 geometry staging
   bcgx::DevBuf d_build, d_build_out;      // device SAH build (build.cu)
+  bcgx::DevBuf d_post_stack, d_post_hist; // bc_post_stack buffers and temporal history (post.cu)
+  struct PostHistory* post_hist = nullptr;
   std::vector<int8_t> mat_kind;           // host copy of the resident materials' kinds
   std::vector<int8_t> mat_is_light;       // 1: material of a sphere light (its emission feeds NEE records)
   int64_t stats[7] = {0, 0, 0, 0, 0, 0, 0};  // bc_scene_stats; [6] counts geometry-only updates
@@ -108,5 +110,6 @@ bc_status cuda_status(bc_context* ctx, cudaError_t e, const char* what);
 bc_status check_kernel_status(bc_context* ctx);
 void destroy_render_buffers(bc_context* ctx);
 void destroy_diff_state(bc_context* ctx);
+void destroy_post_state(bc_context* ctx);
 bc_status update_geometry(bc_context* ctx, const bc_scene_desc& d);  // refit.cu
 }  // namespace bcgx

@@ -305,6 +305,39 @@ bc_status bc_forward(bc_context* ctx, const float* params, uint64_t seed, float*
 bc_status bc_backward(bc_context* ctx, const float* dloss_dimage, float* grad_albedo, float* grad_emission);
 
 /*
+ * The whole post stack of RenderState.Start (renderer.go:2838-2895) on caller
+ * buffers, in Start's order: HBAO+ (hbao_plus > 0) or HBAO (applyHBAO,
+ * 2433-2488), a-trous denoise (2 + min(3, max(taa, txaa)) passes), temporal
+ * accumulation with the previous call's frame (temporalAccumulate, 2316-2364;
+ * weight from max(taa, tsaa, txaa), 2419-2431; the history is kept by the
+ * context when a temporal mode is on and dropped when none is), bloom, a debug
+ * view (makeDebugView, 1972-2032), the basic upscaler to width x height
+ * (bicubicUpscale + edgeAwareSharpen, 2081-2197; internalSize gives the render
+ * size, 2066-2079), FXAA (2557-2587), the TXAA resolve (2589-2595) and tone
+ * mapping to RGBA8. linear_in: render_width x render_height RGB floats;
+ * guides_in: 12 floats per pixel (P xyz, depth, N xyz, valid 0/1, albedo xyz,
+ * 0), required when HBAO, denoise, a temporal mode or a guide-based debug view
+ * is on. linear_out (width x height RGB floats) and rgba_out may be NULL.
+ */
+typedef struct bc_post_desc {
+  int32_t width, height;                /* output (RenderSettings.Width, Height) */
+  int32_t render_width, render_height;  /* size of linear_in and guides_in */
+  int32_t hbao, hbao_plus;
+  int32_t denoise, taa, tsaa, txaa;
+  int32_t bloom, fxaa;
+  int32_t upscale;     /* 0 off, 1 ultra quality, 2 balanced, 3 performance */
+  int32_t debug_view;  /* 0 beauty, 1 albedo, 2 normal, 3 depth, 4 AO, 5 heat */
+  int32_t hdr, reserved;
+  double exposure, gamma;
+  bc_camera camera;    /* this frame's camera (the next call reprojects into it) */
+} bc_post_desc;
+
+bc_status bc_post_stack(bc_context* ctx, const bc_post_desc* desc, const float* linear_in, const float* guides_in,
+                        float* linear_out, uint32_t* rgba_out);
+/* Drops the temporal history (Start sets historyValid = false, e.g. on a new scene). */
+bc_status bc_post_history_reset(bc_context* ctx);
+
+/*
  * The post stack alone, on caller buffers (the part of RenderState.Start that
  * follows the render call, renderer.go:2844-2854 and 2890-2895): a-trous denoise
  * with `2 + min(3, max(taa, txaa))` passes when settings->denoise, bloom when

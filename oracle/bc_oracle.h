@@ -184,4 +184,20 @@ std::vector<V3> apply_bloom(const std::vector<V3>& img, int w, int h, int level)
 V3 tone_map_hdr(V3 c, int hdr);
 uint32_t to_rgba(V3 c, double exposure, double gamma, int hdr);
 
+// bc_oracle_post.cpp: the rest of RenderState.Start's post stack
+std::vector<V3> apply_hbao(const std::vector<V3>& img, const std::vector<Guide>& g, int w, int h, int level, bool plus);
+bool project_point(const Camera& cam, V3 p, int w, int h, int* ox, int* oy);
+std::vector<V3> temporal_accumulate(const std::vector<V3>& cur, const std::vector<Guide>& g, int w, int h,
+                                    const std::vector<V3>& prev, const std::vector<Guide>& pg, const Camera& prev_cam,
+                                    double weight);
+double temporal_weight(int taa, int tsaa, int txaa);
+std::vector<V3> make_debug_view(const std::vector<V3>& lin, const std::vector<Guide>& g, int w, int h, int mode,
+                                int hbao, int hbao_plus);
+std::vector<V3> bicubic_upscale(const std::vector<V3>& src, int sw, int sh, int dw, int dh);
+std::vector<V3> edge_aware_sharpen(const std::vector<V3>& img, int w, int h, double amount);
+std::vector<V3> upscale_basic(const std::vector<V3>& src, int sw, int sh, int dw, int dh, int mode);
+void internal_size(int width, int height, int mode, int* rw, int* rh);
+std::vector<V3> apply_fxaa(const std::vector<V3>& img, int w, int h, int level);
+std::vector<V3> apply_txaa_resolve(const std::vector<V3>& img, int w, int h, int level);
+
 }  // namespace orc

@@ -360,4 +360,43 @@ void orc_to_rgba(const double* img3, int64_t n, double exposure, double gamma, i
   for (int64_t i = 0; i < n; i++) out[i] = to_rgba(ld3(img3 + 3 * i), exposure, gamma, hdr);
 }
 
+void orc_hbao(const double* img3, const double* guides11, int w, int h, int level, int plus, double* out3) {
+  std::vector<V3> o = apply_hbao(load_img(img3, w * h), load_guides(guides11, w * h), w, h, level, plus != 0);
+  for (int i = 0; i < w * h; i++) st3(out3 + 3 * i, o[i]);
+}
+void orc_temporal(const double* cur3, const double* guides11, int w, int h, const double* prev3,
+                  const double* prev_guides11, const double* cam10, double weight, double* out3) {
+  Camera cam{ld3(cam10), ld3(cam10 + 3), ld3(cam10 + 6), cam10[9]};
+  std::vector<V3> o = temporal_accumulate(load_img(cur3, w * h), load_guides(guides11, w * h), w, h,
+                                          load_img(prev3, w * h), load_guides(prev_guides11, w * h), cam, weight);
+  for (int i = 0; i < w * h; i++) st3(out3 + 3 * i, o[i]);
+}
+double orc_temporal_weight(int taa, int tsaa, int txaa) { return temporal_weight(taa, tsaa, txaa); }
+void orc_debug_view(const double* lin3, const double* guides11, int w, int h, int mode, int hbao, int hbao_plus,
+                    double* out3) {
+  std::vector<V3> o = make_debug_view(load_img(lin3, w * h), load_guides(guides11, w * h), w, h, mode, hbao, hbao_plus);
+  for (int i = 0; i < w * h; i++) st3(out3 + 3 * i, o[i]);
+}
+void orc_upscale(const double* src3, int sw, int sh, int dw, int dh, int mode, double* out3) {
+  std::vector<V3> o = upscale_basic(load_img(src3, sw * sh), sw, sh, dw, dh, mode);
+  for (int i = 0; i < dw * dh; i++) st3(out3 + 3 * i, o[i]);
+}
+void orc_sharpen(const double* img3, int w, int h, double amount, double* out3) {
+  std::vector<V3> o = edge_aware_sharpen(load_img(img3, w * h), w, h, amount);
+  for (int i = 0; i < w * h; i++) st3(out3 + 3 * i, o[i]);
+}
+void orc_fxaa(const double* img3, int w, int h, int level, double* out3) {
+  std::vector<V3> o = apply_fxaa(load_img(img3, w * h), w, h, level);
+  for (int i = 0; i < w * h; i++) st3(out3 + 3 * i, o[i]);
+}
+void orc_txaa(const double* img3, int w, int h, int level, double* out3) {
+  std::vector<V3> o = apply_txaa_resolve(load_img(img3, w * h), w, h, level);
+  for (int i = 0; i < w * h; i++) st3(out3 + 3 * i, o[i]);
+}
+void orc_internal_size(int w, int h, int mode, int* out2) { internal_size(w, h, mode, out2, out2 + 1); }
+int orc_project_point(const double* cam10, const double* p3, int w, int h, int* out2) {
+  Camera cam{ld3(cam10), ld3(cam10 + 3), ld3(cam10 + 6), cam10[9]};
+  return project_point(cam, ld3(p3), w, h, out2, out2 + 1) ? 1 : 0;
+}
+
 }  // extern "C"

@@ -30,6 +30,16 @@ _SIG = [
     ("orc_scene_set_bvh", None, [C.c_void_p, C.c_char_p, C.c_int, C.c_int]),
     ("orc_add_material", C.c_int, [C.c_void_p, C.c_int, f64p, C.c_double, C.c_double, f64p]),
     ("orc_set_material", C.c_int, [C.c_void_p, C.c_int, f64p, f64p]),
+    ("orc_hbao", None, [f64p, f64p, C.c_int, C.c_int, C.c_int, C.c_int, f64p]),
+    ("orc_temporal", None, [f64p, f64p, C.c_int, C.c_int, f64p, f64p, f64p, C.c_double, f64p]),
+    ("orc_temporal_weight", C.c_double, [C.c_int, C.c_int, C.c_int]),
+    ("orc_debug_view", None, [f64p, f64p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, f64p]),
+    ("orc_upscale", None, [f64p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, f64p]),
+    ("orc_sharpen", None, [f64p, C.c_int, C.c_int, C.c_double, f64p]),
+    ("orc_fxaa", None, [f64p, C.c_int, C.c_int, C.c_int, f64p]),
+    ("orc_txaa", None, [f64p, C.c_int, C.c_int, C.c_int, f64p]),
+    ("orc_internal_size", None, [C.c_int, C.c_int, C.c_int, P(C.c_int)]),
+    ("orc_project_point", C.c_int, [f64p, f64p, C.c_int, C.c_int, P(C.c_int)]),
     ("orc_add_sphere", None, [C.c_void_p, f64p, C.c_double, C.c_int]),
     ("orc_add_triangles", None, [C.c_void_p, C.c_int64, f64p, i32p]),
     ("orc_build", None, [C.c_void_p]), ("orc_refit", None, [C.c_void_p]),
@@ -351,3 +361,105 @@ def to_rgba(img, exposure, gamma, hdr):
     out = np.zeros(len(a), np.uint32)
     lib().orc_to_rgba(_p(a, C.c_double), len(a), float(exposure), float(gamma), int(hdr), _p(out, C.c_uint32))
     return out.reshape(np.shape(img)[:-1])
+
+
+# ---- the rest of RenderState.Start's post stack (bc_oracle_post.cpp) ----------------
+def _img_out(h, w):
+    return np.zeros((h, w, 3))
+
+
+def hbao(img, guides11, level, plus):
+    H, W = img.shape[:2]
+    out = _img_out(H, W)
+    lib().orc_hbao(_p(_f64(img), C.c_double), _p(_f64(guides11), C.c_double), W, H, int(level), int(plus),
+                   _p(out, C.c_double))
+    return out
+
+
+def cam10(cam):
+    return _f64(list(cam.position) + list(cam.target) + list(cam.up) + [cam.fov])
+
+
+def temporal(cur, guides11, prev, prev_guides11, prev_cam, weight):
+    H, W = cur.shape[:2]
+    out = _img_out(H, W)
+    lib().orc_temporal(_p(_f64(cur), C.c_double), _p(_f64(guides11), C.c_double), W, H, _p(_f64(prev), C.c_double),
+                       _p(_f64(prev_guides11), C.c_double), _p(cam10(prev_cam), C.c_double), float(weight),
+                       _p(out, C.c_double))
+    return out
+
+
+def temporal_weight(taa, tsaa, txaa):
+    return lib().orc_temporal_weight(int(taa), int(tsaa), int(txaa))
+
+
+def debug_view(lin, guides11, mode, hbao_level=0, hbao_plus=0):
+    H, W = lin.shape[:2]
+    out = _img_out(H, W)
+    lib().orc_debug_view(_p(_f64(lin), C.c_double), _p(_f64(guides11), C.c_double), W, H, int(mode), int(hbao_level),
+                         int(hbao_plus), _p(out, C.c_double))
+    return out
+
+
+def upscale(src, dw, dh, mode):
+    sh, sw = src.shape[:2]
+    out = _img_out(dh, dw)
+    lib().orc_upscale(_p(_f64(src), C.c_double), sw, sh, int(dw), int(dh), int(mode), _p(out, C.c_double))
+    return out
+
+
+def sharpen(img, amount):
+    H, W = img.shape[:2]
+    out = _img_out(H, W)
+    lib().orc_sharpen(_p(_f64(img), C.c_double), W, H, float(amount), _p(out, C.c_double))
+    return out
+
+
+def fxaa(img, level):
+    H, W = img.shape[:2]
+    out = _img_out(H, W)
+    lib().orc_fxaa(_p(_f64(img), C.c_double), W, H, int(level), _p(out, C.c_double))
+    return out
+
+
+def txaa(img, level):
+    H, W = img.shape[:2]
+    out = _img_out(H, W)
+    lib().orc_txaa(_p(_f64(img), C.c_double), W, H, int(level), _p(out, C.c_double))
+    return out
+
+
+def internal_size(w, h, mode):
+    out = (C.c_int * 2)()
+    lib().orc_internal_size(int(w), int(h), int(mode), out)
+    return out[0], out[1]
+
+
+def post_stack(lin, guides11, width, height, history=None, cam=None, **lv):
+    """RenderState.Start's post order (renderer.go:2838-2895) composed from the
+    passes above. history: None or (prev_lin, prev_guides11, prev_cam). Returns
+    (final linear, new history or None)."""
+    g = lambda k: int(lv.get(k, 0))
+    rh, rw = lin.shape[:2]
+    job = _f64(lin)
+    if g("hbao_plus") > 0:
+        job = hbao(job, guides11, g("hbao_plus"), True)
+    elif g("hbao") > 0:
+        job = hbao(job, guides11, g("hbao"), False)
+    if g("denoise"):
+        job = atrous(job, guides11, 2 + min(3, max(g("taa"), g("txaa"))))
+    tw = temporal_weight(g("taa"), g("tsaa"), g("txaa"))
+    if tw > 0 and history is not None and history[0].shape[:2] == (rh, rw):
+        job = temporal(job, guides11, history[0], history[1], history[2], tw)
+    if g("bloom") > 0:
+        job = bloom(job, g("bloom"))
+    job = debug_view(job, guides11, g("debug_view"), g("hbao"), g("hbao_plus"))
+    new_hist = (job.copy(), _f64(guides11).copy(), cam) if tw > 0 else None
+    final = job
+    if g("upscale") != 0 and (rw != width or rh != height):
+        final = upscale(job, width, height, g("upscale"))
+    if g("fxaa") > 0:
+        final = fxaa(final, g("fxaa"))
+    if g("txaa") > 0:
+        final = txaa(final, g("txaa"))
+    return final, new_hist

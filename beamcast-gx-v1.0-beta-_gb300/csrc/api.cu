@@ -134,7 +134,8 @@ void bc_destroy(bc_context* ctx) {
   destroy_post_state(ctx);
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_tri, &ctx->d_slot64, &ctx->d_snorm, &ctx->d_slot_prim, &ctx->d_mats,
                     &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ,
-                    &ctx->d_kids8, &ctx->d_geom, &ctx->d_build, &ctx->d_build_out})
+                    &ctx->d_kids8, &ctx->d_geom, &ctx->d_build, &ctx->d_build_out, &ctx->d_order[0],
+                    &ctx->d_order[1], &ctx->d_order[2]})
     b->release();
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->d_work) cudaFree(ctx->d_work);
@@ -201,6 +202,10 @@ static bc_status install_scene(bc_context* ctx, const PackedScene& ps, const std
   ds.n_prims = ps.n_prims;
   ds.stack_need = ps.stack_need;
   ds.has_spheres = ps.has_spheres;
+  for (int k = 0; k < 3; k++) {
+    ds.lo[k] = ps.scene_lo[k];
+    ds.hi[k] = ps.scene_hi[k];
+  }
   ctx->stats[0] = (int64_t)ps.nodes.size();
   ctx->stats[1] = ps.n_prims;
   ctx->stats[2] = ps.n_binary;
@@ -321,8 +326,14 @@ bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, flo
   if (((uintptr_t)d_rays & 15u) != 0) return set_error(ctx, BC_ERR_INVALID_ARG, "rays must be 16-byte aligned");
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  void* order = nullptr;
+  if (ctx->raycast_sort && n >= kMinOrderedRays) {
+    cudaError_t e = ctx->d_order[2].ensure(ray_order_bytes(n));
+    if (e) return cuda_status(ctx, e, "ray order buffers");
+    order = ctx->d_order[2].p;
+  }
   cudaError_t e = launch_raycast_closest(ctx->ds, (const float4*)d_rays, n, d_t_out, d_prim_out, ctx->d_status,
-                                         ctx->d_work + 2, ctx->raycast_variant, st);
+                                         ctx->d_work + 2, ctx->raycast_variant, order, st);
   return cuda_status(ctx, e, "ray-cast launch");
 }
 
@@ -345,6 +356,12 @@ bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out
   }
   const int64_t chunk = (int64_t)1 << 20;
   cudaStream_t streams[2] = {ctx->stream, ctx->aux_stream};
+  void* order[2] = {nullptr, nullptr};
+  if (ctx->raycast_sort && n >= kMinOrderedRays)
+    for (int k = 0; k < 2; k++) {
+      if ((e = ctx->d_order[k].ensure(ray_order_bytes(std::min(chunk, n))))) return cuda_status(ctx, e, "ray order buffers");
+      order[k] = ctx->d_order[k].p;
+    }
   for (int64_t off = 0, c = 0; off < n && e == cudaSuccess; off += chunk, c++) {
     const int64_t m = std::min(chunk, n - off);
     cudaStream_t st = streams[c & 1];
@@ -352,7 +369,7 @@ bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out
     e = cudaMemcpyAsync(dr, rays + 8 * off, (size_t)m * 32, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
       e = launch_raycast_closest(ctx->ds, dr, m, ctx->d_t.as<float>() + off, ctx->d_prim.as<int32_t>() + off,
-                                 ctx->d_status, ctx->d_work + (c & 1), ctx->raycast_variant, st);
+                                 ctx->d_status, ctx->d_work + (c & 1), ctx->raycast_variant, order[c & 1], st);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(t_out + off, ctx->d_t.as<float>() + off, (size_t)m * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
@@ -410,6 +427,11 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     ctx->raycast_variant = value ? ctx->raycast_minblocks : 0;
     return BC_OK;
   }
+  if (n == "raycast_sort") {
+    if (value != 0 && value != 1) return set_error(ctx, BC_ERR_INVALID_ARG, "raycast_sort must be 0 or 1");
+    ctx->raycast_sort = (int)value;
+    return BC_OK;
+  }
   if (n == "render_wave_cap") {
     if (value < 4096 || value > (1 << 27))
       return set_error(ctx, BC_ERR_INVALID_ARG, "render_wave_cap must be in [4096, 2^27]");
@@ -435,6 +457,7 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
   if (n == "raycast_minblocks") { *value = ctx->raycast_minblocks; return BC_OK; }
   if (n == "raycast_exact") { *value = ctx->raycast_exact; return BC_OK; }
   if (n == "render_wave_cap") { *value = ctx->render_wave_cap; return BC_OK; }
+  if (n == "raycast_sort") { *value = ctx->raycast_sort; return BC_OK; }
   if (n == "render_graph") { *value = ctx->render_graph; return BC_OK; }
   if (n == "render_engine") { *value = ctx->render_engine; return BC_OK; }
   return BC_ERR_INVALID_ARG;

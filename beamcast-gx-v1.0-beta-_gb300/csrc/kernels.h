@@ -19,6 +19,7 @@ struct DeviceScene {
   int32_t n_mats = 0, n_lights = 0, n_prims = 0;
   int32_t stack_need = 0;
   bool has_spheres = false;
+  float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // scene bounds (ray order grid)
 };
 
 // Picks the smallest compiled stack size >= need; 0 if none fits.
@@ -26,9 +27,13 @@ int stack_variant(int need);
 
 // Exact closest hit over n rays (8 floats each); see bc_raycast in bc_gx.h.
 // `work` is an 8-byte device counter private to this launch's stream (persistent kernels).
+// order_scratch (ray_order_bytes(n) bytes, or NULL): rays are traced in a
+// spatially coherent order (batches of at least kMinOrderedRays rays).
+constexpr int64_t kMinOrderedRays = 65536;
+size_t ray_order_bytes(int64_t n);
 cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int64_t n, float* t_out,
                                    int32_t* prim_out, unsigned* status, unsigned long long* work, int variant,
-                                   cudaStream_t st);
+                                   void* order_scratch, cudaStream_t st);
 // Exact any hit.
 cudaError_t launch_raycast_any(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
                                int variant, cudaStream_t st);

@@ -310,6 +310,10 @@ bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::v
     out->depth = std::max(out->depth, ps.depth);
     out->stack_need = std::max(out->stack_need, ps.stack_need);
     out->has_spheres = out->has_spheres || ps.has_spheres;
+    for (int a = 0; a < 3; a++) {  // bounds of the whole set
+      out->scene_lo[a] = k == 0 ? ps.scene_lo[a] : std::min(out->scene_lo[a], ps.scene_lo[a]);
+      out->scene_hi[a] = k == 0 ? ps.scene_hi[a] : std::max(out->scene_hi[a], ps.scene_hi[a]);
+    }
   }
   return BC_OK;
 }

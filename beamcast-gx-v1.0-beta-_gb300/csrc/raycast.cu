@@ -130,7 +130,8 @@ template <int STACK, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_closest_exact_persistent(SceneView sv, const float4* __restrict__ rays,
                                                                         int64_t n, float* __restrict__ t_out,
                                                                         int32_t* __restrict__ prim_out,
-                                                                        unsigned* status, unsigned long long* work) {
+                                                                        unsigned* status, unsigned long long* work,
+                                                                        const int32_t* __restrict__ perm) {
   __shared__ ParkQueue park[4];
   ParkQueue& q = park[threadIdx.x >> 5];
   const unsigned lane = threadIdx.x & 31u;
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(128, MINB) k_closest_exact_persistent(SceneVie
       if (need) {
         const unsigned long long my = base + (unsigned long long)__popc(m & below);
         if (my < (unsigned long long)n) {
-          idx = (long long)my;
+          idx = perm ? (long long)perm[my] : (long long)my;
           const float4 a = __ldg(rays + 2 * idx), b = __ldg(rays + 2 * idx + 1);
           r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
           leaf.reset(b.w);
@@ -199,7 +200,8 @@ template <int STACK>
 __global__ void __launch_bounds__(128) k_closest_fast_persistent(SceneView sv, const float4* __restrict__ rays,
                                                                  int64_t n, float* __restrict__ t_out,
                                                                  int32_t* __restrict__ prim_out, unsigned* status,
-                                                                 unsigned long long* work) {
+                                                                 unsigned long long* work,
+                                                                 const int32_t* __restrict__ perm) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned below = (1u << lane) - 1u;
   long long idx = -1;
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(128) k_closest_fast_persistent(SceneView sv, c
       if (need) {
         const unsigned long long my = base + (unsigned long long)__popc(m & below);
         if (my < (unsigned long long)n) {
-          idx = (long long)my;
+          idx = perm ? (long long)perm[my] : (long long)my;
           const float4 a = __ldg(rays + 2 * idx), b = __ldg(rays + 2 * idx + 1);
           r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
           leaf.reset(b.w);
@@ -237,6 +239,78 @@ __global__ void __launch_bounds__(128) k_closest_fast_persistent(SceneView sv, c
       idx = -1;
     }
   }
+}
+
+// ---- ray order -------------------------------------------------------------------
+// Rays are traced in the order of a 21-bit key: the Morton code of the origin
+// on a 64^3 grid over the scene bounds, then the direction octant, so a warp's
+// rays start near each other and head the same way (fewer divergent node
+// visits, better L1 reuse). A counting sort over the 2^21 keys gives the
+// permutation; rays and results stay in the caller's order.
+constexpr int kKeyBits = 21, kKeyBins = 1 << kKeyBits, kScanBlock = 1024;
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // 6 bits -> every third bit
+  v &= 63u;
+  v = (v | (v << 8)) & 0x0000f00fu;
+  v = (v | (v << 4)) & 0x000c30c3u;
+  v = (v | (v << 2)) & 0x00249249u;
+  return v;
+}
+
+__global__ void k_ray_keys(const float4* __restrict__ rays, int64_t n, float3 lo, float3 scale,
+                           uint32_t* __restrict__ keys, int32_t* __restrict__ bins) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
+  const uint32_t qx = (uint32_t)min(max((a.x - lo.x) * scale.x, 0.0f), 63.0f);
+  const uint32_t qy = (uint32_t)min(max((a.y - lo.y) * scale.y, 0.0f), 63.0f);
+  const uint32_t qz = (uint32_t)min(max((a.z - lo.z) * scale.z, 0.0f), 63.0f);
+  const uint32_t oct = (b.x < 0.0f ? 1u : 0u) | (b.y < 0.0f ? 2u : 0u) | (b.z < 0.0f ? 4u : 0u);
+  const uint32_t key = ((spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2)) << 3) | oct;  // NaN origins -> 0
+  keys[i] = key;
+  atomicAdd(&bins[key], 1);
+}
+
+// exclusive scan of each 1024-bin block in place; block totals out
+__global__ void __launch_bounds__(kScanBlock) k_scan_bins(int32_t* __restrict__ bins, int32_t* __restrict__ totals) {
+  __shared__ int32_t sh[kScanBlock];
+  const int i = blockIdx.x * kScanBlock + threadIdx.x;
+  const int v = bins[i];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = 1; o < kScanBlock; o <<= 1) {
+    const int add = (int)threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += add;
+    __syncthreads();
+  }
+  bins[i] = sh[threadIdx.x] - v;
+  if (threadIdx.x == kScanBlock - 1) totals[blockIdx.x] = sh[threadIdx.x];
+}
+
+// exclusive scan of the block totals (kKeyBins / kScanBlock = 2048 of them), one block
+__global__ void __launch_bounds__(kScanBlock) k_scan_totals(int32_t* __restrict__ totals) {
+  __shared__ int32_t sh[kScanBlock];
+  const int a = totals[2 * threadIdx.x], b = totals[2 * threadIdx.x + 1];
+  sh[threadIdx.x] = a + b;
+  __syncthreads();
+  for (int o = 1; o < kScanBlock; o <<= 1) {
+    const int add = (int)threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += add;
+    __syncthreads();
+  }
+  const int ex = sh[threadIdx.x] - (a + b);
+  totals[2 * threadIdx.x] = ex;
+  totals[2 * threadIdx.x + 1] = ex + a;
+}
+
+__global__ void k_ray_scatter(int64_t n, const uint32_t* __restrict__ keys, int32_t* __restrict__ bins,
+                              const int32_t* __restrict__ totals, int32_t* __restrict__ perm) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = keys[i];
+  perm[totals[k / kScanBlock] + atomicAdd(&bins[k], 1)] = (int32_t)i;
 }
 
 template <class K>
@@ -263,7 +337,7 @@ SceneView view_of(const DeviceScene& s) {
 // 8: <= 64 registers). Selected per context (bc_set_option "raycast_minblocks").
 template <int STACK, int MINB>
 cudaError_t closest_stack(const DeviceScene& s, const float4* rays, int64_t n, float* t, int32_t* p, unsigned* status,
-                          unsigned long long* work, cudaStream_t st) {
+                          unsigned long long* work, const int32_t* perm, cudaStream_t st) {
   const int64_t grid = (n + 127) / 128;
   if (s.has_spheres) {
     k_closest_exact<STACK, true, MINB><<<(unsigned)grid, 128, 0, st>>>(view_of(s), rays, n, t, p, status);
@@ -273,7 +347,7 @@ cudaError_t closest_stack(const DeviceScene& s, const float4* rays, int64_t n, f
     cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
     const int g = (int)std::min<int64_t>(blocks, (n + 127) / 128);
-    k_closest_exact_persistent<STACK, MINB><<<g, 128, 0, st>>>(view_of(s), rays, n, t, p, status, work);
+    k_closest_exact_persistent<STACK, MINB><<<g, 128, 0, st>>>(view_of(s), rays, n, t, p, status, work, perm);
   }
   return cudaGetLastError();
 }
@@ -291,7 +365,7 @@ cudaError_t any_stack(const DeviceScene& s, const float4* rays, int64_t n, uint8
 
 template <int STACK>
 cudaError_t closest_var(const DeviceScene& s, const float4* rays, int64_t n, float* t, int32_t* p, unsigned* status,
-                        unsigned long long* work, int variant, cudaStream_t st) {
+                        unsigned long long* work, int variant, const int32_t* perm, cudaStream_t st) {
   if (variant == 0) {  // fast, not exact
     const int64_t grid = (n + 127) / 128;
     if (s.has_spheres) {
@@ -302,14 +376,14 @@ cudaError_t closest_var(const DeviceScene& s, const float4* rays, int64_t n, flo
       cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), st);
       if (e != cudaSuccess) return e;
       const int g = (int)std::min<int64_t>(blocks, grid);
-      k_closest_fast_persistent<STACK><<<g, 128, 0, st>>>(view_of(s), rays, n, t, p, status, work);
+      k_closest_fast_persistent<STACK><<<g, 128, 0, st>>>(view_of(s), rays, n, t, p, status, work, perm);
     }
     return cudaGetLastError();
   }
   switch (variant) {
-    case 6: return closest_stack<STACK, 6>(s, rays, n, t, p, status, work, st);
-    case 8: return closest_stack<STACK, 8>(s, rays, n, t, p, status, work, st);
-    default: return closest_stack<STACK, 1>(s, rays, n, t, p, status, work, st);
+    case 6: return closest_stack<STACK, 6>(s, rays, n, t, p, status, work, perm, st);
+    case 8: return closest_stack<STACK, 8>(s, rays, n, t, p, status, work, perm, st);
+    default: return closest_stack<STACK, 1>(s, rays, n, t, p, status, work, perm, st);
   }
 }
 
@@ -325,14 +399,38 @@ cudaError_t any_var(const DeviceScene& s, const float4* rays, int64_t n, uint8_t
 
 }  // namespace
 
+size_t ray_order_bytes(int64_t n) {
+  return (size_t)kKeyBins * 4 + (size_t)(kKeyBins / kScanBlock) * 4 + (size_t)n * 8 + 4 * 256;
+}
+
 cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int64_t n, float* t_out,
                                    int32_t* prim_out, unsigned* status, unsigned long long* work, int variant,
-                                   cudaStream_t st) {
+                                   void* order_scratch, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  const int32_t* perm = nullptr;
+  if (order_scratch && n >= kMinOrderedRays && !s.has_spheres) {
+    char* q = (char*)order_scratch;
+    int32_t* bins = (int32_t*)q;
+    int32_t* totals = (int32_t*)(q + (size_t)kKeyBins * 4);
+    uint32_t* keys = (uint32_t*)(q + (size_t)kKeyBins * 4 + ((kKeyBins / kScanBlock) * 4 + 255) / 256 * 256);
+    int32_t* pm = (int32_t*)((char*)keys + ((size_t)n * 4 + 255) / 256 * 256);
+    cudaError_t e = cudaMemsetAsync(bins, 0, (size_t)kKeyBins * 4, st);
+    if (e) return e;
+    const float3 lo = make_float3(s.lo[0], s.lo[1], s.lo[2]);
+    auto sc = [](float a, float b) { return b > a ? 64.0f / (b - a) : 0.0f; };
+    const float3 scale = make_float3(sc(s.lo[0], s.hi[0]), sc(s.lo[1], s.hi[1]), sc(s.lo[2], s.hi[2]));
+    const unsigned g = (unsigned)((n + 255) / 256);
+    k_ray_keys<<<g, 256, 0, st>>>(rays, n, lo, scale, keys, bins);
+    k_scan_bins<<<kKeyBins / kScanBlock, kScanBlock, 0, st>>>(bins, totals);
+    k_scan_totals<<<1, kScanBlock, 0, st>>>(totals);
+    k_ray_scatter<<<g, 256, 0, st>>>(n, keys, bins, totals, pm);
+    if ((e = cudaGetLastError())) return e;
+    perm = pm;
+  }
   switch (stack_variant(s.stack_need)) {
-    case 64: return closest_var<64>(s, rays, n, t_out, prim_out, status, work, variant, st);
-    case 128: return closest_var<128>(s, rays, n, t_out, prim_out, status, work, variant, st);
-    case 256: return closest_var<256>(s, rays, n, t_out, prim_out, status, work, variant, st);
+    case 64: return closest_var<64>(s, rays, n, t_out, prim_out, status, work, variant, perm, st);
+    case 128: return closest_var<128>(s, rays, n, t_out, prim_out, status, work, variant, perm, st);
+    case 256: return closest_var<256>(s, rays, n, t_out, prim_out, status, work, variant, perm, st);
     default: return cudaErrorInvalidValue;
   }
 }

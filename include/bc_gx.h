@@ -379,6 +379,10 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *   "raycast_exact"      1 (default): bc_raycast is exact as documented there;
  *                        0: plain fp32 closest hit, t = the fp32 distance, with no
  *                        exactness contract near edges and ties.
+ *   "raycast_sort"       1 (default): batches of at least 65,536 rays are traced
+ *                        in a spatially coherent order (origin Morton code on a
+ *                        64^3 grid over the scene bounds, then direction octant);
+ *                        results are returned in the caller's order either way.
  *   "render_wave_cap"    paths in flight per wave of the renderer, 4096 .. 2^27
  *                        (default 2^25: ~160 bytes of device memory per path,
  *                        allocated up to what a render needs); images do not

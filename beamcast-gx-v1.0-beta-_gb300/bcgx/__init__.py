@@ -8,11 +8,12 @@ from ._lib import BCError, LIB_PATH, lib
 from .context import Context, gpu_available, persistent_context, render_cuda
 from .scene import (MAT_DIFFUSE, MAT_EMISSIVE, MAT_GLASS, MAT_METAL, PRIM_SPHERE, PRIM_TRIANGLE, Material, Scene,
                     SceneArrays)
-from .settings import Camera, RenderSettings, default_camera, effective_spp, quality, ultra_realism_settings
+from .settings import (INTEGRATOR_PATH, INTEGRATOR_PHOTON, INTEGRATOR_RECURSIVE, Camera, RenderSettings, default_camera,
+                       effective_spp, quality, ultra_realism_settings)
 
 __all__ = [
     "BCError", "LIB_PATH", "lib", "Context", "gpu_available", "persistent_context", "render_cuda",
     "MAT_DIFFUSE", "MAT_EMISSIVE", "MAT_GLASS", "MAT_METAL", "PRIM_SPHERE", "PRIM_TRIANGLE", "Material", "Scene",
     "SceneArrays", "Camera", "RenderSettings", "default_camera", "effective_spp", "quality",
-    "ultra_realism_settings",
+    "ultra_realism_settings", "INTEGRATOR_PATH", "INTEGRATOR_RECURSIVE", "INTEGRATOR_PHOTON",
 ]

@@ -46,6 +46,7 @@ class SettingsC(C.Structure):
         ("adaptive_sampling", C.c_int32), ("adaptive_threshold", C.c_double), ("denoise", C.c_int32),
         ("taa", C.c_int32), ("txaa", C.c_int32), ("bloom", C.c_int32), ("hdr", C.c_int32),
         ("exposure", C.c_double), ("gamma", C.c_double), ("seed", C.c_uint64),
+        ("integrator", C.c_int32), ("photon_mapping", C.c_int32),
     ]
 
 
@@ -88,6 +89,7 @@ SIGNATURES = [
     ("bc_render_frame", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, u32p, u32p, i64p]),
     ("bc_render_moments", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, f32p, i64p]),
     ("bc_render_batch", C.c_int, [C.c_void_p, P(ViewC), C.c_int32, P(f32p), i64p]),
+    ("bc_photon_map", C.c_int, [C.c_void_p, C.c_int32, P(SettingsC), C.c_int32, f32p, P(C.c_int32), i64p]),
     ("bc_diff_configure", C.c_int, [C.c_void_p, P(DiffDescC)]),
     ("bc_diff_set_target", C.c_int, [C.c_void_p, f32p]),
     ("bc_forward", C.c_int, [C.c_void_p, f32p, C.c_uint64, f32p, f64p]),

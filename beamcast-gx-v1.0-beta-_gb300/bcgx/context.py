@@ -171,6 +171,18 @@ class Context:
         check(lib().bc_render_batch(self._h, vc, n, ptrs if readback else None, C.byref(rays)), self._h)
         return outs, rays.value
 
+    def photon_map(self, settings: RenderSettings, scene: int = 0):
+        """buildPhotonMap for (scene, settings): dict(photons (n, 10): position, normal,
+        flux, emission index in append order; rays)."""
+        sc = settings.c()
+        n = C.c_int32(0)
+        rays = C.c_int64(0)
+        check(lib().bc_photon_map(self._h, int(scene), C.byref(sc), 0, None, C.byref(n), C.byref(rays)), self._h)
+        out = np.zeros((max(n.value, 1), 10), dtype=np.float32)
+        check(lib().bc_photon_map(self._h, int(scene), C.byref(sc), n.value, ptr(out, C.c_float), C.byref(n),
+                                  C.byref(rays)), self._h)
+        return {"photons": out[:n.value], "rays": rays.value}
+
     # -- differentiable rendering --
     def diff_configure(self, cam: Camera, settings: RenderSettings, albedo_materials, emission_materials=()):
         """Parameters: albedo RGB of each diffuse material in albedo_materials, then

@@ -15,6 +15,9 @@ from . import _lib
 SAMPLER_RANDOM, SAMPLER_HALTON, SAMPLER_R2 = "Random", "Halton", "R2"
 _SAMPLER_CODE = {SAMPLER_RANDOM: 0, SAMPLER_HALTON: 1, SAMPLER_R2: 2}
 BACKEND_AUTO, BACKEND_CPU, BACKEND_GPU = "Auto", "CPU", "OpenCL GPU"
+# IntegratorMode (renderer.go:1002-1006)
+INTEGRATOR_PATH, INTEGRATOR_RECURSIVE, INTEGRATOR_PHOTON = "Path Tracing", "Recursive Ray Tracing", "Photon Mapping"
+_INTEGRATOR_CODE = {INTEGRATOR_PATH: 0, INTEGRATOR_RECURSIVE: 1, INTEGRATOR_PHOTON: 2}
 
 
 @dataclass
@@ -70,6 +73,8 @@ class RenderSettings:
     bvh_mode: str = "SAH"
     bvh_bins: int = 16
     bvh_leaf_size: int = 4
+    integrator: str = INTEGRATOR_PATH
+    photon_mapping: int = 0
     seed: int = 0x5EED
 
     def c(self) -> _lib.SettingsC:
@@ -85,6 +90,8 @@ class RenderSettings:
         s.bloom, s.hdr = self.bloom, self.hdr
         s.exposure, s.gamma = float(self.exposure), float(self.gamma)
         s.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
+        s.integrator = _INTEGRATOR_CODE[self.integrator]
+        s.photon_mapping = int(self.photon_mapping)
         return s
 
     def copy(self) -> "RenderSettings":
@@ -113,14 +120,17 @@ def quality(name: str) -> RenderSettings:
     elif name == "Balanced":
         b.width, b.height, b.spp, b.bounces, b.denoise, b.quality = 1280, 720, 16, 8, True, name
         b.fxaa, b.taa, b.hbao, b.bloom, b.hdr, b.msaa = 2, 2, 1, 1, 2, 1
+        b.photon_mapping = 1
         b.adaptive_threshold = 0.0008
     elif name == "High":
         b.width, b.height, b.spp, b.bounces, b.denoise, b.quality = 1600, 900, 48, 10, True, name
         b.fxaa, b.taa, b.tsaa, b.hbao_plus, b.bloom, b.hdr, b.msaa = 2, 2, 1, 2, 2, 3, 2
+        b.photon_mapping = 2
         b.adaptive_threshold, b.firefly_clamp = 0.00035, 32
     elif name == "Ultra":
         b.width, b.height, b.spp, b.bounces, b.denoise, b.quality = 1920, 1080, 96, 12, True, name
         b.fxaa, b.taa, b.tsaa, b.txaa, b.hbao_plus, b.bloom, b.hdr, b.msaa = 3, 3, 2, 1, 3, 3, 3, 2
+        b.photon_mapping = 3
         b.adaptive_threshold, b.firefly_clamp = 0.00018, 48
     elif name == "Ultra Realism":
         b.width, b.height, b.spp, b.bounces, b.denoise, b.quality = 2560, 1440, 256, 16, True, name

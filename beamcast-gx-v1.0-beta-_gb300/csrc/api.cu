@@ -132,6 +132,7 @@ void bc_destroy(bc_context* ctx) {
   destroy_render_buffers(ctx);
   destroy_diff_state(ctx);
   destroy_post_state(ctx);
+  destroy_photon_state(ctx);
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_tri, &ctx->d_slot64, &ctx->d_snorm, &ctx->d_slot_prim, &ctx->d_mats,
                     &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ,
                     &ctx->d_kids8, &ctx->d_geom, &ctx->d_build, &ctx->d_build_out, &ctx->d_order[0],
@@ -173,6 +174,7 @@ static bc_status install_scene(bc_context* ctx, const PackedScene& ps, const std
   ctx->has_scene = false;
   ctx->ranges.clear();
   ctx->geom.valid = false;
+  ctx->scene_gen++;
   const size_t slots = (size_t)ps.n_prims;
   bc_status st;
   if ((st = upload(ctx, ctx->d_nodes, ps.nodes.data(), ps.nodes.size() * sizeof(Node8), "BVH8 upload")) ||
@@ -269,6 +271,8 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
     // only the geometry moved: rewrite primitives and node boxes on the device
     st = update_geometry(ctx, *scene);
     if (st == BC_OK) {
+      ctx->ranges[0].diag = scene_diag(*scene);
+      ctx->scene_gen++;  // cached photon maps of the old geometry are stale
       ctx->geom_rev = geometry_rev;
       ctx->stats[6]++;
       return BC_OK;
@@ -282,6 +286,7 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
   SceneRange r;
   r.n_lights = (int32_t)ps.lights.size();
   r.n_slots = ps.n_prims;
+  r.diag = scene_diag(*scene);
   if ((st = install_scene(ctx, ps, std::vector<SceneRange>{r}))) return st;
   if ((st = keep_geometry_map(ctx, *scene, ps))) return st;
   ctx->is_set = false;

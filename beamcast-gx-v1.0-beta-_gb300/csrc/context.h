@@ -99,6 +99,8 @@ struct bc_context {
   int render_graph = 1;                 // replay a captured wave graph (bc_set_option "render_graph")
   int render_engine = 0;                // 0: wave engine, 1: one kernel per view (bc_set_option "render_engine")
   struct DiffState* diff = nullptr;  // differentiable rendering (diff.cu)
+  struct PhotonCache* photons = nullptr;  // photon maps of the photon-mapping integrator (photon.cu)
+  uint64_t scene_gen = 0;                 // bumped by every scene or geometry upload
   // rendering state (render.cu)
   struct RenderBuffers* rb = nullptr;
   std::atomic<int> cancel{0};
@@ -113,5 +115,6 @@ bc_status check_kernel_status(bc_context* ctx);
 void destroy_render_buffers(bc_context* ctx);
 void destroy_diff_state(bc_context* ctx);
 void destroy_post_state(bc_context* ctx);
+void destroy_photon_state(bc_context* ctx);
 bc_status update_geometry(bc_context* ctx, const bc_scene_desc& d);  // refit.cu
 }  // namespace bcgx

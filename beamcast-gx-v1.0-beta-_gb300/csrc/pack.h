@@ -34,6 +34,7 @@ struct SceneRange {
   int32_t slot_off = 0, n_slots = 0;
   int32_t prim_off = 0;                // added to its primitive indices (slot_prim, light prims)
   int32_t mat_off = 0;
+  double diag = 0;                     // length of the scene's bounds diagonal (photon radius)
 };
 
 // Fills `out`; returns BC_OK or BC_ERR_BAD_SCENE / BC_ERR_INVALID_ARG with a message.
@@ -45,6 +46,10 @@ bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::v
                          std::string* err);
 // Sphere-light records and per-primitive light selection pdfs of a scene.
 void pack_scene_lights(const bc_scene_desc& d, PackedScene* out);
+
+// |Scene.Bounds().Max - Min| (renderer.go:1137-1146, 1164-1165): the root node
+// box is the union of the primitive boxes; an empty scene has the unit cube's.
+double scene_diag(const bc_scene_desc& d);
 
 float round_down_f32(double x);
 float round_up_f32(double x);

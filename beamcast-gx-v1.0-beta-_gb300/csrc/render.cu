@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "context.h"
+#include "photon.cuh"
 #include "sampling.cuh"
 #include "trace_core.cuh"
 #include "wave.h"
@@ -69,6 +70,22 @@ struct GradRec {
   int cap;
 };
 
+// Vertex records of the recursive integrator (traceRecursiveInner,
+// renderer.go:1569-1621). The reference samples directLight at a diffuse vertex
+// after tracing the subtree below it, so a path draws all its light samples
+// after its last bounce, deepest vertex first. A diffuse vertex records its
+// point, material, facing normal and the weight its directLight term carries;
+// when the path ends, the records are unwound in that order (each draws its
+// light sample and queues its shadow ray) and overwritten with the sample's
+// contribution and a visibility flag, which the accumulation adds up.
+struct RecurRec {
+  float4* a;    // [bounce * cap + path]: (point, material bits; < 0: no light sample), then (contribution, visible)
+  float4* n;    // (facing normal, 0)
+  float4* w;    // (weight of the vertex's directLight term, 0)
+  int32_t* nb;  // vertices shaded per path
+  int cap;
+};
+
 // Device counters of a wave. cur/next alternate between [0] and [1].
 struct WaveCounters {
   int q[2];
@@ -94,8 +111,9 @@ struct ViewGPU {
   int adaptive;       // adaptivePixel's early stop (renderer.go:1961-1968)
   float adapt_thr;    // max(1e-8, AdaptiveThreshold)
   int min_samples;    // min(8, spp)
-  int pad;
+  int integrator;     // BC_INTEGRATOR_* (pixelRadiance, renderer.go:1833-1842)
   unsigned long long seed;
+  PhotonView pm;      // photon integrator: the frame's photon map (null table: empty map)
 };
 
 // Per-pixel state of the adaptive stop: samples accumulated, luminance sums.
@@ -370,10 +388,87 @@ struct GuideOut {
   long long px;  // frame pixel, < 0: no guide
 };
 
-// One vertex of trace() (renderer.go:1497-1560) for a path whose extension ray
-// hit `slot` at fp32 distance t (slot < 0: miss). Updates s.L / s.tp and, when
-// the path continues, its next ray (store_continuation).
-template <class P>
+// Guide outputs of a first vertex: normal and depth, and the compact guide
+// words (gpu_opencl_windows.go:791-797): Euclidean depth, octahedral normal
+// 10:10, material 11 bits, valid bit, jitter.
+__device__ __forceinline__ void write_guides(const GuideOut& gd, float3 N, float t, float3 d, int m) {
+  gd.nd[gd.px] = make_float4(N.x, N.y, N.z, t);
+  const float dl = sqrtf(dot3(d, d));
+  float3 q = N * (1.0f / (fabsf(N.x) + fabsf(N.y) + fabsf(N.z) + 1e-20f));
+  float px = q.x, py = q.y;
+  if (q.z < 0.0f) {
+    float ax = 1.0f - fabsf(q.y), ay = 1.0f - fabsf(q.x);
+    px = copysignf(ax, q.x);
+    py = copysignf(ay, q.y);
+  }
+  px = fminf(fmaxf(px * 0.5f + 0.5f, 0.0f), 1.0f);
+  py = fminf(fmaxf(py * 0.5f + 0.5f, 0.0f), 1.0f);
+  const uint32_t qx = (uint32_t)rintf(px * 1023.0f), qy = (uint32_t)rintf(py * 1023.0f);
+  const uint32_t mm = (uint32_t)min(max(m, 0), 2047);
+  uint32_t* g = gd.c + 3 * (size_t)gd.px;
+  g[0] = __float_as_uint(t * dl);
+  g[1] = 0x80000000u | (mm << 20) | (qy << 10) | qx;
+  g[2] = gd.jit[gd.px];
+}
+
+// directLight (renderer.go:1427-1465) at a diffuse vertex (p, N) of material
+// M: draws the light sample and returns 0 (no contribution), 1 (contribution
+// that needs no shadow ray: the light point is within 1e-6 of the offset
+// origin, where visible() returns true) or 2 (shadow ray so/sd to trace).
+// `weight` multiplies the contribution.
+__device__ __forceinline__ int sample_direct(const ViewGPU& wp, const ShadeScene& sc, Pcg32& rng, float3 p, float3 N,
+                                             const MatGPU& M, float3 weight, float4* so, float4* sd, float3* contrib) {
+  if (wp.n_lights <= 0) return 0;
+  int li;
+  float sel;
+  if (!wp.power) {  // rng.Intn (in fp64 so the index matches the CPU draw)
+    li = min((int)((double)rng.uniform() * (double)wp.n_lights), wp.n_lights - 1);
+    sel = 1.0f / (float)wp.n_lights;
+  } else {  // sort.Search over LightCDF
+    const double r = (double)rng.uniform();
+    int lo = 0, hi = wp.n_lights;
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      if (!(__ldg(&sc.lights[wp.light_off + mid].cdf) >= r)) lo = mid + 1; else hi = mid;
+    }
+    li = min(lo, wp.n_lights - 1);
+    sel = __ldg(&sc.lights[wp.light_off + li].select_pdf);
+  }
+  const LightGPU Lg = sc.lights[wp.light_off + li];
+  const float3 ln = sel > 0.0f ? rand_unit_vector(rng) : f3(0, 0, 1);
+  const float3 q = f3(Lg.cx, Lg.cy, Lg.cz) + ln * Lg.r;
+  const float3 to = q - p;
+  const float dist2 = dot3(to, to);
+  if (!(dist2 >= 1e-8f && sel > 0.0f)) return 0;
+  const float3 ld = unit3(to);
+  const float ndl = fmaxf(0.0f, dot3(N, ld));
+  const float cosL = fmaxf(0.0f, dot3(ln * -1.0f, ld));
+  if (!(ndl > 0.0f && cosL > 0.0f)) return 0;
+  const float area = 4.0f * kPi * Lg.r * Lg.r;
+  const float lightPDF = sel * dist2 / (cosL * area);
+  if (!(lightPDF > 0.0f)) return 0;
+  const float bsdfPDF = ndl / kPi;
+  const float w = wp.mis ? power_heuristic(lightPDF, bsdfPDF) : 1.0f;
+  const float3 f = f3(M.cr, M.cg, M.cb) * (1.0f / kPi);
+  *contrib = had(weight, had(f, f3(Lg.er, Lg.eg, Lg.eb)) * (ndl * w / lightPDF));
+  const float3 from = p + N * 2e-4f;  // visible (renderer.go:1333-1341)
+  const float3 sdv = q - from;
+  const float sd2 = dot3(sdv, sdv);
+  if (sd2 < 1e-12f) return 1;
+  const float dist = sqrtf(sd2);
+  const float3 dirn = sdv * (1.0f / dist);
+  *so = make_float4(from.x, from.y, from.z, dist - 1e-4f);
+  *sd = make_float4(dirn.x, dirn.y, dirn.z, __int_as_float(wp.root));
+  return 2;
+}
+
+// One vertex of trace() (renderer.go:1497-1560), or of tracePhotonMapped
+// (1763-1831: a photon gather at diffuse vertices, emitters without an MIS
+// weight), for a path whose extension ray hit `slot` at fp32 distance t
+// (slot < 0: miss). Updates s.L / s.tp and, when the path continues, its next
+// ray (store_continuation). ALT: the batch has views of the other integrators
+// (the path-only kernels compile without their code).
+template <bool ALT, class P>
 __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, const ShadeScene& sc, P& s, float t,
                                              int slot, int bounce, const GuideOut& gd, VertexOut& out) {
   out.alive = false;
@@ -394,53 +489,18 @@ __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, cons
       Pcg32 rng = s.rng;
       uint32_t flags = s.flags;
       float ppdf = s.ppdf;
-      const float3 p = o + d * t;
-      const float4 r2 = __ldg(sc.sv.tri + 3 * slot + 2);
-      const bool sphere = r2.w < 0.0f;
-      float3 N;
-      bool front;
-      float radius = 0.0f;
-      if (sphere) {  // sphereHitAccel normal (renderer.go:670-676)
-        const float4 c = __ldg(sc.sv.tri + 3 * slot);
-        radius = c.w;
-        float3 outward = (p - f3(c.x, c.y, c.z)) * (1.0f / c.w);
-        front = dot3(d, outward) < 0.0f;
-        N = front ? outward : outward * -1.0f;
-      } else {
-        N = f3(nrm.x, nrm.y, nrm.z);
-        front = dot3(d, N) < 0.0f;
-        if (!front) N = N * -1.0f;
-      }
+      const Surface S = hit_surface(sc.sv, slot, nrm, o, d, t);
+      const float3 p = S.p, N = S.N;
       const MatGPU M = sc.mats[m];
       const int kind = (int)M.kind;
-      if (gd.px >= 0) {
-        gd.nd[gd.px] = make_float4(N.x, N.y, N.z, t);
-        // compact guide (gpu_opencl_windows.go:791-797): Euclidean depth,
-        // octahedral normal 10:10, material 11 bits, valid bit, jitter
-        const float dl = sqrtf(dot3(d, d));
-        float3 q = N * (1.0f / (fabsf(N.x) + fabsf(N.y) + fabsf(N.z) + 1e-20f));
-        float px = q.x, py = q.y;
-        if (q.z < 0.0f) {
-          float ax = 1.0f - fabsf(q.y), ay = 1.0f - fabsf(q.x);
-          px = copysignf(ax, q.x);
-          py = copysignf(ay, q.y);
-        }
-        px = fminf(fmaxf(px * 0.5f + 0.5f, 0.0f), 1.0f);
-        py = fminf(fmaxf(py * 0.5f + 0.5f, 0.0f), 1.0f);
-        const uint32_t qx = (uint32_t)rintf(px * 1023.0f), qy = (uint32_t)rintf(py * 1023.0f);
-        const uint32_t mm = (uint32_t)min(max(m, 0), 2047);
-        uint32_t* g = gd.c + 3 * (size_t)gd.px;
-        g[0] = __float_as_uint(t * dl);
-        g[1] = 0x80000000u | (mm << 20) | (qy << 10) | qx;
-        g[2] = gd.jit[gd.px];
-      }
+      if (gd.px >= 0) write_guides(gd, N, t, d, m);
       if (kind == BC_MAT_EMISSIVE) {
         float w = 1.0f;
-        if (wp.mis && (flags & 1u)) {  // lightDirectionalPDF is 0 for triangles
+        if ((!ALT || wp.integrator == BC_INTEGRATOR_PATH) && wp.mis && (flags & 1u)) {  // 0 for triangles
           float lpdf = 0.0f;
-          if (sphere) {
+          if (S.sphere) {
             const int prim = __ldg(sc.sv.slot_prim + slot);
-            lpdf = light_dir_pdf(sc, wp.n_lights, wp.power, prim, radius, s.prev(), p, N);
+            lpdf = light_dir_pdf(sc, wp.n_lights, wp.power, prim, S.radius, s.prev(), p, N);
           }
           w = power_heuristic(ppdf, lpdf);
         }
@@ -453,55 +513,14 @@ __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, cons
         if (kind == BC_MAT_DIFFUSE) {
           out.rec_m = m;
           out.rec_v = L;  // everything added from here on carries this albedo once more
-          if (wp.n_lights > 0) {  // directLight (renderer.go:1427-1465)
-            int li;
-            float sel;
-            if (!wp.power) {  // rng.Intn (in fp64 so the index matches the CPU draw)
-              li = min((int)((double)rng.uniform() * (double)wp.n_lights), wp.n_lights - 1);
-              sel = 1.0f / (float)wp.n_lights;
-            } else {  // sort.Search over LightCDF
-              const double r = (double)rng.uniform();
-              int lo = 0, hi = wp.n_lights;
-              while (lo < hi) {
-                int mid = (lo + hi) >> 1;
-                if (!(__ldg(&sc.lights[wp.light_off + mid].cdf) >= r)) lo = mid + 1; else hi = mid;
-              }
-              li = min(lo, wp.n_lights - 1);
-              sel = __ldg(&sc.lights[wp.light_off + li].select_pdf);
-            }
-            const LightGPU Lg = sc.lights[wp.light_off + li];
-            const float3 ln = sel > 0.0f ? rand_unit_vector(rng) : f3(0, 0, 1);
-            const float3 q = f3(Lg.cx, Lg.cy, Lg.cz) + ln * Lg.r;
-            const float3 to = q - p;
-            const float dist2 = dot3(to, to);
-            if (dist2 >= 1e-8f && sel > 0.0f) {
-              const float3 ld = unit3(to);
-              const float ndl = fmaxf(0.0f, dot3(N, ld));
-              const float cosL = fmaxf(0.0f, dot3(ln * -1.0f, ld));
-              if (ndl > 0.0f && cosL > 0.0f) {
-                const float area = 4.0f * kPi * Lg.r * Lg.r;
-                const float lightPDF = sel * dist2 / (cosL * area);
-                if (lightPDF > 0.0f) {
-                  const float bsdfPDF = ndl / kPi;
-                  const float w = wp.mis ? power_heuristic(lightPDF, bsdfPDF) : 1.0f;
-                  const float3 f = f3(M.cr, M.cg, M.cb) * (1.0f / kPi);
-                  const float3 contrib = had(tp, had(f, f3(Lg.er, Lg.eg, Lg.eb)) * (ndl * w / lightPDF));
-                  const float3 from = p + N * 2e-4f;  // visible (renderer.go:1333-1341)
-                  const float3 sdv = q - from;
-                  const float sd2 = dot3(sdv, sdv);
-                  if (sd2 < 1e-12f) {
-                    L = L + contrib;
-                  } else {
-                    const float dist = sqrtf(sd2);
-                    const float3 dirn = sdv * (1.0f / dist);
-                    out.shadow = true;
-                    out.so = make_float4(from.x, from.y, from.z, dist - 1e-4f);
-                    out.sd = make_float4(dirn.x, dirn.y, dirn.z, __int_as_float(wp.root));
-                    out.scon = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
-                  }
-                }
-              }
-            }
+          if (ALT && wp.integrator == BC_INTEGRATOR_PHOTON) L = L + had(tp, photon_gather(wp.pm, p, N));
+          float3 contrib;
+          const int k = sample_direct(wp, sc, rng, p, N, M, tp, &out.so, &out.sd, &contrib);
+          if (k == 1) {
+            L = L + contrib;
+          } else if (k == 2) {
+            out.shadow = true;
+            out.scon = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
           }
           tp = had(tp, f3(M.cr, M.cg, M.cb));
           nd_dir = rand_cos_hemisphere(N, rng);
@@ -522,7 +541,7 @@ __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, cons
         } else {  // glass
           float eta = M.ior;
           if (eta <= 1.0f) eta = 1.5f;
-          const float ratio = front ? 1.0f / eta : eta;
+          const float ratio = S.front ? 1.0f / eta : eta;
           const float3 un = unit3(d);
           const float cosT = fminf(dot3(un * -1.0f, N), 1.0f);
           const float sinT = sqrtf(fmaxf(0.0f, 1.0f - cosT * cosT));
@@ -553,11 +572,131 @@ __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, cons
   s.L = L;
 }
 
+// One vertex of traceRecursiveInner (renderer.go:1569-1621). s.tp is the weight
+// of the vertex's value and s.L gathers the emitted and background radiance.
+// A diffuse vertex is recorded (its light sample comes when the path ends) and
+// the subtree below it weighs weight * color / p while depth < 8
+// (renderer.go:1591-1596). Returns true when the path ends at this vertex;
+// s.rng then holds the stream the unwinding continues.
+template <class P>
+__device__ __forceinline__ bool shade_recursive(const ViewGPU& wp, int n_mats, const ShadeScene& sc, P& s, float t,
+                                                int slot, int bounce, const GuideOut& gd, const RecurRec& rr,
+                                                int path) {
+  s.load_vertex();  // the unwinding needs the stream even after a miss
+  Pcg32 rng = s.rng;
+  const float3 o = s.o, d = s.d;
+  float3 W = s.tp;
+  float3 L = s.L;
+  bool cont = false;
+  float3 nd_dir = d, no = o;
+  float4 rec = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+  const size_t r = (size_t)bounce * rr.cap + path;
+  if (slot < 0) {
+    L = L + had(W, background(d));
+  } else {
+    const float4 nrm = __ldg(sc.sv.snorm + slot);
+    const int m = __float_as_int(nrm.w);
+    if (m >= 0 && m < n_mats) {
+      const Surface S = hit_surface(sc.sv, slot, nrm, o, d, t);
+      const float3 p = S.p, N = S.N;
+      const MatGPU M = sc.mats[m];
+      const int kind = (int)M.kind;
+      const float3 col = f3(M.cr, M.cg, M.cb);
+      if (gd.px >= 0) write_guides(gd, N, t, d, m);
+      if (kind == BC_MAT_EMISSIVE) {
+        L = L + had(W, f3(M.er, M.eg, M.eb));
+      } else if (kind == BC_MAT_DIFFUSE) {
+        const float scale = (wp.bounces - bounce < 8) ? 1.0f / fminf(fmaxf(maxcomp(col), 0.1f), 0.95f) : 1.0f;
+        const float3 Wv = W * scale;
+        rec = make_float4(p.x, p.y, p.z, __int_as_float(m));
+        rr.n[r] = make_float4(N.x, N.y, N.z, 0.0f);
+        rr.w[r] = make_float4(Wv.x, Wv.y, Wv.z, 0.0f);
+        W = had(Wv, col);
+        nd_dir = rand_cos_hemisphere(N, rng);
+        no = p + N * 2e-4f;
+        cont = true;
+      } else if (kind == BC_MAT_METAL) {
+        const float rough = fminf(fmaxf(M.rough, 0.0f), 1.0f);
+        nd_dir = unit3(reflect3(unit3(d), N) + rand_in_unit_sphere(rng) * rough);
+        if (dot3(nd_dir, N) > 0.0f) {
+          W = had(W, col);
+          no = p + N * 2e-4f;
+          cont = true;
+        }
+      } else {  // glass and any other kind
+        float eta = M.ior;
+        if (eta <= 1.0f) eta = 1.5f;
+        const float ratio = S.front ? 1.0f / eta : eta;
+        const float3 un = unit3(d);
+        const float cosT = fminf(dot3(un * -1.0f, N), 1.0f);
+        const float sinT = sqrtf(fmaxf(0.0f, 1.0f - cosT * cosT));
+        if (ratio * sinT > 1.0f || schlick(cosT, ratio) > rng.uniform())
+          nd_dir = reflect3(un, N);
+        else
+          nd_dir = refract3(un, N, ratio);
+        W = had(W, col);
+        no = p + nd_dir * 2e-4f;
+        cont = true;
+      }
+    }
+  }
+  rr.a[r] = rec;
+  s.L = L;
+  s.rng = rng;
+  if (cont && bounce + 1 < wp.bounces) {  // depth - 1 > 0: the subtree is traced
+    s.tp = W;
+    s.store_continuation(no, nd_dir);
+    return false;
+  }
+  return true;
+}
+
+// The end of a recursive path whose last vertex is `last`: the recorded
+// diffuse vertices draw their light samples deepest first, as the reference's
+// recursion returns; each record becomes (contribution, visible) and each
+// shadow ray is queued with its record's bounce + 1 in the contribution's w.
+__device__ __forceinline__ void unwind_recursive(const ViewGPU& wp, const ShadeScene& sc, Pcg32 rng,
+                                                 const RecurRec& rr, int path, int last, ShadowSoA sh,
+                                                 WaveCounters* cnt, long long sh_cap, unsigned* status) {
+  for (int b = last; b >= 0; b--) {
+    const size_t r = (size_t)b * rr.cap + path;
+    const float4 A = rr.a[r];
+    const int m = __float_as_int(A.w);
+    float4 res = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (m >= 0) {
+      const float4 Nn = rr.n[r], Wv = rr.w[r];
+      const MatGPU M = sc.mats[m];
+      float4 so, sd;
+      float3 c;
+      const int k = sample_direct(wp, sc, rng, f3(A.x, A.y, A.z), f3(Nn.x, Nn.y, Nn.z), M, f3(Wv.x, Wv.y, Wv.z),
+                                  &so, &sd, &c);
+      if (k == 1) {
+        res = make_float4(c.x, c.y, c.z, 1.0f);
+      } else if (k == 2) {
+        res = make_float4(c.x, c.y, c.z, 0.0f);
+        const int q = atomicAdd(&cnt->shadow, 1);
+        if (q < sh_cap) {
+          sh.o[q] = so;
+          sh.d[q] = sd;
+          sh.c[q] = make_float4(c.x, c.y, c.z, __int_as_float(b + 1));
+          sh.path[q] = path;
+        } else {
+          atomicOr(status, kStatusCapacity);
+        }
+      }
+    }
+    rr.a[r] = res;
+  }
+  rr.nb[path] = last + 1;
+}
+
+template <bool ALT>
 __global__ void __launch_bounds__(256, 3) k_shade(const ViewGPU* __restrict__ views, int n_mats, ShadeScene sc,
                                                PathSoA ps, const int* __restrict__ qcur, int* __restrict__ qnext,
                                                ShadowSoA sh, WaveCounters* cnt, int cur, int bounce,
                                                float4* __restrict__ guide_nd, uint32_t* __restrict__ guide_c,
-                                               const uint32_t* __restrict__ guide_jit, GradRec rec) {
+                                               const uint32_t* __restrict__ guide_jit, GradRec rec, RecurRec rr,
+                                               long long sh_cap, unsigned* status) {
   const int n = *((volatile int*)&cnt->q[cur]);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     cnt->work_ext = 0;  // the next bounce's extend and this bounce's connect start from zero
@@ -575,7 +714,13 @@ __global__ void __launch_bounds__(256, 3) k_shade(const ViewGPU* __restrict__ vi
       SoAPath s(ps, path);
       GuideOut gd{guide_nd, guide_c, guide_jit, -1};
       if (bounce == 0 && wp.want_guides && ps.samp[path] == 0) gd.px = wp.pix_off + ps.pix[path];
-      shade_vertex(wp, n_mats, sc, s, ps.hit_t[path], ps.hit_slot[path], bounce, gd, out);
+      if (ALT && wp.integrator == BC_INTEGRATOR_RECURSIVE) {
+        const bool ended = shade_recursive(wp, n_mats, sc, s, ps.hit_t[path], ps.hit_slot[path], bounce, gd, rr, path);
+        out.alive = !ended;
+        if (ended) unwind_recursive(wp, sc, s.rng, rr, path, bounce, sh, cnt, sh_cap, status);
+      } else {
+        shade_vertex<ALT>(wp, n_mats, sc, s, ps.hit_t[path], ps.hit_slot[path], bounce, gd, out);
+      }
       ps.lx[path] = s.L.x; ps.ly[path] = s.L.y; ps.lz[path] = s.L.z;
       if (rec.m) {
         const size_t r = (size_t)bounce * rec.cap + path;
@@ -588,10 +733,14 @@ __global__ void __launch_bounds__(256, 3) k_shade(const ViewGPU* __restrict__ vi
     if (out.alive) qnext[qn] = path;
     const int qs = warp_reserve(&cnt->shadow, out.shadow);
     if (out.shadow) {
-      sh.o[qs] = out.so;
-      sh.d[qs] = out.sd;
-      sh.c[qs] = out.scon;
-      sh.path[qs] = path;
+      if (qs < sh_cap) {
+        sh.o[qs] = out.so;
+        sh.d[qs] = out.sd;
+        sh.c[qs] = out.scon;
+        sh.path[qs] = path;
+      } else {
+        atomicOr(status, kStatusCapacity);
+      }
     }
   }
 }
@@ -599,8 +748,9 @@ __global__ void __launch_bounds__(256, 3) k_shade(const ViewGPU* __restrict__ vi
 // ---- connect -----------------------------------------------------------------
 template <int STACK, bool SPH>
 __global__ void __launch_bounds__(128) k_connect(SceneView sv, PathSoA ps, ShadowSoA sh, WaveCounters* cnt,
-                                                 unsigned* status) {
-  const int n = *((volatile int*)&cnt->shadow);
+                                                 RecurRec rr, long long sh_cap, unsigned* status) {
+  // entries past the queue were never written (the shading step flagged them)
+  const int n = (int)min((long long)*((volatile int*)&cnt->shadow), sh_cap);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->shadow_rays, (unsigned long long)n);
   const unsigned lane = threadIdx.x & 31u;
   const unsigned below = (1u << lane) - 1u;
@@ -636,9 +786,14 @@ __global__ void __launch_bounds__(128) k_connect(SceneView sv, PathSoA ps, Shado
       if (!leaf.done) {  // no occluder: the light sample counts
         const int path = sh.path[i];
         const float4 c = sh.c[i];
-        ps.lx[path] += c.x;
-        ps.ly[path] += c.y;
-        ps.lz[path] += c.z;
+        const int tag = __float_as_int(c.w);  // 0, or the recursive record's bounce + 1
+        if (tag == 0) {
+          ps.lx[path] += c.x;
+          ps.ly[path] += c.y;
+          ps.lz[path] += c.z;
+        } else {
+          rr.a[(size_t)(tag - 1) * rr.cap + path].w = 1.0f;
+        }
       }
       i = -1;
     }
@@ -659,7 +814,7 @@ __device__ __forceinline__ float3 clamp_sample(float3 c, float limit) {
 // sample order (path = view.path_off + s * npix + p): no atomics, and the sum
 // does not depend on thread scheduling.
 __global__ void k_accumulate(const BatchState* __restrict__ bs, const ViewGPU* __restrict__ views, PathSoA ps,
-                             float* __restrict__ sum, float* __restrict__ sumsq, AdaptState ad) {
+                             float* __restrict__ sum, float* __restrict__ sumsq, AdaptState ad, RecurRec rr) {
   const long long w0 = bs->w0;
   const long long w1 = min(bs->total, w0 + (long long)bs->cap);
   if (w1 <= w0) return;
@@ -692,7 +847,13 @@ __global__ void k_accumulate(const BatchState* __restrict__ bs, const ViewGPU* _
       bool stop = false;
       for (int s = s_lo; s < s_hi && !stop; s++) {
         const long long i = V.path_off + (long long)s * V.npix + p - w0;
-        const float3 c = clamp_sample(f3(ps.lx[i], ps.ly[i], ps.lz[i]), V.clamp);
+        float3 L = f3(ps.lx[i], ps.ly[i], ps.lz[i]);
+        if (V.integrator == BC_INTEGRATOR_RECURSIVE)  // the visible light samples, deepest vertex first
+          for (int b = rr.nb[i] - 1; b >= 0; b--) {
+            const float4 A = rr.a[(size_t)b * rr.cap + i];
+            if (A.w == 1.0f) L = L + f3(A.x, A.y, A.z);
+          }
+        const float3 c = clamp_sample(L, V.clamp);
         acc = acc + c;
         acc2 = acc2 + had(c, c);
         if (V.adaptive) stop = adaptive_step(V, c, &an, &sl, &ssl);
@@ -810,7 +971,7 @@ __global__ void k_finish_views(const ViewGPU* __restrict__ views, int n_views, c
 // one-view-per-launch form the wave engine is measured against. Shadow rays are
 // traced in place; a lane idles once its path ends until the warp's longest
 // path of that sample is done.
-template <int STACK, bool SPH>
+template <int STACK, bool SPH, bool ALT>
 __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict__ views, int v, int n_mats,
                                                       ShadeScene sc, const double2* __restrict__ seq,
                                                       float* __restrict__ sum, float* __restrict__ sumsq,
@@ -849,7 +1010,7 @@ __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict_
         segs++;
         const GuideOut gd{guide_nd, guide_c, guide_jit, (b == 0 && guide) ? V.pix_off + p : -1};
         VertexOut out;
-        shade_vertex(V, n_mats, sc, st, leaf.best_t, leaf.best_slot, b, gd, out);
+        shade_vertex<ALT>(V, n_mats, sc, st, leaf.best_t, leaf.best_slot, b, gd, out);
         if (out.shadow) {
           shadows++;
           const Ray32 sr = make_ray(out.so.x, out.so.y, out.so.z, out.sd.x, out.sd.y, out.sd.z, 1e-4f);
@@ -905,6 +1066,7 @@ T* carve(char*& p, size_t n) {
 
 struct RenderBuffers {
   int cap = 0;          // path slots
+  long long sh_cap = 0; // shadow queue entries
   size_t frame_px = 0;  // pixels of the frame buffers
   bcgx::DevBuf paths, shadow, queues, counters, seq, frame, table;
   bcgx::HostBuf staging;
@@ -930,6 +1092,10 @@ struct RenderBuffers {
   bcgx::DevBuf rec;
   bcgx::GradRec grec{};
   int rec_bounces = 0, rec_cap = 0;
+  // vertex records of the recursive integrator
+  bcgx::DevBuf rrec;
+  bcgx::RecurRec rr{};
+  int rr_bounces = 0, rr_cap = 0;
   // one wave as an instantiated CUDA graph, and the launch arguments it was captured with
   cudaGraphExec_t graph = nullptr;
   std::vector<uintptr_t> graph_key;
@@ -950,42 +1116,54 @@ void destroy_render_buffers(bc_context* ctx) {
   rb->table.release();
   rb->staging.release();
   rb->rec.release();
+  rb->rrec.release();
   delete rb;
   ctx->rb = nullptr;
 }
 
-static bc_status ensure_paths(bc_context* ctx, int cap) {
+// Path slots, queues and a shadow queue of sh_cap entries (one per path and
+// bounce for the one-shadow-ray integrators; a recursive path can queue one per
+// recorded vertex when it ends).
+static bc_status ensure_paths(bc_context* ctx, int cap, long long sh_cap) {
   RenderBuffers* rb = ctx->rb;
-  if (rb->cap >= cap) return BC_OK;
-  size_t per = 16 * sizeof(float) + 2 * sizeof(uint64_t) + sizeof(uint32_t) + sizeof(float) + 4 * sizeof(int32_t);
-  cudaError_t e = rb->paths.ensure((size_t)cap * per + 64 * 256);
-  if (e == cudaSuccess) e = rb->shadow.ensure((size_t)cap * (3 * sizeof(float4) + sizeof(int32_t)) + 8 * 256);
-  if (e == cudaSuccess) e = rb->queues.ensure((size_t)cap * 2 * sizeof(int) + 4 * 256);
-  if (e != cudaSuccess) {
-    rb->cap = 0;
-    return cuda_status(ctx, e, "path buffers");
+  if (rb->cap < cap) {
+    size_t per = 16 * sizeof(float) + 2 * sizeof(uint64_t) + sizeof(uint32_t) + sizeof(float) + 4 * sizeof(int32_t);
+    cudaError_t e = rb->paths.ensure((size_t)cap * per + 64 * 256);
+    if (e == cudaSuccess) e = rb->queues.ensure((size_t)cap * 2 * sizeof(int) + 4 * 256);
+    if (e != cudaSuccess) {
+      rb->cap = 0;
+      return cuda_status(ctx, e, "path buffers");
+    }
+    char* p = (char*)rb->paths.p;
+    PathSoA& s = rb->ps;
+    float** fl[] = {&s.ox, &s.oy, &s.oz, &s.dx, &s.dy, &s.dz, &s.tx, &s.ty, &s.tz, &s.lx, &s.ly, &s.lz, &s.px, &s.py, &s.pz, &s.ppdf};
+    for (float** f : fl) *f = carve<float>(p, cap);
+    s.rs = carve<uint64_t>(p, cap);
+    s.ri = carve<uint64_t>(p, cap);
+    s.flags = carve<uint32_t>(p, cap);
+    s.hit_t = carve<float>(p, cap);
+    s.hit_slot = carve<int32_t>(p, cap);
+    s.view = carve<int32_t>(p, cap);
+    s.pix = carve<int32_t>(p, cap);
+    s.samp = carve<int32_t>(p, cap);
+    char* qq = (char*)rb->queues.p;
+    rb->q[0] = carve<int>(qq, cap);
+    rb->q[1] = carve<int>(qq, cap);
+    rb->cap = cap;
   }
-  char* p = (char*)rb->paths.p;
-  PathSoA& s = rb->ps;
-  float** fl[] = {&s.ox, &s.oy, &s.oz, &s.dx, &s.dy, &s.dz, &s.tx, &s.ty, &s.tz, &s.lx, &s.ly, &s.lz, &s.px, &s.py, &s.pz, &s.ppdf};
-  for (float** f : fl) *f = carve<float>(p, cap);
-  s.rs = carve<uint64_t>(p, cap);
-  s.ri = carve<uint64_t>(p, cap);
-  s.flags = carve<uint32_t>(p, cap);
-  s.hit_t = carve<float>(p, cap);
-  s.hit_slot = carve<int32_t>(p, cap);
-  s.view = carve<int32_t>(p, cap);
-  s.pix = carve<int32_t>(p, cap);
-  s.samp = carve<int32_t>(p, cap);
-  char* q = (char*)rb->shadow.p;
-  rb->sh.o = carve<float4>(q, cap);
-  rb->sh.d = carve<float4>(q, cap);
-  rb->sh.c = carve<float4>(q, cap);
-  rb->sh.path = carve<int32_t>(q, cap);
-  char* qq = (char*)rb->queues.p;
-  rb->q[0] = carve<int>(qq, cap);
-  rb->q[1] = carve<int>(qq, cap);
-  rb->cap = cap;
+  if (rb->sh_cap < sh_cap) {
+    cudaError_t e = rb->shadow.ensure((size_t)sh_cap * (3 * sizeof(float4) + sizeof(int32_t)) + 8 * 256);
+    if (e != cudaSuccess) {
+      rb->sh_cap = 0;
+      return cuda_status(ctx, e, "shadow queue");
+    }
+    char* q = (char*)rb->shadow.p;
+    rb->sh.o = carve<float4>(q, sh_cap);
+    rb->sh.d = carve<float4>(q, sh_cap);
+    rb->sh.c = carve<float4>(q, sh_cap);
+    rb->sh.path = carve<int32_t>(q, sh_cap);
+    rb->sh_cap = sh_cap;
+  }
   return BC_OK;
 }
 
@@ -1109,6 +1287,8 @@ struct WaveShape {
   int bounces;
   bool lights;
   const GradArgs* grad;  // non-null: gradient render
+  bool recursive;        // the batch has views of the recursive integrator
+  bool alt;              // the batch has views of the recursive or photon integrator
 };
 
 template <int STACK, bool SPH>
@@ -1125,6 +1305,8 @@ static WaveShape wave_shape(int cap, int bounces, bool lights, const GradArgs* g
   w.bounces = bounces;
   w.lights = lights;
   w.grad = grad;
+  w.recursive = false;
+  w.alt = false;
   return w;
 }
 
@@ -1133,6 +1315,7 @@ template <int STACK, bool SPH>
 static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const ShadeScene& sc, cudaStream_t st) {
   RenderBuffers* rb = ctx->rb;
   WaveCounters* c = rb->cnt;
+  const RecurRec rr = w.recursive ? rb->rr : RecurRec{nullptr, nullptr, nullptr, nullptr, 0};
   k_generate<<<w.gen_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->q[0], rb->seq_xy, rb->guide_jit, c,
                                          rb->adapt);
   int cur = 0;
@@ -1142,16 +1325,23 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
   for (int b = 0; b < w.bounces; b++) {
     k_extend<STACK, SPH><<<w.ext_grid, 128, 0, st>>>(sc.sv, rb->views, rb->ps, rb->q[cur], c, cur, ctx->d_status);
     const GradRec rec = w.grad ? rb->grec : GradRec{nullptr, nullptr, nullptr, 0};
-    k_shade<<<w.shade_grid, 256, 0, st>>>(rb->views, ctx->ds.n_mats, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1], rb->sh,
-                                          c, cur, b, rb->guide_nd, rb->guide_c, rb->guide_jit, rec);
-    if (w.lights) k_connect<STACK, SPH><<<w.con_grid, 128, 0, st>>>(sc.sv, rb->ps, rb->sh, c, ctx->d_status);
+    if (w.alt)
+      k_shade<true><<<w.shade_grid, 256, 0, st>>>(rb->views, ctx->ds.n_mats, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1],
+                                                  rb->sh, c, cur, b, rb->guide_nd, rb->guide_c, rb->guide_jit, rec,
+                                                  rr, rb->sh_cap, ctx->d_status);
+    else
+      k_shade<false><<<w.shade_grid, 256, 0, st>>>(rb->views, ctx->ds.n_mats, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1],
+                                                   rb->sh, c, cur, b, rb->guide_nd, rb->guide_c, rb->guide_jit, rec,
+                                                   rr, rb->sh_cap, ctx->d_status);
+    if (w.lights)
+      k_connect<STACK, SPH><<<w.con_grid, 128, 0, st>>>(sc.sv, rb->ps, rb->sh, c, rr, rb->sh_cap, ctx->d_status);
     cur ^= 1;
   }
   if (w.grad)
     k_gradient<<<gradient_grid(), 256, 3 * w.grad->n_params * sizeof(double), st>>>(rb->bs, rb->views, rb->ps,
                                                                                   rb->grec, *w.grad, sc.mats);
   k_accumulate<<<w.acc_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr,
-                                           rb->adapt);
+                                           rb->adapt, rr);
   k_advance<<<1, 32, 0, st>>>(rb->bs, c);
   return cudaGetLastError();
 }
@@ -1159,10 +1349,12 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
 // Runs `n_waves` waves, through one captured CUDA graph when the option allows.
 template <int STACK, bool SPH>
 static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const ShadeScene& sc, int64_t n_waves,
-                           const GradArgs* grad) {
+                           const GradArgs* grad, bool recursive, bool alt) {
   RenderBuffers* rb = ctx->rb;
   cudaStream_t st = ctx->stream;
-  const WaveShape w = wave_shape<STACK, SPH>(rb->cap, bounces, lights, grad);
+  WaveShape w = wave_shape<STACK, SPH>(rb->cap, bounces, lights, grad);
+  w.recursive = recursive;
+  w.alt = alt;
   const bool use_graph = ctx->render_graph != 0 && n_waves > 1;
   if (use_graph) {
     // every value the captured launches were given
@@ -1180,6 +1372,10 @@ static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const Shad
     };
     add_bytes(&rb->ps, sizeof(rb->ps));
     add_bytes(&rb->sh, sizeof(rb->sh));
+    key.push_back((uintptr_t)rb->sh_cap);
+    key.push_back((uintptr_t)recursive);
+    key.push_back((uintptr_t)alt);
+    if (recursive) add_bytes(&rb->rr, sizeof(rb->rr));
     add_bytes(&sc, sizeof(sc));
     key.push_back((uintptr_t)(grad != nullptr));
     if (grad) {
@@ -1224,6 +1420,10 @@ static bc_status check_view(bc_context* ctx, const ViewRequest& r) {
     return set_error(ctx, BC_ERR_INVALID_ARG, "invalid render size, rows, spp or bounces");
   if ((int64_t)s.width * s.height > (1 << 26)) return set_error(ctx, BC_ERR_INVALID_ARG, "frame too large");
   if (s.bounces > kMaxBounces) return set_error(ctx, BC_ERR_INVALID_ARG, "bounces above 1024");
+  if (s.integrator < BC_INTEGRATOR_PATH || s.integrator > BC_INTEGRATOR_PHOTON)
+    return set_error(ctx, BC_ERR_INVALID_ARG, "unknown integrator");
+  if (s.integrator == BC_INTEGRATOR_RECURSIVE && ctx->render_engine == 1)
+    return set_error(ctx, BC_ERR_INVALID_ARG, "the one-kernel form renders the path and photon integrators");
   return BC_OK;
 }
 
@@ -1231,7 +1431,7 @@ static bc_status check_view(bc_context* ctx, const ViewRequest& r) {
 // frame buffers are kept. Leaves the per-view table in rb->views.
 // The one-kernel form: one launch per view.
 template <int STACK, bool SPH>
-static bc_status run_plain(bc_context* ctx, const ShadeScene& sc, const std::vector<ViewGPU>& views) {
+static bc_status run_plain(bc_context* ctx, const ShadeScene& sc, const std::vector<ViewGPU>& views, bool alt) {
   RenderBuffers* rb = ctx->rb;
   for (int v = 0; v < (int)views.size(); v++) {
     if (*(volatile int*)ctx->h_cancel || ctx->cancel.load()) {
@@ -1239,9 +1439,14 @@ static bc_status run_plain(bc_context* ctx, const ShadeScene& sc, const std::vec
       return set_error(ctx, BC_ERR_CANCELLED, "render cancelled");
     }
     const int grid = (views[v].npix + 127) / 128;
-    k_render_plain<STACK, SPH><<<grid, 128, 0, ctx->stream>>>(
-        rb->views, v, ctx->ds.n_mats, sc, rb->seq_xy, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr, rb->guide_nd,
-        rb->guide_c, rb->guide_jit, rb->cnt, ctx->d_status, rb->adapt);
+    if (alt)
+      k_render_plain<STACK, SPH, true><<<grid, 128, 0, ctx->stream>>>(
+          rb->views, v, ctx->ds.n_mats, sc, rb->seq_xy, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr, rb->guide_nd,
+          rb->guide_c, rb->guide_jit, rb->cnt, ctx->d_status, rb->adapt);
+    else
+      k_render_plain<STACK, SPH, false><<<grid, 128, 0, ctx->stream>>>(
+          rb->views, v, ctx->ds.n_mats, sc, rb->seq_xy, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr, rb->guide_nd,
+          rb->guide_c, rb->guide_jit, rb->cnt, ctx->d_status, rb->adapt);
     cudaError_t e = cudaGetLastError();
     if (e) return cuda_status(ctx, e, "one-kernel render launch");
   }
@@ -1253,16 +1458,21 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
   if (req.empty()) return set_error(ctx, BC_ERR_INVALID_ARG, "no views");
   bc_status bst;
-  for (const ViewRequest& r : req)
+  for (const ViewRequest& r : req) {
     if ((bst = check_view(ctx, r))) return bst;
+    if (grad && r.s.integrator != BC_INTEGRATOR_PATH)
+      return set_error(ctx, BC_ERR_INVALID_ARG, "gradient renders use the path integrator");
+  }
   if (!ctx->rb) ctx->rb = new RenderBuffers();
   RenderBuffers* rb = ctx->rb;
   const int n = (int)req.size();
   std::vector<ViewGPU> views(n);
   std::vector<double> X, Y;
   long long total = 0;
-  int max_bounces = 0;
-  bool lights = false;
+  int max_bounces = 0, rec_bounces = 0;
+  bool lights = false, alt = false;
+  std::vector<const unsigned long long*> photon_rays;  // ray counters of photon maps built for this call
+  const uint64_t photon_pin = photon_clock(ctx);
   for (int v = 0; v < n; v++) {
     const ViewRequest& r = req[v];
     const SceneRange& sr = ctx->ranges[r.scene];
@@ -1292,6 +1502,14 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
     V.adapt_thr = (float)std::max(1e-8, r.s.adaptive_threshold);
     V.min_samples = std::min(8, V.spp);
     V.seed = r.s.seed;
+    V.integrator = r.s.integrator;
+    alt = alt || V.integrator != BC_INTEGRATOR_PATH;
+    if (V.integrator == BC_INTEGRATOR_RECURSIVE) rec_bounces = std::max(rec_bounces, V.bounces);
+    if (V.integrator == BC_INTEGRATOR_PHOTON) {  // built once per frame (renderer.go:2728-2734), then cached
+      const unsigned long long* built = nullptr;
+      if ((bst = photon_map_for(ctx, r.scene, r.s, photon_pin, &V.pm, &built))) return bst;
+      if (built) photon_rays.push_back(built);
+    }
     camera_basis(r.cam, (double)V.W / (double)V.H, V.origin, V.lower, V.horiz, V.vert);
     V.path_off = total;
     total += (long long)V.npix * V.spp;
@@ -1301,9 +1519,28 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
   long long cap_limit = ctx->render_wave_cap;
   if (grad)  // path replay records cost 20 bytes per path and bounce: keep them under 8 GB
     cap_limit = std::min<long long>(cap_limit, std::max<long long>(4096, (8LL << 30) / (20LL * max_bounces)));
+  if (rec_bounces)  // a recursive path queues up to one shadow ray per vertex when it ends
+    cap_limit = std::max<long long>(4096, cap_limit / rec_bounces);
   const int cap = (int)std::max<long long>(1, std::min<long long>(total, cap_limit));
-  if ((bst = ensure_paths(ctx, cap))) return bst;
+  const long long sh_cap = (long long)cap * std::max(1, rec_bounces);
+  if ((bst = ensure_paths(ctx, cap, sh_cap))) return bst;
   if ((bst = ensure_frame(ctx, frame_px))) return bst;
+  if (rec_bounces && (rb->rr_bounces < rec_bounces || rb->rr_cap < cap)) {  // stride: this render's wave size
+    const size_t nrec = (size_t)rec_bounces * cap;
+    cudaError_t e = rb->rrec.ensure(nrec * 3 * sizeof(float4) + (size_t)cap * sizeof(int32_t) + 8 * 256);
+    if (e) {
+      rb->rr_bounces = rb->rr_cap = 0;
+      return cuda_status(ctx, e, "recursive vertex records");
+    }
+    char* p = (char*)rb->rrec.p;
+    rb->rr.a = carve<float4>(p, nrec);
+    rb->rr.n = carve<float4>(p, nrec);
+    rb->rr.w = carve<float4>(p, nrec);
+    rb->rr.nb = carve<int32_t>(p, cap);
+    rb->rr.cap = cap;
+    rb->rr_bounces = rec_bounces;
+    rb->rr_cap = cap;
+  }
   if (grad) {  // path replay records: one per path and bounce
     if (max_bounces > kMaxGradBounces) return set_error(ctx, BC_ERR_INVALID_ARG, "gradient renders allow 64 bounces");
     // stride: this render's wave size (path slots >= cap are never used by it)
@@ -1383,27 +1620,31 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
   const int stack = stack_variant(ctx->ds.stack_need);
   const bool sph = ctx->ds.has_spheres;
   if (ctx->render_engine == 1 && !grad) {
-    if (stack == 64) bst = sph ? run_plain<64, true>(ctx, sc, views) : run_plain<64, false>(ctx, sc, views);
-    else if (stack == 128) bst = sph ? run_plain<128, true>(ctx, sc, views) : run_plain<128, false>(ctx, sc, views);
-    else bst = sph ? run_plain<256, true>(ctx, sc, views) : run_plain<256, false>(ctx, sc, views);
+    if (stack == 64) bst = sph ? run_plain<64, true>(ctx, sc, views, alt) : run_plain<64, false>(ctx, sc, views, alt);
+    else if (stack == 128) bst = sph ? run_plain<128, true>(ctx, sc, views, alt) : run_plain<128, false>(ctx, sc, views, alt);
+    else bst = sph ? run_plain<256, true>(ctx, sc, views, alt) : run_plain<256, false>(ctx, sc, views, alt);
   } else if (stack == 64)
-    bst = sph ? run_waves<64, true>(ctx, max_bounces, lights, sc, n_waves, grad)
-              : run_waves<64, false>(ctx, max_bounces, lights, sc, n_waves, grad);
+    bst = sph ? run_waves<64, true>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt)
+              : run_waves<64, false>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt);
   else if (stack == 128)
-    bst = sph ? run_waves<128, true>(ctx, max_bounces, lights, sc, n_waves, grad)
-              : run_waves<128, false>(ctx, max_bounces, lights, sc, n_waves, grad);
+    bst = sph ? run_waves<128, true>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt)
+              : run_waves<128, false>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt);
   else
-    bst = sph ? run_waves<256, true>(ctx, max_bounces, lights, sc, n_waves, grad)
-              : run_waves<256, false>(ctx, max_bounces, lights, sc, n_waves, grad);
+    bst = sph ? run_waves<256, true>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt)
+              : run_waves<256, false>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt);
   if (bst) return bst;
   k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sum, rb->out, rb->adapt.n);
   if (rb->want_sumsq)
     k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sumsq, rb->post_tmp, rb->adapt.n);
   e = cudaGetLastError();
   unsigned long long r = 0;
+  std::vector<unsigned long long> pr(photon_rays.size(), 0);
   if (!e) e = cudaMemcpyAsync(&r, &rb->cnt->rays, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream);
+  for (size_t k = 0; k < photon_rays.size() && !e; k++)
+    e = cudaMemcpyAsync(&pr[k], photon_rays[k], sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
   if (!e) e = cudaStreamSynchronize(ctx->stream);
   if (e) return cuda_status(ctx, e, "render");
+  for (unsigned long long v : pr) r += v;  // Start counts the photon map's rays (renderer.go:2809)
   if (rays) *rays = (int64_t)r;
   return check_kernel_status(ctx);
 }

@@ -32,6 +32,15 @@ struct GradArgs {
 bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, size_t frame_px, int64_t* rays,
                        const GradArgs* grad);
 float* render_mean(bc_context* ctx);
+
+// Photon maps (photon.cu). photon_map_for returns the map of resident scene
+// `scene` for the seed, PhotonMapping level and bounces of `s`, from the cache
+// or built on the context's stream (then *built_rays is its device ray
+// counter); maps used after photon_clock() returned `pin` are not evicted.
+struct PhotonView;
+uint64_t photon_clock(bc_context* ctx);
+bc_status photon_map_for(bc_context* ctx, int scene, const bc_settings& s, uint64_t pin, PhotonView* view,
+                         const unsigned long long** built_rays);
 int gradient_grid();
 int effective_spp(const bc_settings& s);
 

@@ -93,9 +93,13 @@ typedef struct bc_camera {
   double fov_deg;
 } bc_camera;
 
+/* IntegratorMode (renderer.go:1002-1006); pixelRadiance (1833-1842) dispatches on it. */
+#define BC_INTEGRATOR_PATH 0      /* trace (1484-1563) */
+#define BC_INTEGRATOR_RECURSIVE 1 /* traceRecursive (1565-1621) */
+#define BC_INTEGRATOR_PHOTON 2    /* tracePhotonMapped (1763-1831) over buildPhotonMap (1642-1728) */
+
 /*
  * The subset of RenderSettings (renderer.go:1027-1062) that the hot path reads.
- * Path integrator only (IntegratorPath).
  */
 typedef struct bc_settings {
   int32_t width, height, spp, bounces;
@@ -110,6 +114,8 @@ typedef struct bc_settings {
   int32_t bloom, hdr;             /* bloom level, tone-map curve (renderer.go:2034-2053) */
   double exposure, gamma;
   uint64_t seed;                  /* path RNG seed: equal seeds give equal images */
+  int32_t integrator;             /* BC_INTEGRATOR_* */
+  int32_t photon_mapping;         /* PhotonMapping level 1-4 (budget 512..16384 photons); others: no photons */
 } bc_settings;
 
 /* ---- context ------------------------------------------------------------ */
@@ -208,7 +214,15 @@ bc_status bc_occluded_device(bc_context* ctx, const float* d_rays, int64_t n, ui
  * compact guide encoding (gpu_opencl_windows.go:519-521, 791-797): depth float
  * bits; valid<<31 | material<<20 | octN.y<<10 | octN.x; jitter v<<16 | u.
  * rays_out (may be NULL) receives the number of extension rays traced (the
- * reference's Rays, renderer.go:1491).
+ * reference's Rays, renderer.go:1491), plus the photon map's rays in the call
+ * that builds it (renderer.go:2809).
+ *
+ * settings->integrator picks pixelRadiance's integrator (renderer.go:1833-1842).
+ * The photon integrator builds its photon map (buildPhotonMap) once per scene,
+ * seed, PhotonMapping level and bounce count and keeps it for the next chunks
+ * and frames; emission k of the map draws from its own stream keyed by
+ * (seed, k). The recursive integrator runs in the wave engine only
+ * (render_engine 1 rejects it).
  */
 bc_status bc_render_rows(bc_context* ctx, const bc_camera* cam, const bc_settings* settings, int32_t y0,
                          int32_t rows, float* linear_out, uint32_t* guide_out, int64_t* rays_out);
@@ -257,6 +271,19 @@ typedef struct bc_view {
  */
 bc_status bc_render_batch(bc_context* ctx, const bc_view* views, int32_t n_views, float* const* linear_out,
                           int64_t* rays_out);
+
+/*
+ * The photon map of the photon integrator (buildPhotonMap, renderer.go:1642-1728)
+ * for scene `scene` of the resident set (0 after bc_scene_upload) and the seed,
+ * bounces and photon_mapping level of *settings: the same map the renders use.
+ * photons_out receives min(n, capacity) photons of 10 floats (position,
+ * normal, flux, emission index) in the reference's append order; *n_out the
+ * photon count n (0 without sphere lights or for levels outside 1-4);
+ * *rays_out the rays traced by the emissions that ran. Outputs may be NULL
+ * when capacity is 0.
+ */
+bc_status bc_photon_map(bc_context* ctx, int32_t scene, const bc_settings* settings, int32_t capacity,
+                        float* photons_out, int32_t* n_out, int64_t* rays_out);
 
 /* ---- differentiable rendering ------------------------------------------ */
 

@@ -17,6 +17,7 @@
 #include <vector>
 #include <string>
 #include <atomic>
+#include <unordered_map>
 
 namespace orc {
 
@@ -131,7 +132,11 @@ struct Settings {
   int taa = 0, txaa = 0, bloom = 0, hdr = 2;
   double exposure = 0, gamma = 2.2;
   int tile = 8;
+  int integrator = 0;      // IntegratorMode (renderer.go:1002-1006): 0 path, 1 recursive, 2 photon
+  int photon_mapping = 0;  // RenderSettings.PhotonMapping level (photon budget and radius)
+  int64_t photon_seed = -1;  // seed of the photon map's emission streams; < 0: the render seed
 };
+enum Integrator { IntegratorPath = 0, IntegratorRecursive = 1, IntegratorPhoton = 2 };
 int effective_spp(const Settings& s);  // renderer.go:2395
 
 // PCG32 stream; the GPU kernels draw from the same generator so that a
@@ -165,12 +170,40 @@ struct Guide { V3 p{0, 0, 0}, n{0, 0, 0}, albedo{0, 0, 0}; double depth = 0; boo
 struct TraceStats { int64_t segments = 0, shadow = 0; Counters c; };
 
 V3 trace(const Scene& s, Ray ray, const Settings& st, Rng& rng, TraceStats* stats, Guide* guide);
+V3 direct_light(const Scene& s, const Hit& h, V3 hitP, const Material& mat, Rng& rng, const Settings& st,
+                TraceStats* stats);
+V3 material_preview_color(const Material& m);
+
+// bc_oracle_integrators.cpp: the recursive and photon-mapping integrators
+// (renderer.go:1565-1831). Photon emission k draws from its own stream,
+// make_path_rng(seed, k, kPhotonStream), where the reference draws every
+// emission from one time-seeded generator (renderer.go:1651).
+constexpr uint64_t kPhotonStream = 0xFFFFFFFFull;
+struct Photon { V3 p, n, flux; int emission = 0; };
+struct PhotonMap {
+  std::vector<Photon> photons;                          // append order
+  std::unordered_map<uint64_t, std::vector<int>> grid;  // cell key -> photon indices in append order
+  double cell = 0, radius = 0;
+};
+AABB scene_bounds(const Scene& s);              // renderer.go:1137-1146
+int photon_budget(int level);                   // renderer.go:1148-1161
+double photon_radius(const Scene& s, int level);  // renderer.go:1163-1182
+uint64_t photon_cell_key(int64_t x, int64_t y, int64_t z);  // renderer.go:1636-1639
+PhotonMap build_photon_map(const Scene& s, const Settings& st, uint64_t seed, int64_t* rays);
+V3 photon_gather(const PhotonMap& pm, V3 p, V3 n, int max_photons);
+V3 trace_recursive(const Scene& s, Ray ray, const Settings& st, Rng& rng, TraceStats* stats, Guide* guide);
+V3 trace_photon(const Scene& s, Ray ray, const Settings& st, Rng& rng, TraceStats* stats, Guide* guide,
+                const PhotonMap& pm);
+// pixelRadiance (renderer.go:1833-1842)
+V3 pixel_radiance(const Scene& s, Ray ray, const Settings& st, Rng& rng, TraceStats* stats, Guide* guide,
+                  const PhotonMap* pm);
 
 struct RenderOut {
   std::vector<V3> linear;   // mean radiance per pixel
   std::vector<V3> sumsq;    // per-channel mean of squared sample radiance
   std::vector<Guide> guides;
   int64_t segments = 0, shadow = 0;
+  int64_t photon_rays = 0;  // rays of the photon map build (RenderState.Start adds them to Rays)
   Counters c;
 };
 // Tile-parallel render shaped like RenderState.Start's CPU path

@@ -40,7 +40,19 @@ struct orc_settings {
   int32_t rr_depth, adaptive;
   double adaptive_threshold;
   int32_t tile;
+  int32_t integrator, photon_mapping;
+  int64_t photon_seed;
 };
+
+static Settings load_settings(const orc_settings* cs) {
+  Settings st;
+  st.width = cs->width; st.height = cs->height; st.spp = cs->spp; st.bounces = cs->bounces;
+  st.msaa = cs->msaa; st.tsaa = cs->tsaa; st.sampler = cs->sampler; st.mis = cs->mis != 0;
+  st.power_light = cs->power_light != 0; st.firefly_clamp = cs->firefly_clamp; st.rr_depth = cs->rr_depth;
+  st.adaptive = cs->adaptive != 0; st.adaptive_threshold = cs->adaptive_threshold; st.tile = cs->tile;
+  st.integrator = cs->integrator; st.photon_mapping = cs->photon_mapping; st.photon_seed = cs->photon_seed;
+  return st;
+}
 
 void* orc_scene_new() { return new Scene(); }
 void orc_scene_free(void* s) { delete (Scene*)s; }
@@ -303,15 +315,11 @@ void orc_camera_basis(const double* cam10, double aspect, double* out12) {
 
 // Render: linear3 = per-pixel mean, sumsq3 = per-pixel mean of squares,
 // guides11 = (p3, n3, albedo3, depth, valid) or NULL,
-// stats5 = (segments, shadow rays, box tests, tri tests, sphere tests).
+// stats6 = (segments, shadow rays, box tests, tri tests, sphere tests, photon map rays).
 int orc_render(void* sp, const double* cam10, const orc_settings* cs, uint64_t seed, int threads, double* linear3,
-               double* sumsq3, double* guides11, int64_t* stats5) {
+               double* sumsq3, double* guides11, int64_t* stats6) {
   Scene* s = (Scene*)sp;
-  Settings st;
-  st.width = cs->width; st.height = cs->height; st.spp = cs->spp; st.bounces = cs->bounces;
-  st.msaa = cs->msaa; st.tsaa = cs->tsaa; st.sampler = cs->sampler; st.mis = cs->mis != 0;
-  st.power_light = cs->power_light != 0; st.firefly_clamp = cs->firefly_clamp; st.rr_depth = cs->rr_depth;
-  st.adaptive = cs->adaptive != 0; st.adaptive_threshold = cs->adaptive_threshold; st.tile = cs->tile;
+  Settings st = load_settings(cs);
   Camera cam{ld3(cam10), ld3(cam10 + 3), ld3(cam10 + 6), cam10[9]};
   RenderOut out;
   render(*s, cam, st, seed, threads, &out, nullptr);
@@ -325,11 +333,36 @@ int orc_render(void* sp, const double* cam10, const orc_settings* cs, uint64_t s
       st3(q, g.p); st3(q + 3, g.n); st3(q + 6, g.albedo); q[9] = g.depth; q[10] = g.valid ? 1 : 0;
     }
   }
-  if (stats5) {
-    stats5[0] = out.segments; stats5[1] = out.shadow; stats5[2] = out.c.boxes; stats5[3] = out.c.tris;
-    stats5[4] = out.c.spheres;
+  if (stats6) {
+    stats6[0] = out.segments; stats6[1] = out.shadow; stats6[2] = out.c.boxes; stats6[3] = out.c.tris;
+    stats6[4] = out.c.spheres; stats6[5] = out.photon_rays;
   }
   return 0;
+}
+
+// buildPhotonMap: photons in append order, 10 doubles each (P, N, flux,
+// emission index) up to `cap`; returns the photon count. out3 = (radius, rays, 0).
+int64_t orc_photon_map(void* sp, const orc_settings* cs, uint64_t seed, int64_t cap, double* photons10,
+                       double* out3) {
+  Settings st = load_settings(cs);
+  int64_t rays = 0;
+  PhotonMap pm = build_photon_map(*(Scene*)sp, st, seed, &rays);
+  const int64_t n = (int64_t)pm.photons.size();
+  for (int64_t i = 0; i < n && i < cap; i++) {
+    const Photon& ph = pm.photons[i];
+    double* q = photons10 + 10 * i;
+    st3(q, ph.p); st3(q + 3, ph.n); st3(q + 6, ph.flux); q[9] = ph.emission;
+  }
+  if (out3) { out3[0] = pm.radius; out3[1] = (double)rays; out3[2] = 0; }
+  return n;
+}
+
+// PhotonMap.gather at n points (3 + 3 doubles each) over the map built from
+// (settings, seed); out3 per point.
+void orc_photon_gather(void* sp, const orc_settings* cs, uint64_t seed, int64_t n, const double* pn6, double* out3) {
+  Settings st = load_settings(cs);
+  PhotonMap pm = build_photon_map(*(Scene*)sp, st, seed, nullptr);
+  for (int64_t i = 0; i < n; i++) st3(out3 + 3 * i, photon_gather(pm, ld3(pn6 + 6 * i), ld3(pn6 + 6 * i + 3), 64));
 }
 
 static std::vector<Guide> load_guides(const double* g11, int n) {

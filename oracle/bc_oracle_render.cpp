@@ -164,7 +164,7 @@ double light_directional_pdf(const Scene& s, int pi, V3 from, V3 lp, V3 ln, bool
   return sel * dist2 / (cosL * area);
 }
 
-static V3 direct_light(const Scene& s, const Hit& h, V3 hitP, const Material& mat, Rng& rng,
+V3 direct_light(const Scene& s, const Hit& h, V3 hitP, const Material& mat, Rng& rng,
                        const Settings& st, TraceStats* stats) {  // renderer.go:1427-1465
   if (mat.kind != MatDiffuse || s.light_spheres.empty()) return v3(0, 0, 0);
   double selectPDF;
@@ -193,7 +193,7 @@ static V3 direct_light(const Scene& s, const Hit& h, V3 hitP, const Material& ma
   return mul(had(f, lm.emission), nd * w / lightPDF);
 }
 
-static V3 material_preview_color(const Material& m) {  // renderer.go:1467-1475
+V3 material_preview_color(const Material& m) {  // renderer.go:1467-1475
   if (m.kind == MatEmissive)
     return v3(clampd(m.emission.x / 8, 0, 1), clampd(m.emission.y / 8, 0, 1), clampd(m.emission.z / 8, 0, 1));
   if (dot(m.color, m.color) > 0) return m.color;
@@ -363,7 +363,8 @@ std::vector<int> make_tile_order(int tx, int ty, const std::string& mode) {
 // (seed, pixel, sample), which makes renders independent of thread count.
 static V3 adaptive_pixel(const Scene& s, V3 origin, V3 lower, V3 horiz, V3 vert, int x, int y, int W, int H,
                          const Settings& st, uint64_t seed, const std::vector<double>& SX,
-                         const std::vector<double>& SY, TraceStats* stats, Guide* guide, V3* sumsq_out) {
+                         const std::vector<double>& SY, TraceStats* stats, Guide* guide, V3* sumsq_out,
+                         const PhotonMap* pm) {
   int pixelSPP = effective_spp(st);
   V3 sum = v3(0, 0, 0), sq = v3(0, 0, 0);
   double sumLum = 0, sumSqLum = 0;
@@ -384,7 +385,8 @@ static V3 adaptive_pixel(const Scene& s, V3 origin, V3 lower, V3 horiz, V3 vert,
     double u = ((double)x + jx) / (double)std::max(W - 1, 1);
     double v = ((double)(H - 1 - y) + jy) / (double)std::max(H - 1, 1);
     V3 dir = sub(add(add(lower, mul(horiz, u)), mul(vert, v)), origin);
-    V3 c = clamp_firefly(trace(s, Ray{origin, dir}, st, rng, stats, sample == 0 ? guide : nullptr), st.firefly_clamp);
+    V3 c = clamp_firefly(pixel_radiance(s, Ray{origin, dir}, st, rng, stats, sample == 0 ? guide : nullptr, pm),
+                         st.firefly_clamp);
     sum = add(sum, c);
     sq = add(sq, had(c, c));
     double lum = luminance(c);
@@ -417,6 +419,10 @@ void render(const Scene& s, const Camera& cam, const Settings& st, uint64_t seed
   std::vector<int> order = make_tile_order(tx, ty, "Center");
   std::vector<double> SX, SY;
   build_sample_sequence(st, &SX, &SY);
+  // renderer.go:2728-2734: the photon map is built once per frame, before the tiles
+  PhotonMap pm;
+  if (st.integrator == IntegratorPhoton)
+    pm = build_photon_map(s, st, st.photon_seed >= 0 ? (uint64_t)st.photon_seed : seed, &out->photon_rays);
   if (threads < 1) threads = (int)std::max(1u, std::thread::hardware_concurrency());
   threads = std::min(threads, std::max(1, total));
   std::atomic<int> next{0};
@@ -433,7 +439,7 @@ void render(const Scene& s, const Camera& cam, const Settings& st, uint64_t seed
         for (int x = x0; x < x1; x++) {
           size_t i = (size_t)y * W + x;
           out->linear[i] = adaptive_pixel(s, origin, lower, horiz, vert, x, y, W, H, st, seed, SX, SY, &per[id],
-                                          &out->guides[i], &out->sumsq[i]);
+                                          &out->guides[i], &out->sumsq[i], &pm);
         }
     }
   };

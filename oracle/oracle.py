@@ -22,7 +22,21 @@ class OrcSettings(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("bounces", C.c_int32),
                 ("msaa", C.c_int32), ("tsaa", C.c_int32), ("sampler", C.c_int32), ("mis", C.c_int32),
                 ("power_light", C.c_int32), ("firefly_clamp", C.c_double), ("rr_depth", C.c_int32),
-                ("adaptive", C.c_int32), ("adaptive_threshold", C.c_double), ("tile", C.c_int32)]
+                ("adaptive", C.c_int32), ("adaptive_threshold", C.c_double), ("tile", C.c_int32),
+                ("integrator", C.c_int32), ("photon_mapping", C.c_int32), ("photon_seed", C.c_int64)]
+
+_INTEGRATOR_CODE = {"Path Tracing": 0, "Recursive Ray Tracing": 1, "Photon Mapping": 2}
+
+
+def _orc_settings(st, tile=8, photon_seed=None):
+    return OrcSettings(width=st.width, height=st.height, spp=st.spp, bounces=st.bounces, msaa=st.msaa,
+                       tsaa=st.tsaa, sampler={"Random": 0, "Halton": 1, "R2": 2}[st.sampler], mis=int(st.mis),
+                       power_light=int(st.power_light_sampling), firefly_clamp=float(st.firefly_clamp),
+                       rr_depth=st.rr_depth, adaptive=int(st.adaptive_sampling),
+                       adaptive_threshold=float(st.adaptive_threshold), tile=tile,
+                       integrator=_INTEGRATOR_CODE[getattr(st, "integrator", "Path Tracing")],
+                       photon_mapping=int(getattr(st, "photon_mapping", 0)),
+                       photon_seed=-1 if photon_seed is None else int(photon_seed))
 
 
 _SIG = [
@@ -69,6 +83,8 @@ _SIG = [
     ("orc_clamp_firefly", None, [f64p, C.c_double, f64p]),
     ("orc_camera_basis", None, [f64p, C.c_double, f64p]),
     ("orc_render", C.c_int, [C.c_void_p, f64p, P(OrcSettings), C.c_uint64, C.c_int, f64p, f64p, f64p, i64p]),
+    ("orc_photon_map", C.c_int64, [C.c_void_p, P(OrcSettings), C.c_uint64, C.c_int64, f64p, f64p]),
+    ("orc_photon_gather", None, [C.c_void_p, P(OrcSettings), C.c_uint64, C.c_int64, f64p, f64p]),
     ("orc_atrous", None, [f64p, f64p, C.c_int, C.c_int, C.c_int, f64p]),
     ("orc_bloom", None, [f64p, C.c_int, C.c_int, C.c_int, f64p]),
     ("orc_tone_map", None, [f64p, C.c_int64, C.c_int, f64p]),
@@ -257,20 +273,36 @@ class OracleScene:
     def light_selection_pdf(self, prim, power=True):
         return lib().orc_light_selection_pdf(self.h, int(prim), 1 if power else 0)
 
-    def render(self, cam, st, seed=1, threads=0, tile=8):
-        """Returns dict(linear, sumsq, guides (H,W,11), stats)."""
-        cs = OrcSettings(width=st.width, height=st.height, spp=st.spp, bounces=st.bounces, msaa=st.msaa,
-                         tsaa=st.tsaa, sampler={"Random": 0, "Halton": 1, "R2": 2}[st.sampler], mis=int(st.mis),
-                         power_light=int(st.power_light_sampling), firefly_clamp=float(st.firefly_clamp),
-                         rr_depth=st.rr_depth, adaptive=int(st.adaptive_sampling),
-                         adaptive_threshold=float(st.adaptive_threshold), tile=tile)
+    def render(self, cam, st, seed=1, threads=0, tile=8, photon_seed=None):
+        """Returns dict(linear, sumsq, guides (H,W,11), stats). photon_seed: seed of
+        the photon map's emission streams (default: `seed`)."""
+        cs = _orc_settings(st, tile, photon_seed)
         cam10 = _f64(list(cam.position) + list(cam.target) + list(cam.up) + [cam.fov])
         W, H = st.width, st.height
-        lin = np.zeros((H, W, 3)); sq = np.zeros((H, W, 3)); g = np.zeros((H, W, 11)); stats = np.zeros(5, np.int64)
+        lin = np.zeros((H, W, 3)); sq = np.zeros((H, W, 3)); g = np.zeros((H, W, 11)); stats = np.zeros(6, np.int64)
         lib().orc_render(self.h, _p(cam10, C.c_double), C.byref(cs), int(seed), int(threads), _p(lin, C.c_double),
                          _p(sq, C.c_double), _p(g, C.c_double), _p(stats, C.c_int64))
         return {"linear": lin, "sumsq": sq, "guides": g,
-                "stats": dict(zip(("segments", "shadow", "boxes", "tris", "spheres"), stats.tolist()))}
+                "stats": dict(zip(("segments", "shadow", "boxes", "tris", "spheres", "photon_rays"),
+                                  stats.tolist()))}
+
+    def photon_map(self, st, seed=1):
+        """buildPhotonMap: dict(photons (n, 10): P, N, flux, emission index, in append
+        order; radius; rays)."""
+        cs = _orc_settings(st)
+        cap = 16384 + max(2, st.bounces) + 16
+        out = np.zeros((cap, 10)); o3 = np.zeros(3)
+        n = lib().orc_photon_map(self.h, C.byref(cs), int(seed), cap, _p(out, C.c_double), _p(o3, C.c_double))
+        return {"photons": out[:min(n, cap)].copy(), "radius": float(o3[0]), "rays": int(o3[1])}
+
+    def photon_gather(self, st, points, normals, seed=1):
+        """PhotonMap.gather(p, n, 64) at each point over the map of (st, seed)."""
+        pn = np.ascontiguousarray(np.concatenate([np.asarray(points, np.float64),
+                                                  np.asarray(normals, np.float64)], axis=1))
+        out = np.zeros((len(pn), 3))
+        lib().orc_photon_gather(self.h, C.byref(_orc_settings(st)), int(seed), len(pn), _p(pn, C.c_double),
+                                _p(out, C.c_double))
+        return out
 
 
 def aabb_hit(box6, ray6, tmin=1e-4, tmax=1e30):

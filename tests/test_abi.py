@@ -44,3 +44,29 @@ def test_null_arguments_rejected(native_lib):
     assert L.bc_raycast(None, None, 0, None, None) == 7
     buf = C.create_string_buffer(64)
     assert L.bc_last_error(None, buf, 64) == 0
+
+
+def test_struct_layouts_match_the_header(native_lib, tmp_path):
+    """The ctypes mirrors of the ABI structs have the C compiler's size and field
+    offsets (a field added to the header must be added to the mirror)."""
+    from bcgx import _lib
+    pairs = [("bc_scene_desc", _lib.SceneDesc), ("bc_camera", _lib.CameraC), ("bc_settings", _lib.SettingsC),
+             ("bc_view", _lib.ViewC), ("bc_diff_desc", _lib.DiffDescC), ("bc_post_desc", _lib.PostDescC)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "bc_gx.h"', "int main(void) {"]
+    for cname, py in pairs:
+        lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            lines.append(f'  printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        name, field, value = line.split()
+        got[(name, field)] = int(value)
+    for cname, py in pairs:
+        assert got[(cname, "sizeof")] == C.sizeof(py), cname
+        for f in py._fields_:
+            assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])

@@ -711,6 +711,97 @@ def run_build(args):
     return 0
 
 
+def _bench_settings(w, h, spp, bounces):
+    """benchmarkSettings (benchmark.go:71-94): Draft with adaptive sampling, post
+    and upscaling off, Random sampler, MIS, power-weighted lights, 16-bin SAH."""
+    import bcgx
+    q = bcgx.quality("Draft")
+    q.width, q.height, q.spp, q.bounces = w, h, spp, bounces
+    q.adaptive_sampling, q.denoise = False, False
+    q.fxaa, q.taa, q.tsaa, q.txaa, q.hbao, q.hbao_plus, q.bloom = 0, 0, 0, 0, 0, 0, 0
+    q.msaa, q.sampler, q.mis, q.power_light_sampling = 1, "Random", True, True
+    q.bvh_mode, q.bvh_bins, q.bvh_leaf_size = "SAH", 16, 4
+    return q
+
+
+def run_integrators(args):
+    """The reference's integrator comparison (benchmarkIntegrators,
+    benchmark.go:202-216): the Cornell-like room at 384x216, 2 spp, 5 bounces,
+    for the path, recursive and photon-mapping integrators (PhotonMapping 1).
+    A step is one frame through bc_render_frame (post off) with a new seed, so
+    the photon integrator rebuilds its photon map every frame as Start does.
+    value = rays (path segments, plus the photon map's) / frame time. One JSON
+    line per integrator; `large` repeats the frame at 1920x1080, 64 spp."""
+    import ctypes as C
+    import numpy as np
+    import bcgx
+    from bcgx import scenes
+    spec, cam = scenes.cornell_reference_scene()
+    ctx = bcgx.Context(0)
+    ctx.upload(scenes.to_scene(spec))
+    L = bcgx.lib()
+    cc = cam.c()
+
+    def frames(st, n, seed0, readback=False):
+        times, rays = [], 0
+        for k in range(n):
+            q = st.copy()
+            q.seed = seed0 + k
+            sc = q.c()
+            r = C.c_int64(0)
+            lin = np.empty((q.height, q.width, 3), np.float32) if readback else None
+            t0 = time.perf_counter()
+            bcgx._lib.check(L.bc_render_frame(ctx.handle, C.byref(cc), C.byref(sc), bcgx._lib.ptr(lin, C.c_float),
+                                              None, None, C.byref(r)), ctx.handle)
+            times.append(time.perf_counter() - t0)
+            rays += r.value
+        return times, rays
+
+    for integ in (bcgx.INTEGRATOR_PATH, bcgx.INTEGRATOR_RECURSIVE, bcgx.INTEGRATOR_PHOTON):
+        st = _bench_settings(384, 216, 2, 5)
+        st.integrator = integ
+        if integ == bcgx.INTEGRATOR_PHOTON:
+            st.photon_mapping = 1
+        frames(st, args.warmup, 1000)
+        clocks = ClockSampler(0)
+        clocks.start()
+        times, rays = frames(st, args.steps, 2000)
+        big = st.copy()
+        big.width, big.height, big.spp = 1920, 1080, 64
+        frames(big, 1, 3000)
+        bt, br = frames(big, 2, 3100)
+        clk = clocks.stop()
+        et, er = frames(st, 1, 4000, readback=True)
+        value = rays / sum(times) / 1e6
+        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 primary rays)",
+                "data": "synthetic, seeded",
+                "config": {"workload": f"integrator comparison: Cornell-like room, 384x216, 2 spp, 5 bounces, "
+                                       f"{integ}" + (", PhotonMapping 1" if st.photon_mapping else ""),
+                           "rays_per_frame": rays // max(1, args.steps)},
+                "large": {"value": br / sum(bt) / 1e6, "unit": METRIC, "ms_per_frame": 1e3 * sum(bt) / len(bt),
+                          "frame": "1920x1080, 64 spp"},
+                "e2e": {"value": er / sum(et) / 1e6, "unit": METRIC, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": st.width * st.height * 12},
+                "gpu_launches": None, "clocks": clk}
+        if not args.no_cpu_baseline:
+            import oracle
+            ref = oracle.OracleScene.from_spec(spec)
+            cst = st.copy()
+            cst.spp = 2048
+            t0 = time.perf_counter()
+            out = ref.render(cam, cst, seed=7, threads=0)
+            dt = time.perf_counter() - t0
+            segs = out["stats"]["segments"] + out["stats"]["photon_rays"]
+            line["cpu_baseline"] = {"value": segs / dt / 1e6, "unit": METRIC, "cores": os.cpu_count(),
+                                    "kind": "port", "sample": f"384x216 at 2048 spp, {dt:.1f} s"}
+            line["roofline"] = _render_roofline(out["stats"], value)
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     global N_TRIS, N_RAYS
     ap = argparse.ArgumentParser()
@@ -723,7 +814,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
     ap.add_argument("--minblocks", type=int, default=0, help="ray-cast register variant (1, 6, 8; 0 = library default)")
     ap.add_argument("--fast", action="store_true", help="plain fp32 closest hit instead of the exact contract")
-    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch", "diff", "refit", "build"],
+    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch", "diff", "refit", "build", "integrators"],
                     help="raycast (default, the headline line) or a render workload")
     ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
     ap.add_argument("--rmse", action="store_true", help="render workloads: RMSE against a converged image")
@@ -747,6 +838,8 @@ def main():
         return run_refit(args)
     if args.workload == "build":
         return run_build(args)
+    if args.workload == "integrators":
+        return run_integrators(args)
     if args.workload != "raycast":
         return run_render(args)
     return run_gpu(args)

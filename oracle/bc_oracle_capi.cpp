@@ -340,6 +340,10 @@ int orc_render(void* sp, const double* cam10, const orc_settings* cs, uint64_t s
   return 0;
 }
 
+int orc_photon_budget(int level) { return photon_budget(level); }
+uint64_t orc_photon_cell_key(int64_t x, int64_t y, int64_t z) { return photon_cell_key(x, y, z); }
+double orc_photon_radius(void* sp, int level) { return photon_radius(*(Scene*)sp, level); }
+
 // buildPhotonMap: photons in append order, 10 doubles each (P, N, flux,
 // emission index) up to `cap`; returns the photon count. out3 = (radius, rays, 0).
 int64_t orc_photon_map(void* sp, const orc_settings* cs, uint64_t seed, int64_t cap, double* photons10,

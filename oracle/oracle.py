@@ -83,6 +83,9 @@ _SIG = [
     ("orc_clamp_firefly", None, [f64p, C.c_double, f64p]),
     ("orc_camera_basis", None, [f64p, C.c_double, f64p]),
     ("orc_render", C.c_int, [C.c_void_p, f64p, P(OrcSettings), C.c_uint64, C.c_int, f64p, f64p, f64p, i64p]),
+    ("orc_photon_budget", C.c_int, [C.c_int]),
+    ("orc_photon_cell_key", C.c_uint64, [C.c_int64, C.c_int64, C.c_int64]),
+    ("orc_photon_radius", C.c_double, [C.c_void_p, C.c_int]),
     ("orc_photon_map", C.c_int64, [C.c_void_p, P(OrcSettings), C.c_uint64, C.c_int64, f64p, f64p]),
     ("orc_photon_gather", None, [C.c_void_p, P(OrcSettings), C.c_uint64, C.c_int64, f64p, f64p]),
     ("orc_atrous", None, [f64p, f64p, C.c_int, C.c_int, C.c_int, f64p]),
@@ -285,6 +288,9 @@ class OracleScene:
         return {"linear": lin, "sumsq": sq, "guides": g,
                 "stats": dict(zip(("segments", "shadow", "boxes", "tris", "spheres", "photon_rays"),
                                   stats.tolist()))}
+
+    def photon_radius(self, level):
+        return lib().orc_photon_radius(self.h, int(level))
 
     def photon_map(self, st, seed=1):
         """buildPhotonMap: dict(photons (n, 10): P, N, flux, emission index, in append

@@ -14,6 +14,10 @@ renderer.go, computed here in pure Python independently of the C++ oracle:
 * radicalInverse (renderer.go:1844-1858) for n = 1..256, bases 2 and 3, and
   pixelSampleRotation (1906-1915) on a grid of pixels: both are integer or
   fixed-order fp64 arithmetic, so Python floats reproduce them bit for bit.
+* photonBudget (renderer.go:1148-1161) for levels -1..6, photonCellKey
+  (1636-1639) on integer cells (int64 products wrapping, then XOR), and
+  photonRadius (1163-1182) of NewCornellScene (2960-2979): Scene.Bounds
+  (1137-1146) over AddTriangle's padded boxes (257-269) and AddSphere's (246-256).
 
 Run: python tests/golden/make_golden.py
 """
@@ -78,6 +82,41 @@ def pixel_sample_rotation(x: int, y: int):
     return float(h1) * inv, float(h2) * inv
 
 
+def photon_budget(level: int) -> int:
+    return {1: 512, 2: 2048, 3: 8192, 4: 16384}.get(level, 0)
+
+
+def photon_cell_key(x: int, y: int, z: int) -> int:
+    m = (1 << 64) - 1
+    return ((x * 73856093) & m) ^ ((y * 19349663) & m) ^ ((z * 83492791) & m)
+
+
+def cornell_bounds():
+    tris = [((-3, -2, -8), (3, -2, -8), (3, -2, -2)), ((-3, -2, -8), (3, -2, -2), (-3, -2, -2)),
+            ((-3, -2, -8), (-3, -2, -2), (-3, 4, -2)), ((-3, -2, -8), (-3, 4, -2), (-3, 4, -8)),
+            ((3, -2, -2), (3, -2, -8), (3, 4, -8)), ((3, -2, -2), (3, 4, -8), (3, 4, -2))]
+    spheres = [((-.9, -1, -5.2), 1), ((1.1, -1.2, -4.2), .8), ((0, 3.2, -5), .65)]
+    lo, hi = [float("inf")] * 3, [float("-inf")] * 3
+    for t in tris:
+        for k in range(3):
+            lo[k] = min(lo[k], min(float(v[k]) for v in t) - 1e-6)
+            hi[k] = max(hi[k], max(float(v[k]) for v in t) + 1e-6)
+    for c, r in spheres:
+        for k in range(3):
+            lo[k] = min(lo[k], c[k] - r)
+            hi[k] = max(hi[k], c[k] + r)
+    return lo, hi
+
+
+def photon_radius(lo, hi, level: int) -> float:
+    e = [hi[k] - lo[k] for k in range(3)]
+    diag = (e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) ** 0.5
+    if diag < 1e-3:
+        diag = 10.0
+    base = diag * 0.03
+    return {1: base * 1.8, 2: base * 1.2, 3: base * 0.85, 4: base * 0.6}.get(level, base)
+
+
 def main():
     boxes = [((-1, -1, -1), (1, 1, 1)), ((2, -3, -4), (6, 5, 2)), ((-10, 0, -2), (-2, 0.1, 8))]
     rays = [((0, 0, 5), (0, 0, -1)), ((0, 0, 0), (1, 0, 0)), ((4, 10, 0), (0, -1, 0)), ((20, 20, 20), (1, 1, 1)),
@@ -98,6 +137,11 @@ def main():
                            for x in (0, 1, 17, 319, 2559) for y in (0, 1, 29, 239, 1439)],
         "stress_scene": {"spheres": 1 + 20 * 41 + 1, "lights": 1},
         "showcase_scene": {"spheres": 5, "lights": 1},
+        "photon_budget": {str(lv): photon_budget(lv) for lv in range(-1, 7)},
+        "photon_cell_key": [{"c": list(c), "key": format(photon_cell_key(*c), "016x")}
+                            for c in ((0, 0, 0), (1, 2, 3), (-1, -1, -1), (-7, 12, -3), (100000, -250000, 3),
+                                      (-(1 << 40), 1 << 41, -(1 << 42)), (2147483647, -2147483648, 1))],
+        "photon_radius_cornell": {str(lv): f64_bits(photon_radius(*cornell_bounds(), lv)) for lv in range(0, 6)},
     }
     with open(os.path.join(HERE, "reference_pins.json"), "w") as f:
         json.dump(pins, f, indent=1, sort_keys=True)

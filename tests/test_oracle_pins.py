@@ -208,3 +208,50 @@ def test_stress_scene_counts(orc, pins):
     s = orc.OracleScene.from_spec(spec)
     c = s.counts()
     assert c["prims"] == pins["stress_scene"]["spheres"] and c["lights"] == pins["stress_scene"]["lights"]
+
+
+def test_photon_functions(orc, pins):
+    """photonBudget, photonCellKey and photonRadius of NewCornellScene
+    (renderer.go:1148-1182, 1636-1639) against the pure-Python restatement."""
+    import struct
+    from bcgx import scenes
+    for lv, want in pins["photon_budget"].items():
+        assert orc.lib().orc_photon_budget(int(lv)) == want
+    for case in pins["photon_cell_key"]:
+        assert format(orc.lib().orc_photon_cell_key(*case["c"]), "016x") == case["key"]
+    spec, _ = scenes.cornell_reference_scene()
+    ref = orc.OracleScene.from_spec(spec)
+    for lv, bits in pins["photon_radius_cornell"].items():
+        assert struct.pack("<d", ref.photon_radius(int(lv))).hex() == bits, lv
+
+
+def test_photon_map_properties(orc):
+    """buildPhotonMap on the Cornell-like room: the stop rule (the budget is
+    checked before each emission, so the last one may overshoot by fewer than
+    max(2, bounces) photons), append order by emission, every photon on a
+    diffuse surface facing its normal, flux along a path never growing before
+    Russian roulette rescales it; empty maps for levels outside 1-4."""
+    import numpy as np
+    import bcgx
+    from bcgx import scenes
+    spec, _ = scenes.cornell_reference_scene()
+    ref = orc.OracleScene.from_spec(spec)
+    st = bcgx.quality("Draft")
+    st.bounces = 5
+    for lv, budget in ((1, 512), (2, 2048)):
+        st.photon_mapping = lv
+        m = ref.photon_map(st, seed=3)
+        ph = m["photons"]
+        assert budget <= len(ph) < budget + max(2, st.bounces)
+        em = ph[:, 9]
+        assert np.all(np.diff(em) >= 0)
+        # all but the last emission ran before the budget was reached
+        last = em[-1]
+        assert np.sum(em < last) < budget
+        assert np.allclose(np.linalg.norm(ph[:, 3:6], axis=1), 1.0, atol=1e-9)
+        assert np.all(ph[:, 6:9] >= 0) and np.all(ph[:, 6:9].max(axis=1) > 0)
+        assert m["rays"] >= len(ph)
+        assert m["radius"] > 0
+    for lv in (0, 5):
+        st.photon_mapping = lv
+        assert len(ref.photon_map(st, seed=3)["photons"]) == 0

@@ -802,6 +802,32 @@ def run_integrators(args):
     return 0
 
 
+def run_calibration(args):
+    """CPU-baseline calibration: the oracle on the reference's published CPU case
+    (GIGA suite "CPU scaling", benchmarkSettings(448, 252, 4, 6, workers) on
+    NewStressScene: 902,710 rays, 2.70 Mray/s on 1 worker and 4.91 on 2 of an
+    unnamed 5-CPU container), on 1 and 2 threads of this host. No GPU work."""
+    import oracle
+    from bcgx import scenes
+    spec, cam = scenes.stress_scene()
+    ref = oracle.OracleScene.from_spec(spec)
+    q = _bench_settings(448, 252, 4, 6)
+    out = {"metric": "Mrays/s per worker", "impl": "oracle", "workload":
+           "Stress scene 448x252, 4 spp, 6 bounces (benchmarkSettings)",
+           "reference_published": {"1": 2.70, "2": 4.91, "rays": 902710}}
+    for th in (1, 2):
+        best = None
+        for _ in range(3):
+            t0 = time.perf_counter()
+            r = ref.render(cam, q, seed=1, threads=th)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        out[str(th)] = r["stats"]["segments"] / best / 1e6
+        out["rays"] = r["stats"]["segments"]
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     global N_TRIS, N_RAYS
     ap = argparse.ArgumentParser()
@@ -814,7 +840,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
     ap.add_argument("--minblocks", type=int, default=0, help="ray-cast register variant (1, 6, 8; 0 = library default)")
     ap.add_argument("--fast", action="store_true", help="plain fp32 closest hit instead of the exact contract")
-    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch", "diff", "refit", "build", "integrators"],
+    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch", "diff", "refit", "build", "integrators",
+                             "calibration"],
                     help="raycast (default, the headline line) or a render workload")
     ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
     ap.add_argument("--rmse", action="store_true", help="render workloads: RMSE against a converged image")
@@ -840,6 +867,8 @@ def main():
         return run_build(args)
     if args.workload == "integrators":
         return run_integrators(args)
+    if args.workload == "calibration":
+        return run_calibration(args)
     if args.workload != "raycast":
         return run_render(args)
     return run_gpu(args)

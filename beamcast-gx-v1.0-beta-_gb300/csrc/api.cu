@@ -359,7 +359,7 @@ bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out
     e = cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_status(ctx, e, "ray-cast stream");
   }
-  const int64_t chunk = (int64_t)1 << 20;
+  const int64_t chunk = ctx->raycast_chunk;
   cudaStream_t streams[2] = {ctx->stream, ctx->aux_stream};
   void* order[2] = {nullptr, nullptr};
   if (ctx->raycast_sort && n >= kMinOrderedRays)
@@ -437,6 +437,12 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     ctx->raycast_sort = (int)value;
     return BC_OK;
   }
+  if (n == "raycast_chunk") {
+    if (value < 65536 || value > (1LL << 28))
+      return set_error(ctx, BC_ERR_INVALID_ARG, "raycast_chunk must be in [65536, 2^28]");
+    ctx->raycast_chunk = (long long)value;
+    return BC_OK;
+  }
   if (n == "render_wave_cap") {
     if (value < 4096 || value > (1 << 27))
       return set_error(ctx, BC_ERR_INVALID_ARG, "render_wave_cap must be in [4096, 2^27]");
@@ -463,6 +469,7 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
   if (n == "raycast_exact") { *value = ctx->raycast_exact; return BC_OK; }
   if (n == "render_wave_cap") { *value = ctx->render_wave_cap; return BC_OK; }
   if (n == "raycast_sort") { *value = ctx->raycast_sort; return BC_OK; }
+  if (n == "raycast_chunk") { *value = ctx->raycast_chunk; return BC_OK; }
   if (n == "render_graph") { *value = ctx->render_graph; return BC_OK; }
   if (n == "render_engine") { *value = ctx->render_engine; return BC_OK; }
   return BC_ERR_INVALID_ARG;

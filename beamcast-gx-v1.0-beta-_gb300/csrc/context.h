@@ -88,6 +88,7 @@ struct bc_context {
   int raycast_exact = 1;      // 0: plain fp32 closest hit (bc_set_option "raycast_exact")
   int raycast_variant = 6;    // 0 = fast kernel, else the exact kernel's minblocks
   int raycast_sort = 1;       // trace rays in a spatially coherent order (bc_set_option "raycast_sort")
+  long long raycast_chunk = 1 << 21;  // rays per pipelined chunk of bc_raycast (bc_set_option "raycast_chunk")
   bcgx::DevBuf d_order[3];    // ray order scratch: [0], [1] the two streams of bc_raycast, [2] bc_raycast_device
   // ray-cast staging
   bcgx::DevBuf d_rays, d_t, d_prim, d_occ;

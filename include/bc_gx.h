@@ -410,8 +410,8 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *                        in a spatially coherent order (origin Morton code on a
  *                        64^3 grid over the scene bounds, then direction octant);
  *                        results are returned in the caller's order either way.
- *   "raycast_chunk"      rays per chunk of bc_raycast / bc_occluded with host
- *                        buffers, 65,536 .. 2^28 (default 2^21): chunks alternate
+ *   "raycast_chunk"      rays per chunk of bc_raycast (host buffers),
+ *                        65,536 .. 2^28 (default 2^21): chunks alternate
  *                        between two streams, so one chunk's copies overlap
  *                        another's kernel.
  *   "render_wave_cap"    paths in flight per wave of the renderer, 4096 .. 2^27

@@ -187,3 +187,84 @@ def test_integrator_argument_errors(gpu_ctx):
     assert rc == 7  # BC_ERR_INVALID_ARG
     with pytest.raises(bcgx.BCError, match="INVALID_ARG"):
         gpu_ctx.photon_map(st, scene=3)
+
+
+def test_batch_with_more_photon_maps_than_the_cache_holds(gpu_ctx):
+    """20 photon views with 20 seeds need 20 maps in one call (the cache keeps 16
+    between calls): the maps of the call are never evicted under it, and every
+    view equals the same view rendered alone."""
+    spec, cam = scenes.cornell_reference_scene()
+    gpu_ctx.upload(scenes.to_scene(spec))
+    views = [(0, cam, _settings(PHOTON, w=32, h=24, spp=2, bounces=4, level=1, seed=500 + k)) for k in range(20)]
+    outs, _ = gpu_ctx.render_batch(views)
+    outs2, _ = gpu_ctx.render_batch(views[::-1])  # the same maps again, in another order
+    for k, (_, c, st) in enumerate(views):
+        alone = gpu_ctx.render_frame(c, st, want_guides=False, want_rgba=False)["linear"]
+        assert np.array_equal(outs[k], alone), k
+        assert np.array_equal(outs2[19 - k], alone), k
+
+
+def test_photon_maps_of_a_scene_set(gpu_ctx):
+    """Views of two resident scenes at two photon levels in one batch: each view
+    uses its own scene's map (radius from its own bounds) and equals the view alone."""
+    a, cam_a = scenes.cornell_reference_scene()
+    b, cam_b = scenes.showcase_scene()
+    gpu_ctx.upload_set([scenes.to_scene(a), scenes.to_scene(b)])
+    va = (0, cam_a, _settings(PHOTON, w=48, h=32, spp=2, bounces=4, level=1, seed=61))
+    vb = (1, cam_b, _settings(PHOTON, w=40, h=30, spp=2, bounces=4, level=2, seed=62))
+    outs, _ = gpu_ctx.render_batch([va, vb])
+    (oa,), _ = gpu_ctx.render_batch([va])
+    (ob,), _ = gpu_ctx.render_batch([vb])
+    assert np.array_equal(outs[0], oa) and np.array_equal(outs[1], ob)
+    ma = gpu_ctx.photon_map(va[2], scene=0)["photons"]
+    mb = gpu_ctx.photon_map(vb[2], scene=1)["photons"]
+    assert 512 <= len(ma) < 512 + 4 and 2048 <= len(mb) < 2048 + 4
+
+
+def test_photon_map_follows_a_geometry_update(gpu_ctx):
+    """A geometry-only update (moved primitives, refit boxes) drops the cached
+    photon map: the next photon frame equals a fresh upload of the moved scene."""
+    spec, cam = scenes.cornell_reference_scene()
+    s = scenes.to_scene(spec)
+    gpu_ctx.upload(s)
+    st = _settings(PHOTON, w=64, h=48, spp=4, bounces=5, level=2, seed=71)
+    before = gpu_ctx.render_frame(cam, st, want_guides=False, want_rgba=False)["linear"]
+    map_before = gpu_ctx.photon_map(st)["photons"]
+    updates = gpu_ctx.scene_stats()["geometry_updates"]
+    rng = np.random.default_rng(4)
+    for i in range(s.counts()["prims"]):
+        s.translate_primitive(int(i), tuple(rng.uniform(-0.05, 0.05, 3)))
+    s.refit()
+    gpu_ctx.upload(s)
+    assert gpu_ctx.scene_stats()["geometry_updates"] == updates + 1
+    moved = gpu_ctx.render_frame(cam, st, want_guides=False, want_rgba=False)["linear"]
+    map_moved = gpu_ctx.photon_map(st)["photons"]
+    gpu_ctx.upload(s, scene_id=0xF0F0)  # full upload of the moved scene
+    fresh = gpu_ctx.render_frame(cam, st, want_guides=False, want_rgba=False)["linear"]
+    map_fresh = gpu_ctx.photon_map(st)["photons"]
+    assert not np.array_equal(map_before[:, 0:3], map_moved[:, 0:3][:len(map_before)])
+    # emission by emission, the rebuilt map equals the fresh upload's (a re-quantized
+    # node box may turn an fp32 traversal decision and split one emission's path)
+    assert abs(len(map_moved) - len(map_fresh)) < max(2, st.bounces)
+    em, ef = map_moved[:, 9].astype(np.int64), map_fresh[:, 9].astype(np.int64)
+    k = int(min(em.max(), ef.max()))
+    same = 0
+    for e in range(k + 1):
+        a_, b_ = map_moved[em == e], map_fresh[ef == e]
+        same += int(a_.shape == b_.shape and (a_.size == 0 or np.abs(a_ - b_).max() <= 1e-5))
+    assert same >= 0.98 * (k + 1), same / (k + 1)
+    assert np.all(moved == fresh, axis=-1).mean() >= 0.99
+    assert not np.array_equal(before, moved)
+
+
+def test_recursive_with_adaptive_stop(gpu_ctx, cornell):
+    """adaptivePixel's early stop (renderer.go:1957-1968) over recursive samples:
+    CRN against the oracle with the stop on."""
+    spec, cam, ref = cornell
+    gpu_ctx.upload(scenes.to_scene(spec))
+    st = _settings(RECURSIVE, spp=32, bounces=5, seed=81)
+    st.adaptive_sampling, st.adaptive_threshold = True, 0.002
+    m_g, _, _ = gpu_ctx.render_moments(cam, st)
+    m_c = ref.render(cam, st, seed=81, threads=0)["linear"]
+    close = np.all(np.abs(m_g - m_c) <= 2e-3 * (1 + np.abs(m_c)), axis=2)
+    assert close.mean() > 0.95, f"only {close.mean():.4f} of pixels replay the CPU paths"

@@ -60,6 +60,12 @@ class DiffDescC(C.Structure):
                 ("emission_materials", P(C.c_int32))]
 
 
+class TuneReportC(C.Structure):
+    _fields_ = [("raycast_minblocks", C.c_int32), ("raycast_sort", C.c_int32), ("render_wave_cap", C.c_int64),
+                ("n_timed", C.c_int32), ("reserved", C.c_int32), ("best_ms", C.c_double), ("default_ms", C.c_double),
+                ("worst_ms", C.c_double)]
+
+
 class PostDescC(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("render_width", C.c_int32),
                 ("render_height", C.c_int32), ("hbao", C.c_int32), ("hbao_plus", C.c_int32),
@@ -89,6 +95,8 @@ SIGNATURES = [
     ("bc_render_frame", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, u32p, u32p, i64p]),
     ("bc_render_moments", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, f32p, i64p]),
     ("bc_render_batch", C.c_int, [C.c_void_p, P(ViewC), C.c_int32, P(f32p), i64p]),
+    ("bc_autotune_raycast", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, P(TuneReportC)]),
+    ("bc_autotune_render", C.c_int, [C.c_void_p, P(ViewC), C.c_int32, P(TuneReportC)]),
     ("bc_photon_map", C.c_int, [C.c_void_p, C.c_int32, P(SettingsC), C.c_int32, f32p, P(C.c_int32), i64p]),
     ("bc_diff_configure", C.c_int, [C.c_void_p, P(DiffDescC)]),
     ("bc_diff_set_target", C.c_int, [C.c_void_p, f32p]),

@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import DiffDescC, PostDescC, SceneDesc, ViewC, check, lib, ptr
+from ._lib import DiffDescC, PostDescC, SceneDesc, TuneReportC, ViewC, check, lib, ptr
 from .scene import Scene, SceneArrays
 from .settings import Camera, RenderSettings
 
@@ -182,6 +182,27 @@ class Context:
         check(lib().bc_photon_map(self._h, int(scene), C.byref(sc), n.value, ptr(out, C.c_float), C.byref(n),
                                   C.byref(rays)), self._h)
         return {"photons": out[:n.value], "rays": rays.value}
+
+    # -- autotuner --
+    @staticmethod
+    def _report(r) -> dict:
+        return {k: getattr(r, k) for k, _ in r._fields_ if k != "reserved"}
+
+    def autotune_raycast(self, d_rays: int, n: int) -> dict:
+        """Times the ray-cast variants on these device rays and keeps the fastest."""
+        r = TuneReportC()
+        check(lib().bc_autotune_raycast(self._h, C.c_void_p(d_rays), int(n), C.byref(r)), self._h)
+        return self._report(r)
+
+    def autotune_render(self, views) -> dict:
+        """views as for render_batch: times the wave sizes on a sample of the batch."""
+        n = len(views)
+        vc = (ViewC * n)()
+        for i, (k, cam, st) in enumerate(views):
+            vc[i].scene, vc[i].reserved, vc[i].camera, vc[i].settings = int(k), 0, cam.c(), st.c()
+        r = TuneReportC()
+        check(lib().bc_autotune_render(self._h, vc, n, C.byref(r)), self._h)
+        return self._report(r)
 
     # -- differentiable rendering --
     def diff_configure(self, cam: Camera, settings: RenderSettings, albedo_materials, emission_materials=()):

@@ -342,8 +342,8 @@ bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, flo
   return cuda_status(ctx, e, "ray-cast launch");
 }
 
-// Host-buffer ray cast, pipelined: the rays go in chunks of 1 Mi over two
-// streams, so the copy of chunk c+1 in, the kernel on chunk c and the copy of
+// Host-buffer ray cast, pipelined: the rays go in chunks of raycast_chunk rays
+// (default 2 Mi) over two streams, so the copy of chunk c+1 in, the kernel on chunk c and the copy of
 // chunk c-1 out overlap (copy engines and SMs work at the same time).
 bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out, int32_t* prim_out) {
   if (!ctx) return set_error(nullptr, BC_ERR_INVALID_ARG, "NULL context");

@@ -1,0 +1,171 @@
+// Autotuner: chooses a context's tuning options by timing the candidates on the
+// caller's own work, then keeps the fastest. No counterpart in the reference,
+// whose OpenCL path picks a work-group size once (gpu_opencl_windows.go:285-304).
+//
+//   ray cast: the register budget of the exact kernels (raycast_minblocks 1, 6, 8)
+//             and the coherent ray order (raycast_sort 0, 1); plain fp32 mode has
+//             the order only. CUDA events on the context's stream, best of two
+//             runs after one warm-up, on the caller's rays.
+//   render:   paths per wave (render_wave_cap 2^22 .. 2^26) on the caller's
+//             batch, with spp scaled down so one candidate traces at most
+//             2^27 paths. Images do not depend on the wave size, so no candidate
+//             changes a result.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "context.h"
+#include "kernels.h"
+#include "wave.h"
+
+namespace bcgx {
+
+bc_status batch_requests(bc_context* ctx, const bc_view* views, int32_t n_views, std::vector<ViewRequest>* req,
+                         long long* px);  // render.cu
+
+static bc_status time_raycast(bc_context* ctx, const float* d_rays, int64_t n, float* t, int32_t* p, float* ms) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaEventCreate(&a);
+  if (!e) e = cudaEventCreate(&b);
+  float best = 0.0f;
+  for (int k = 0; k < 3 && !e; k++) {
+    e = cudaEventRecord(a, ctx->stream);
+    if (e) break;
+    bc_status st = bc_raycast_device(ctx, d_rays, n, t, p, ctx->stream);
+    if (st) {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      return st;
+    }
+    e = cudaEventRecord(b, ctx->stream);
+    if (!e) e = cudaEventSynchronize(b);
+    float m = 0.0f;
+    if (!e) e = cudaEventElapsedTime(&m, a, b);
+    if (k == 1 || (k == 2 && m < best)) best = m;  // run 0 warms up
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (e) return cuda_status(ctx, e, "autotune timing");
+  *ms = best;
+  return check_kernel_status(ctx);
+}
+
+}  // namespace bcgx
+
+using namespace bcgx;
+
+extern "C" {
+
+bc_status bc_autotune_raycast(bc_context* ctx, const float* d_rays, int64_t n, bc_tune_report* out) {
+  if (!ctx || !d_rays || n < 1) return set_error(ctx, BC_ERR_INVALID_ARG, "NULL argument or no rays");
+  if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
+  cudaSetDevice(ctx->device);
+  cudaError_t e = ctx->d_t.ensure((size_t)n * 4);
+  if (!e) e = ctx->d_prim.ensure((size_t)n * 4);
+  if (e) return cuda_status(ctx, e, "autotune buffers");
+  struct Cand { int minblocks, sort; };
+  std::vector<Cand> cands;
+  if (ctx->raycast_exact) {
+    for (int mb : {6, 8, 1})
+      for (int so : {1, 0}) cands.push_back(Cand{mb, so});
+  } else {
+    cands = {Cand{ctx->raycast_minblocks, 1}, Cand{ctx->raycast_minblocks, 0}};
+  }
+  const int keep_mb = ctx->raycast_minblocks, keep_sort = ctx->raycast_sort;
+  bc_tune_report rep;
+  std::memset(&rep, 0, sizeof(rep));
+  int best = -1;
+  for (size_t i = 0; i < cands.size(); i++) {
+    ctx->raycast_minblocks = cands[i].minblocks;
+    ctx->raycast_variant = ctx->raycast_exact ? cands[i].minblocks : 0;
+    ctx->raycast_sort = cands[i].sort;
+    float ms = 0.0f;
+    bc_status st = time_raycast(ctx, d_rays, n, ctx->d_t.as<float>(), ctx->d_prim.as<int32_t>(), &ms);
+    if (st) {  // leave the options as they were
+      ctx->raycast_minblocks = keep_mb;
+      ctx->raycast_variant = ctx->raycast_exact ? keep_mb : 0;
+      ctx->raycast_sort = keep_sort;
+      return st;
+    }
+    rep.n_timed++;
+    if (cands[i].minblocks == keep_mb && cands[i].sort == keep_sort) rep.default_ms = ms;
+    if (best < 0 || ms < rep.best_ms) {
+      best = (int)i;
+      rep.best_ms = ms;
+    }
+    if (ms > rep.worst_ms) rep.worst_ms = ms;
+  }
+  ctx->raycast_minblocks = cands[best].minblocks;
+  ctx->raycast_variant = ctx->raycast_exact ? cands[best].minblocks : 0;
+  ctx->raycast_sort = cands[best].sort;
+  rep.raycast_minblocks = ctx->raycast_minblocks;
+  rep.raycast_sort = ctx->raycast_sort;
+  rep.render_wave_cap = ctx->render_wave_cap;
+  if (out) *out = rep;
+  return BC_OK;
+}
+
+bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_views, bc_tune_report* out) {
+  if (!ctx || !views || n_views < 1) return set_error(ctx, BC_ERR_INVALID_ARG, "NULL argument or no views");
+  cudaSetDevice(ctx->device);
+  std::vector<ViewRequest> req;
+  long long px = 0;
+  bc_status st = batch_requests(ctx, views, n_views, &req, &px);
+  if (st) return st;
+  // a bounded sample of the batch: every view keeps its size and bounces, its
+  // spp scales so the sample traces at most 2^27 paths; no adaptive stop
+  long long total = 0;
+  for (const ViewRequest& r : req) total += (long long)r.s.width * r.s.height * effective_spp(r.s);
+  const double f = std::min(1.0, (double)(1LL << 27) / (double)std::max(1LL, total));
+  long long sample = 0;
+  for (ViewRequest& r : req) {
+    const int spp = std::max(1, (int)((double)effective_spp(r.s) * f));
+    r.s.spp = spp;
+    r.s.msaa = 1;
+    r.s.tsaa = 0;
+    r.s.adaptive_sampling = 0;
+    sample += (long long)r.s.width * r.s.height * spp;
+  }
+  const long long keep = ctx->render_wave_cap;
+  bc_tune_report rep;
+  std::memset(&rep, 0, sizeof(rep));
+  long long best_cap = keep;
+  std::vector<long long> caps;
+  for (int lg = 22; lg <= 26; lg++) {
+    const long long cap = 1LL << lg;
+    if (cap > 2 * sample && lg > 22) break;  // larger waves than the work: the same launches
+    caps.push_back(cap);
+  }
+  if (std::find(caps.begin(), caps.end(), keep) == caps.end()) caps.push_back(keep);
+  for (const long long cap : caps) {
+    ctx->render_wave_cap = cap;
+    double ms = 0.0;
+    for (int k = 0; k < 2; k++) {  // the first run may allocate and capture the wave graph
+      const auto t0 = std::chrono::steady_clock::now();
+      int64_t rays = 0;
+      st = render_views(ctx, req, (size_t)px, &rays, nullptr);
+      if (st) {
+        ctx->render_wave_cap = keep;
+        return st;
+      }
+      ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    rep.n_timed++;
+    if (cap == keep) rep.default_ms = ms;
+    if (rep.best_ms == 0.0 || ms < rep.best_ms) {
+      rep.best_ms = ms;
+      best_cap = cap;
+    }
+    if (ms > rep.worst_ms) rep.worst_ms = ms;
+  }
+  ctx->render_wave_cap = best_cap;
+  rep.raycast_minblocks = ctx->raycast_minblocks;
+  rep.raycast_sort = ctx->raycast_sort;
+  rep.render_wave_cap = best_cap;
+  if (out) *out = rep;
+  return BC_OK;
+}
+
+}  // extern "C"

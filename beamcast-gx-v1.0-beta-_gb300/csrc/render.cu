@@ -1689,6 +1689,29 @@ bc_status ensure_post_scratch(bc_context* ctx, int px, PostTargets* t) {
   return BC_OK;
 }
 
+// The whole-frame requests of a batch of views, laid out one after another in
+// the frame buffers; *px = pixels of the batch.
+bc_status batch_requests(bc_context* ctx, const bc_view* views, int32_t n_views, std::vector<ViewRequest>* req,
+                         long long* px) {
+  req->assign(n_views, ViewRequest());
+  *px = 0;
+  for (int v = 0; v < n_views; v++) {
+    ViewRequest& r = (*req)[v];
+    r.scene = views[v].scene;
+    r.cam = views[v].camera;
+    r.s = views[v].settings;
+    r.y0 = 0;
+    r.rows = r.s.height;
+    r.pix_off = *px;
+    r.want_guides = false;
+    if (r.s.width < 1 || r.s.height < 1 || (int64_t)r.s.width * r.s.height > (1 << 26))
+      return set_error(ctx, BC_ERR_INVALID_ARG, "invalid render size in view " + std::to_string(v));
+    *px += (long long)r.s.width * r.s.height;
+  }
+  if (*px > (1LL << 30)) return set_error(ctx, BC_ERR_INVALID_ARG, "batch holds more than 2^30 pixels");
+  return BC_OK;
+}
+
 }  // namespace bcgx
 
 using namespace bcgx;
@@ -1767,22 +1790,10 @@ bc_status bc_render_batch(bc_context* ctx, const bc_view* views, int32_t n_views
                           int64_t* rays_out) {
   if (!ctx || !views || n_views < 1) return set_error(ctx, BC_ERR_INVALID_ARG, "NULL argument or no views");
   cudaSetDevice(ctx->device);
-  std::vector<ViewRequest> req(n_views);
+  std::vector<ViewRequest> req;
   long long px = 0;
-  for (int v = 0; v < n_views; v++) {
-    ViewRequest& r = req[v];
-    r.scene = views[v].scene;
-    r.cam = views[v].camera;
-    r.s = views[v].settings;
-    r.y0 = 0;
-    r.rows = r.s.height;
-    r.pix_off = px;
-    r.want_guides = false;
-    if (r.s.width < 1 || r.s.height < 1 || (int64_t)r.s.width * r.s.height > (1 << 26))
-      return set_error(ctx, BC_ERR_INVALID_ARG, "invalid render size in view " + std::to_string(v));
-    px += (long long)r.s.width * r.s.height;
-  }
-  if (px > (1LL << 30)) return set_error(ctx, BC_ERR_INVALID_ARG, "batch holds more than 2^30 pixels");
+  bc_status bst = batch_requests(ctx, views, n_views, &req, &px);
+  if (bst) return bst;
   int64_t rays = 0;
   bc_status st = render_views(ctx, req, (size_t)px, &rays, nullptr);
   if (st) return st;

@@ -204,6 +204,7 @@ def run_gpu(args):
     d_p = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     torch.cuda.synchronize()
+    tune = ctx.autotune_raycast(d_rays.data_ptr(), N_RAYS) if args.autotune else None
 
     def step():
         ctx.raycast_device(d_rays.data_ptr(), N_RAYS, d_t.data_ptr(), d_p.data_ptr(), stream.cuda_stream)
@@ -274,6 +275,7 @@ def run_gpu(args):
         "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays_per_gpu": N_RAYS,
                    "l2": "flushed between steps (256 MiB write)", "bvh8_nodes": stats["nodes8"],
                    "bvh8_depth": stats["depth8"], "scene_bytes": stats["device_bytes"]},
+        "autotune": tune,
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": N_RAYS * 32,
                 "d2h_bytes_per_step": N_RAYS * 8},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -465,6 +467,7 @@ def run_batch(args):
             r += ctx.render_batch([v], readback=False)[1]
         return time.perf_counter() - t, r
 
+    tune = ctx.autotune_render(views) if args.autotune else None
     for _ in range(args.warmup):
         batched()
     plain()
@@ -508,6 +511,7 @@ def run_batch(args):
             "plain": {"value": plain_v, "unit": METRIC, "ms_per_step": 1e3 * sum(pt) / args.steps,
                       "form": f"{n_views} sequential one-view bc_render_batch calls"},
             "batched_over_plain": value / plain_v,
+            "autotune": tune,
             "plain_one_kernel": kernel_form,
             "batched_over_one_kernel": (value / kernel_form["value"]) if kernel_form else None,
             "e2e": {"value": e2e_r / e2e_t / 1e6, "unit": METRIC, "h2d_bytes_per_step": 0,
@@ -849,6 +853,8 @@ def main():
     ap.add_argument("--adaptive", type=float, default=None,
                     help="render workloads: turn the adaptive stop on with this threshold (Ultra preset: 8e-5)")
     ap.add_argument("--wave-cap", type=int, default=0, help="render workloads: paths per wave (0 = library default)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="raycast and batch workloads: run the autotuner on the workload before timing")
     ap.add_argument("--plain-steps", type=int, default=2,
                     help="render workloads: frames timed with the one-kernel form (0 = skip)")
     args = ap.parse_args()

@@ -430,6 +430,29 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
 bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value);
 bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value);
 
+/*
+ * Autotuner: times the candidate values of the tuning options on the caller's
+ * own work and keeps the fastest in the context (no counterpart in the
+ * reference). Results never depend on the options: every candidate returns the
+ * same hits and images.
+ *
+ * bc_autotune_raycast: device rays as for bc_raycast_device; candidates are
+ * raycast_minblocks 6, 8, 1 with raycast_sort 1 and 0 (exact mode; plain fp32
+ * mode: raycast_sort only). Best of two timed runs each (CUDA events).
+ * bc_autotune_render: the views as for bc_render_batch; candidates are
+ * render_wave_cap 2^22 .. 2^26 (up to twice the sample's paths). Each view's
+ * spp is scaled down so that a candidate traces at most 2^27 paths; the
+ * adaptive stop is off while timing. The second of two runs is timed.
+ */
+typedef struct bc_tune_report {
+  int32_t raycast_minblocks, raycast_sort;  /* options in force after the call */
+  int64_t render_wave_cap;
+  int32_t n_timed, reserved;                /* candidates timed */
+  double best_ms, default_ms, worst_ms;     /* chosen, the options before the call, slowest */
+} bc_tune_report;
+bc_status bc_autotune_raycast(bc_context* ctx, const float* d_rays, int64_t n, bc_tune_report* out);
+bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_views, bc_tune_report* out);
+
 /* Request cancellation of the running or next render of ctx; safe from any thread. */
 bc_status bc_cancel(bc_context* ctx);
 /* Clear a pending cancellation. */

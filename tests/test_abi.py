@@ -51,7 +51,8 @@ def test_struct_layouts_match_the_header(native_lib, tmp_path):
     offsets (a field added to the header must be added to the mirror)."""
     from bcgx import _lib
     pairs = [("bc_scene_desc", _lib.SceneDesc), ("bc_camera", _lib.CameraC), ("bc_settings", _lib.SettingsC),
-             ("bc_view", _lib.ViewC), ("bc_diff_desc", _lib.DiffDescC), ("bc_post_desc", _lib.PostDescC)]
+             ("bc_view", _lib.ViewC), ("bc_diff_desc", _lib.DiffDescC), ("bc_post_desc", _lib.PostDescC),
+             ("bc_tune_report", _lib.TuneReportC)]
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "bc_gx.h"', "int main(void) {"]
     for cname, py in pairs:
         lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')

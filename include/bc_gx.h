@@ -415,7 +415,7 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *                        between two streams, so one chunk's copies overlap
  *                        another's kernel.
  *   "render_wave_cap"    paths in flight per wave of the renderer, 4096 .. 2^27
- *                        (default 2^25: ~160 bytes of device memory per path,
+ *                        (default 2^26: ~160 bytes of device memory per path,
  *                        allocated up to what a render needs); images do not
  *                        depend on it. Each wave ends in a latency-bound tail of
  *                        long paths, so larger waves render faster.

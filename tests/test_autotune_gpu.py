@@ -55,7 +55,7 @@ def test_autotune_render_keeps_images(gpu_ctx):
         after, _ = gpu_ctx.render_batch(views)
         assert all(np.array_equal(a, b) for a, b in zip(before, after))
     finally:
-        gpu_ctx.set_option("render_wave_cap", 1 << 25)
+        gpu_ctx.set_option("render_wave_cap", 1 << 26)
 
 
 def test_autotune_argument_errors(gpu_ctx):

@@ -160,7 +160,7 @@ def test_chunks_batches_and_engines(gpu_ctx):
         try:
             small = gpu_ctx.render_frame(cam, st_r, want_guides=False, want_rgba=False)["linear"]
         finally:
-            gpu_ctx.set_option("render_wave_cap", 1 << 25)
+            gpu_ctx.set_option("render_wave_cap", 1 << 26)
         assert np.array_equal(small, full_r)
     gpu_ctx.set_option("render_engine", 1)
     try:

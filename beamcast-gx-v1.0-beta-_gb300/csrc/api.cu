@@ -271,7 +271,7 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
     // only the geometry moved: rewrite primitives and node boxes on the device
     st = update_geometry(ctx, *scene);
     if (st == BC_OK) {
-      ctx->ranges[0].diag = scene_diag(*scene);
+      scene_extent(*scene, &ctx->ranges[0]);
       ctx->scene_gen++;  // cached photon maps of the old geometry are stale
       ctx->geom_rev = geometry_rev;
       ctx->stats[6]++;
@@ -286,7 +286,7 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
   SceneRange r;
   r.n_lights = (int32_t)ps.lights.size();
   r.n_slots = ps.n_prims;
-  r.diag = scene_diag(*scene);
+  scene_extent(*scene, &r);
   if ((st = install_scene(ctx, ps, std::vector<SceneRange>{r}))) return st;
   if ((st = keep_geometry_map(ctx, *scene, ps))) return st;
   ctx->is_set = false;
@@ -437,6 +437,11 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     ctx->raycast_sort = (int)value;
     return BC_OK;
   }
+  if (n == "photon_grid") {
+    if (value != 0 && value != 1) return set_error(ctx, BC_ERR_INVALID_ARG, "photon_grid must be 0 or 1");
+    ctx->photon_grid = (int)value;
+    return BC_OK;
+  }
   if (n == "raycast_chunk") {
     if (value < 65536 || value > (1LL << 28))
       return set_error(ctx, BC_ERR_INVALID_ARG, "raycast_chunk must be in [65536, 2^28]");
@@ -470,6 +475,7 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
   if (n == "render_wave_cap") { *value = ctx->render_wave_cap; return BC_OK; }
   if (n == "raycast_sort") { *value = ctx->raycast_sort; return BC_OK; }
   if (n == "raycast_chunk") { *value = ctx->raycast_chunk; return BC_OK; }
+  if (n == "photon_grid") { *value = ctx->photon_grid; return BC_OK; }
   if (n == "render_graph") { *value = ctx->render_graph; return BC_OK; }
   if (n == "render_engine") { *value = ctx->render_engine; return BC_OK; }
   return BC_ERR_INVALID_ARG;

@@ -101,6 +101,7 @@ struct bc_context {
   int render_engine = 0;                // 0: wave engine, 1: one kernel per view (bc_set_option "render_engine")
   struct DiffState* diff = nullptr;  // differentiable rendering (diff.cu)
   struct PhotonCache* photons = nullptr;  // photon maps of the photon-mapping integrator (photon.cu)
+  int photon_grid = 1;                    // gathers read the dense cell table (bc_set_option "photon_grid")
   uint64_t scene_gen = 0;                 // bumped by every scene or geometry upload
   // rendering state (render.cu)
   struct RenderBuffers* rb = nullptr;

@@ -12,12 +12,16 @@
 
 namespace bcgx {
 
-double scene_diag(const bc_scene_desc& d) {
-  double e[3] = {2, 2, 2};  // Bounds of a scene without primitives: [-1, 1]^3
-  if (d.n_prims > 0 && d.n_nodes > 0 && d.node_box)
-    for (int k = 0; k < 3; k++) e[k] = d.node_box[3 + k] - d.node_box[k];
+void scene_extent(const bc_scene_desc& d, SceneRange* r) {
+  const bool some = d.n_prims > 0 && d.n_nodes > 0 && d.node_box;
+  double e[3];
+  for (int k = 0; k < 3; k++) {
+    r->lo[k] = some ? d.node_box[k] : -1.0;
+    r->hi[k] = some ? d.node_box[3 + k] : 1.0;
+    e[k] = r->hi[k] - r->lo[k];
+  }
   const double dd = e[0] * e[0] + e[1] * e[1];
-  return std::sqrt(dd + e[2] * e[2]);
+  r->diag = std::sqrt(dd + e[2] * e[2]);
 }
 
 float round_down_f32(double x) { return rd_f32(x); }
@@ -281,7 +285,7 @@ bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::v
     r.n_slots = ps.n_prims;
     r.prim_off = out->n_prims;  // primitive indices and slots share one numbering per scene
     r.mat_off = (int32_t)out->mats.size();
-    r.diag = scene_diag(d[k]);
+    scene_extent(d[k], &r);
     r.light_off = (int32_t)out->lights.size();
     r.n_lights = (int32_t)ps.lights.size();
     if ((int64_t)out->nodes.size() + ps.nodes.size() >= kMaxIndex || (int64_t)out->n_prims + ps.n_prims >= kMaxIndex) {

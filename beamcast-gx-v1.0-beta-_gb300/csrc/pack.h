@@ -35,6 +35,7 @@ struct SceneRange {
   int32_t prim_off = 0;                // added to its primitive indices (slot_prim, light prims)
   int32_t mat_off = 0;
   double diag = 0;                     // length of the scene's bounds diagonal (photon radius)
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // the scene's bounds (photon grid extent)
 };
 
 // Fills `out`; returns BC_OK or BC_ERR_BAD_SCENE / BC_ERR_INVALID_ARG with a message.
@@ -47,9 +48,10 @@ bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::v
 // Sphere-light records and per-primitive light selection pdfs of a scene.
 void pack_scene_lights(const bc_scene_desc& d, PackedScene* out);
 
-// |Scene.Bounds().Max - Min| (renderer.go:1137-1146, 1164-1165): the root node
-// box is the union of the primitive boxes; an empty scene has the unit cube's.
-double scene_diag(const bc_scene_desc& d);
+// Scene.Bounds() (renderer.go:1137-1146) into r->lo / r->hi and the length of its
+// diagonal (1164-1165) into r->diag: the root node box is the union of the
+// primitive boxes; a scene without primitives has [-1, 1]^3.
+void scene_extent(const bc_scene_desc& d, SceneRange* r);
 
 float round_down_f32(double x);
 float round_up_f32(double x);

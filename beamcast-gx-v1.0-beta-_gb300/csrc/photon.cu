@@ -12,6 +12,7 @@
 // then sorts the photons by (cell key, append index) and builds the table that
 // the gather looks keys up in.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -214,17 +215,24 @@ __global__ void __launch_bounds__(1024) k_photon_scan(const int* __restrict__ co
 
 // Sorts the photons by (cell key, append index) (bitonic sort of the padded
 // power of two), lists the distinct keys with their runs, gathers the photons
-// into sorted order and fills the lookup table. One block.
+// into sorted order, fills the lookup table and writes the dense table's box
+// (the photons' cells and two more each side; no dense table when it would
+// hold more than max_cells cells). One block.
 __global__ void __launch_bounds__(1024) k_photon_grid(const int* __restrict__ header, int p2max,
                                                       const unsigned long long* __restrict__ key,
                                                       const float4* __restrict__ pos_u, const float4* __restrict__ nrm_u,
                                                       const float4* __restrict__ flux_u, unsigned long long* skey,
                                                       int* sidx, unsigned long long* ukey, int2* span, float4* pos,
-                                                      float4* nrm, float4* flux, int* table, int tsize,
-                                                      unsigned* status) {
+                                                      float4* nrm, float4* flux, int* table, int tsize, float cell,
+                                                      long long max_cells, PhotonGrid* grid, unsigned* status) {
   __shared__ int sm[32];
+  __shared__ long long cmin[3], cmax[3];
   const int t = threadIdx.x;
   const int n = header[0];
+  if (t < 3) {
+    cmin[t] = LLONG_MAX;
+    cmax[t] = LLONG_MIN;
+  }
   int P2 = 2;
   while (P2 < n) P2 <<= 1;
   if (P2 > p2max) {  // cannot happen: n <= budget + max_bounces - 1 <= p2max
@@ -273,7 +281,32 @@ __global__ void __launch_bounds__(1024) k_photon_grid(const int* __restrict__ he
     flux[i] = flux_u[s];
   }
   for (int s = t; s < tsize; s += 1024) table[s] = 0;
+  long long clo[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, chi[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
+  for (int i = t; i < n; i += 1024) {  // cells of the photons, as the keys were formed
+    const float4 P = pos_u[i];
+    const long long c[3] = {(long long)floorf(P.x / cell), (long long)floorf(P.y / cell), (long long)floorf(P.z / cell)};
+    for (int a = 0; a < 3; a++) {
+      clo[a] = min(clo[a], c[a]);
+      chi[a] = max(chi[a], c[a]);
+    }
+  }
+  for (int a = 0; a < 3; a++) {
+    atomicMin(&cmin[a], clo[a]);
+    atomicMax(&cmax[a], chi[a]);
+  }
   __syncthreads();
+  if (t == 0) {
+    bool ok = n > 0 && max_cells > 0;
+    double cells = 1.0;
+    for (int a = 0; a < 3 && ok; a++) {
+      const long long d = cmax[a] - cmin[a] + 5;
+      ok = d > 0 && d < (1LL << 30);
+      cells *= (double)d;
+      grid->g0[a] = cmin[a] - 2;
+      grid->dim[a] = ok ? (int)d : 0;
+    }
+    if (!ok || cells > (double)max_cells) grid->dim[0] = 0;
+  }
   for (int v = t; v < n_keys; v += 1024) {
     const int first = span[v].x;
     span[v].y = (v + 1 < n_keys ? span[v + 1].x : n) - first;
@@ -284,6 +317,23 @@ __global__ void __launch_bounds__(1024) k_photon_grid(const int* __restrict__ he
       if (atomicCAS(&table[h], 0, v + 1) == 0) break;
       h = (h + 1) & (uint32_t)(tsize - 1);
     }
+  }
+}
+
+}  // namespace bcgx
+
+namespace bcgx {
+
+// The dense table: the run of every cell of the box, looked up in the hash
+// table exactly as a gather would look the cell up.
+__global__ void k_photon_dense(PhotonView pm, const PhotonGrid* __restrict__ grid, int* __restrict__ dense) {
+  const int gx = grid->dim[0];
+  if (gx == 0) return;
+  const int gy = grid->dim[1], gz = grid->dim[2];
+  const long long total = (long long)gx * gy * gz;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const long long x = i % gx, y = (i / gx) % gy, z = i / ((long long)gx * gy);
+    dense[i] = photon_cell_lookup(pm, photon_cell_key(grid->g0[0] + x, grid->g0[1] + y, grid->g0[2] + z));
   }
 }
 
@@ -360,13 +410,20 @@ static bc_status build_entry(bc_context* ctx, int scene, const bc_settings& s, P
   if (radius <= 1e-4) radius = 0.25;
   p.attempts = budget * 6;
   p.np = budget + p.max_bounces;  // the last emission may overshoot the budget by max_bounces - 1
+  // dense table: photons lie in the scene bounds (a cell of slack per side for
+  // fp32 hit points); larger than 2^22 cells, the hash serves alone
+  double cells = 1.0;
+  for (int a = 0; a < 3; a++)
+    cells *= std::floor(sr.hi[a] / radius) - std::floor(sr.lo[a] / radius) + 7.0;
+  const long long max_cells = (cells >= 1.0 && cells <= (double)(1 << 22)) ? (long long)cells : 0;
   int p2max = 2;
   while (p2max < p.np) p2max <<= 1;
   const int tsize = 2 * p2max;
   const size_t a = (size_t)p.attempts, np = (size_t)p.np, p2 = (size_t)p2max;
   const size_t bytes = 4 * 256 + ((a * 4 + 255) / 256) * 256 * 2 + ((np * 16 + 255) / 256) * 256 * 6 +
                        ((np * 8 + 255) / 256) * 256 * 2 + ((p2 * 8 + 255) / 256) * 256 +
-                       ((p2 * 4 + 255) / 256) * 256 + ((np * 8 + 255) / 256) * 256 + ((tsize * 4 + 255) / 256) * 256;
+                       ((p2 * 4 + 255) / 256) * 256 + ((np * 8 + 255) / 256) * 256 + ((tsize * 4 + 255) / 256) * 256 +
+                       256 + (((size_t)max_cells * 4 + 255) / 256) * 256;
   cudaError_t e = cudaMalloc(&p.mem, bytes);
   if (e) {
     p.mem = nullptr;
@@ -389,6 +446,8 @@ static bc_status build_entry(bc_context* ctx, int scene, const bc_settings& s, P
   float4* nrm = take<float4>(c, np);
   float4* flux = take<float4>(c, np);
   int* table = take<int>(c, tsize);
+  PhotonGrid* grid = take<PhotonGrid>(c, 1);
+  int* dense = max_cells ? take<int>(c, (size_t)max_cells) : nullptr;
   p.pos_u = pos_u;
   p.nrm_u = nrm_u;
   p.flux_u = flux_u;
@@ -426,7 +485,16 @@ static bc_status build_entry(bc_context* ctx, int scene, const bc_settings& s, P
   }
   if (!e) {
     k_photon_grid<<<1, 1024, 0, st>>>(p.header, p2max, key, pos_u, nrm_u, flux_u, skey, sidx, ukey, span, pos, nrm,
-                                      flux, table, tsize, ctx->d_status);
+                                      flux, table, tsize, (float)radius, max_cells, grid, ctx->d_status);
+    e = cudaGetLastError();
+  }
+  PhotonView hv{};
+  hv.ukey = ukey;
+  hv.table = table;
+  hv.mask = tsize - 1;
+  if (!e && dense) {
+    const int blocks = (int)std::min<long long>(1024, (max_cells + 255) / 256);
+    k_photon_dense<<<blocks, 256, 0, st>>>(hv, grid, dense);
     e = cudaGetLastError();
   }
   if (e) {
@@ -443,6 +511,8 @@ static bc_status build_entry(bc_context* ctx, int scene, const bc_settings& s, P
   p.view.cell = (float)radius;
   p.view.r2 = (float)(radius * radius);
   p.view.pir2 = (float)(M_PI * radius * radius);
+  p.view.grid = dense ? grid : nullptr;
+  p.view.dense = dense;
   return BC_OK;
 }
 
@@ -500,6 +570,10 @@ bc_status photon_map_for(bc_context* ctx, int scene, const bc_settings& s, uint6
   bc_status st = photon_entry(ctx, scene, s, pin, &p, built_rays);
   if (st) return st;
   *view = p->view;  // an empty map has a null table
+  if (!ctx->photon_grid) {
+    view->grid = nullptr;
+    view->dense = nullptr;
+  }
   return BC_OK;
 }
 

@@ -410,6 +410,9 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *                        in a spatially coherent order (origin Morton code on a
  *                        64^3 grid over the scene bounds, then direction octant);
  *                        results are returned in the caller's order either way.
+ *   "photon_grid"        1 (default): photon gathers find a cell's photons in a
+ *                        dense cell table built with the map; 0: by hash lookup.
+ *                        Both give the same photons in the same order.
  *   "raycast_chunk"      rays per chunk of bc_raycast (host buffers),
  *                        65,536 .. 2^28 (default 2^21): chunks alternate
  *                        between two streams, so one chunk's copies overlap

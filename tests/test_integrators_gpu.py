@@ -268,3 +268,19 @@ def test_recursive_with_adaptive_stop(gpu_ctx, cornell):
     m_c = ref.render(cam, st, seed=81, threads=0)["linear"]
     close = np.all(np.abs(m_g - m_c) <= 2e-3 * (1 + np.abs(m_c)), axis=2)
     assert close.mean() > 0.95, f"only {close.mean():.4f} of pixels replay the CPU paths"
+
+
+def test_dense_photon_table_equals_hash_lookups(gpu_ctx):
+    """Gathers through the dense cell table and through the hash table visit the
+    same photons in the same order: bit-identical photon renders at every level."""
+    spec, cam = scenes.cornell_reference_scene()
+    gpu_ctx.upload(scenes.to_scene(spec))
+    for level in (1, 2, 3, 4):
+        st = _settings(PHOTON, w=64, h=48, spp=4, bounces=5, level=level, seed=90 + level)
+        dense = gpu_ctx.render_frame(cam, st, want_guides=False, want_rgba=False)["linear"]
+        gpu_ctx.set_option("photon_grid", 0)
+        try:
+            hashed = gpu_ctx.render_frame(cam, st, want_guides=False, want_rgba=False)["linear"]
+        finally:
+            gpu_ctx.set_option("photon_grid", 1)
+        assert np.array_equal(dense, hashed), level

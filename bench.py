@@ -282,7 +282,8 @@ def run_gpu(args):
                      "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_ray": bytes_per_ray, **counters},
         "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
-        "gpu_launches": args.steps,
+        # per step: the trace kernel, plus the four ray-order kernels (keys, two scans, scatter)
+        "gpu_launches": args.steps * (5 if ctx.get_option("raycast_sort") and N_RAYS >= 65536 else 1),
         "raycast_minblocks": ctx.get_option("raycast_minblocks"),
         "raycast_exact": ctx.get_option("raycast_exact"),
         "clocks": clk,

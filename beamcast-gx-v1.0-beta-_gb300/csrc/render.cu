@@ -1099,6 +1099,7 @@ struct RenderBuffers {
   // one wave as an instantiated CUDA graph, and the launch arguments it was captured with
   cudaGraphExec_t graph = nullptr;
   std::vector<uintptr_t> graph_key;
+  std::vector<uintptr_t> single_key;  // last single-wave render launched without a graph
 };
 
 namespace bcgx {
@@ -1355,7 +1356,10 @@ static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const Shad
   WaveShape w = wave_shape<STACK, SPH>(rb->cap, bounces, lights, grad);
   w.recursive = recursive;
   w.alt = alt;
-  const bool use_graph = ctx->render_graph != 0 && n_waves > 1;
+  // A wave graph pays for its capture when a render has several waves, or when
+  // a single-wave render repeats with the same launches (a frame loop at fixed
+  // settings): such a render is captured the second time its key is seen.
+  bool use_graph = ctx->render_graph != 0;
   if (use_graph) {
     // every value the captured launches were given
     std::vector<uintptr_t> key = {(uintptr_t)STACK, (uintptr_t)SPH, (uintptr_t)bounces, (uintptr_t)lights,
@@ -1382,7 +1386,10 @@ static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const Shad
       add_bytes(grad, sizeof(*grad));
       add_bytes(&rb->grec, sizeof(rb->grec));
     }
-    if (!rb->graph || rb->graph_key != key) {
+    if (n_waves == 1 && !(rb->graph && rb->graph_key == key) && rb->single_key != key) {
+      rb->single_key = key;  // first sighting: launch directly
+      use_graph = false;
+    } else if (!rb->graph || rb->graph_key != key) {
       if (rb->graph) cudaGraphExecDestroy(rb->graph);
       rb->graph = nullptr;
       rb->graph_key.clear();

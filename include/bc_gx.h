@@ -423,7 +423,9 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *                        depend on it. Each wave ends in a latency-bound tail of
  *                        long paths, so larger waves render faster.
  *   "render_graph"       1 (default): a render of several waves replays one
- *                        captured CUDA graph per wave; 0: plain stream launches.
+ *                        captured CUDA graph per wave, and a single-wave render
+ *                        is captured when the same launches repeat (from the
+ *                        second identical call on); 0: plain stream launches.
  *   "render_engine"      0 (default): the wave engine; 1: one kernel launch per
  *                        view, one thread per pixel looping over samples and
  *                        bounces (the reference OpenCL kernel's shape, kept as the

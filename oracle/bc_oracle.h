@@ -135,6 +135,11 @@ struct Settings {
   int integrator = 0;      // IntegratorMode (renderer.go:1002-1006): 0 path, 1 recursive, 2 photon
   int photon_mapping = 0;  // RenderSettings.PhotonMapping level (photon budget and radius)
   int64_t photon_seed = -1;  // seed of the photon map's emission streams; < 0: the render seed
+  // pixel window [win_x, win_x + win_w) x [win_y, win_y + win_h) of the frame;
+  // win_w == 0 renders the whole frame. Pixels keep their frame coordinates
+  // (camera ray, sample rotation, RNG stream), so a window equals that part of
+  // the whole frame.
+  int win_x = 0, win_y = 0, win_w = 0, win_h = 0;
 };
 enum Integrator { IntegratorPath = 0, IntegratorRecursive = 1, IntegratorPhoton = 2 };
 int effective_spp(const Settings& s);  // renderer.go:2395
@@ -207,7 +212,8 @@ struct RenderOut {
   Counters c;
 };
 // Tile-parallel render shaped like RenderState.Start's CPU path
-// (renderer.go:2692-2826): center-first tiles, one-tile atomic claims.
+// (renderer.go:2692-2826): center-first tiles, one-tile atomic claims. With a
+// window (Settings::win_w > 0) the outputs hold the window's pixels, row-major.
 void render(const Scene& s, const Camera& cam, const Settings& st, uint64_t seed, int threads,
             RenderOut* out, const std::atomic<bool>* cancel);
 

@@ -316,14 +316,13 @@ void orc_camera_basis(const double* cam10, double aspect, double* out12) {
 // Render: linear3 = per-pixel mean, sumsq3 = per-pixel mean of squares,
 // guides11 = (p3, n3, albedo3, depth, valid) or NULL,
 // stats6 = (segments, shadow rays, box tests, tri tests, sphere tests, photon map rays).
-int orc_render(void* sp, const double* cam10, const orc_settings* cs, uint64_t seed, int threads, double* linear3,
-               double* sumsq3, double* guides11, int64_t* stats6) {
+static int render_to(void* sp, const double* cam10, const Settings& st, uint64_t seed, int threads, double* linear3,
+                     double* sumsq3, double* guides11, int64_t* stats6) {
   Scene* s = (Scene*)sp;
-  Settings st = load_settings(cs);
   Camera cam{ld3(cam10), ld3(cam10 + 3), ld3(cam10 + 6), cam10[9]};
   RenderOut out;
   render(*s, cam, st, seed, threads, &out, nullptr);
-  size_t np = (size_t)st.width * st.height;
+  size_t np = out.linear.size();
   for (size_t i = 0; i < np; i++) {
     st3(linear3 + 3 * i, out.linear[i]);
     if (sumsq3) st3(sumsq3 + 3 * i, out.sumsq[i]);
@@ -338,6 +337,20 @@ int orc_render(void* sp, const double* cam10, const orc_settings* cs, uint64_t s
     stats6[4] = out.c.spheres; stats6[5] = out.photon_rays;
   }
   return 0;
+}
+int orc_render(void* sp, const double* cam10, const orc_settings* cs, uint64_t seed, int threads, double* linear3,
+               double* sumsq3, double* guides11, int64_t* stats6) {
+  return render_to(sp, cam10, load_settings(cs), seed, threads, linear3, sumsq3, guides11, stats6);
+}
+// The pixels [x0, x0 + w) x [y0, y0 + h) of the frame, each as the whole-frame
+// render would give it (outputs hold w*h pixels, row-major). Returns -1 for a
+// window outside the frame.
+int orc_render_window(void* sp, const double* cam10, const orc_settings* cs, int x0, int y0, int w, int h,
+                      uint64_t seed, int threads, double* linear3, double* sumsq3, double* guides11, int64_t* stats6) {
+  Settings st = load_settings(cs);
+  if (x0 < 0 || y0 < 0 || w <= 0 || h <= 0 || x0 + w > st.width || y0 + h > st.height) return -1;
+  st.win_x = x0; st.win_y = y0; st.win_w = w; st.win_h = h;
+  return render_to(sp, cam10, st, seed, threads, linear3, sumsq3, guides11, stats6);
 }
 
 int orc_photon_budget(int level) { return photon_budget(level); }

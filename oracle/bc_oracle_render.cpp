@@ -409,13 +409,21 @@ static V3 adaptive_pixel(const Scene& s, V3 origin, V3 lower, V3 horiz, V3 vert,
 void render(const Scene& s, const Camera& cam, const Settings& st, uint64_t seed, int threads, RenderOut* out,
             const std::atomic<bool>* cancel) {
   int W = st.width, H = st.height;
-  out->linear.assign((size_t)W * H, v3(0, 0, 0));
-  out->sumsq.assign((size_t)W * H, v3(0, 0, 0));
-  out->guides.assign((size_t)W * H, Guide{});
+  // the rendered region: the whole frame or the window, clipped to the frame
+  int rx0 = 0, ry0 = 0, RW = W, RH = H;
+  if (st.win_w > 0 && st.win_h > 0) {
+    rx0 = std::max(0, std::min(st.win_x, W));
+    ry0 = std::max(0, std::min(st.win_y, H));
+    RW = std::min(st.win_w, W - rx0);
+    RH = std::min(st.win_h, H - ry0);
+  }
+  out->linear.assign((size_t)RW * RH, v3(0, 0, 0));
+  out->sumsq.assign((size_t)RW * RH, v3(0, 0, 0));
+  out->guides.assign((size_t)RW * RH, Guide{});
   V3 origin, lower, horiz, vert;
   camera_basis(cam, (double)W / (double)H, &origin, &lower, &horiz, &vert);
   int tile = st.tile > 0 ? st.tile : 16;
-  int tx = (W + tile - 1) / tile, ty = (H + tile - 1) / tile, total = tx * ty;
+  int tx = (RW + tile - 1) / tile, ty = (RH + tile - 1) / tile, total = tx * ty;
   std::vector<int> order = make_tile_order(tx, ty, "Center");
   std::vector<double> SX, SY;
   build_sample_sequence(st, &SX, &SY);
@@ -433,11 +441,11 @@ void render(const Scene& s, const Camera& cam, const Settings& st, uint64_t seed
       if (oi >= total) return;
       if (cancel && cancel->load()) return;
       int ti = order[oi];
-      int x0 = (ti % tx) * tile, y0 = (ti / tx) * tile;
-      int x1 = std::min(x0 + tile, W), y1 = std::min(y0 + tile, H);
+      int x0 = rx0 + (ti % tx) * tile, y0 = ry0 + (ti / tx) * tile;
+      int x1 = std::min(x0 + tile, rx0 + RW), y1 = std::min(y0 + tile, ry0 + RH);
       for (int y = y0; y < y1; y++)
         for (int x = x0; x < x1; x++) {
-          size_t i = (size_t)y * W + x;
+          size_t i = (size_t)(y - ry0) * RW + (x - rx0);
           out->linear[i] = adaptive_pixel(s, origin, lower, horiz, vert, x, y, W, H, st, seed, SX, SY, &per[id],
                                           &out->guides[i], &out->sumsq[i], &pm);
         }

@@ -83,6 +83,8 @@ _SIG = [
     ("orc_clamp_firefly", None, [f64p, C.c_double, f64p]),
     ("orc_camera_basis", None, [f64p, C.c_double, f64p]),
     ("orc_render", C.c_int, [C.c_void_p, f64p, P(OrcSettings), C.c_uint64, C.c_int, f64p, f64p, f64p, i64p]),
+    ("orc_render_window", C.c_int, [C.c_void_p, f64p, P(OrcSettings), C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.c_uint64, C.c_int, f64p, f64p, f64p, i64p]),
     ("orc_photon_budget", C.c_int, [C.c_int]),
     ("orc_photon_cell_key", C.c_uint64, [C.c_int64, C.c_int64, C.c_int64]),
     ("orc_photon_radius", C.c_double, [C.c_void_p, C.c_int]),
@@ -276,15 +278,24 @@ class OracleScene:
     def light_selection_pdf(self, prim, power=True):
         return lib().orc_light_selection_pdf(self.h, int(prim), 1 if power else 0)
 
-    def render(self, cam, st, seed=1, threads=0, tile=8, photon_seed=None):
+    def render(self, cam, st, seed=1, threads=0, tile=8, photon_seed=None, window=None):
         """Returns dict(linear, sumsq, guides (H,W,11), stats). photon_seed: seed of
-        the photon map's emission streams (default: `seed`)."""
+        the photon map's emission streams (default: `seed`). window = (x0, y0, w, h)
+        renders only those pixels of the frame (arrays of shape (h, w, ...)), each
+        equal to the whole frame's pixel."""
         cs = _orc_settings(st, tile, photon_seed)
         cam10 = _f64(list(cam.position) + list(cam.target) + list(cam.up) + [cam.fov])
-        W, H = st.width, st.height
+        W, H = (st.width, st.height) if window is None else (int(window[2]), int(window[3]))
         lin = np.zeros((H, W, 3)); sq = np.zeros((H, W, 3)); g = np.zeros((H, W, 11)); stats = np.zeros(6, np.int64)
-        lib().orc_render(self.h, _p(cam10, C.c_double), C.byref(cs), int(seed), int(threads), _p(lin, C.c_double),
-                         _p(sq, C.c_double), _p(g, C.c_double), _p(stats, C.c_int64))
+        if window is None:
+            lib().orc_render(self.h, _p(cam10, C.c_double), C.byref(cs), int(seed), int(threads),
+                             _p(lin, C.c_double), _p(sq, C.c_double), _p(g, C.c_double), _p(stats, C.c_int64))
+        else:
+            x0, y0 = int(window[0]), int(window[1])
+            if lib().orc_render_window(self.h, _p(cam10, C.c_double), C.byref(cs), x0, y0, W, H, int(seed),
+                                       int(threads), _p(lin, C.c_double), _p(sq, C.c_double), _p(g, C.c_double),
+                                       _p(stats, C.c_int64)) != 0:
+                raise ValueError(f"window {tuple(window)} outside the {st.width}x{st.height} frame")
         return {"linear": lin, "sumsq": sq, "guides": g,
                 "stats": dict(zip(("segments", "shadow", "boxes", "tris", "spheres", "photon_rays"),
                                   stats.tolist()))}

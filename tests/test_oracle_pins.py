@@ -255,3 +255,18 @@ def test_photon_map_properties(orc):
     for lv in (0, 5):
         st.photon_mapping = lv
         assert len(ref.photon_map(st, seed=3)["photons"]) == 0
+
+
+def test_window_render_equals_frame(orc):
+    """A pixel window of the oracle's render (used for converged crops) holds the
+    whole frame's pixels bit for bit, and a window outside the frame is refused."""
+    spec, cam, st = scenes.cornell_box()
+    st.width, st.height, st.spp = 64, 48, 4
+    s = orc.OracleScene.from_spec(spec)
+    full = s.render(cam, st, seed=3, threads=4)
+    win = s.render(cam, st, seed=3, threads=4, window=(10, 7, 21, 13))
+    assert win["linear"].shape == (13, 21, 3)
+    assert np.array_equal(full["linear"][7:20, 10:31], win["linear"])
+    assert np.array_equal(full["sumsq"][7:20, 10:31], win["sumsq"])
+    with pytest.raises(ValueError):
+        s.render(cam, st, window=(60, 0, 10, 4))

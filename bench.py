@@ -311,6 +311,66 @@ def _render_roofline(stats, mseg_per_s):
             "scope": "whole frame (all kernels), not one kernel"}
 
 
+CONVERGED_SPP = 16384
+
+
+def rmse_vs_converged(scene, spec, cam, st, window, conv_spp=CONVERGED_SPP, threads=0):
+    """RMSE of linear HDR radiance (per pixel and channel, post passes off) over a
+    pixel window (x0, y0, w, h), against a converged image of that window
+    rendered by the oracle (fp64 CPU restatement of the reference's integrator)
+    at conv_spp samples per pixel. effectiveSPP caps a render at 4096 samples
+    per pixel (renderer.go:2395-2417), so the converged image is the mean of
+    conv_spp / 4096 renders of 4096 samples with distinct seeds. Reported at the
+    configuration's own spp for the GPU wave engine, the GPU one-kernel form and
+    the oracle (each with its own seed, independent of the converged image's),
+    plus the GPU's own conv_spp image against the oracle's: with agreeing
+    estimators that difference is the two images' residual noise. Equal spp
+    gives equal RMSE when the estimators agree, so throughput ratios at equal
+    spp are ratios at equal RMSE."""
+    import numpy as np
+    import bcgx
+    import oracle
+    x0, y0, w, h = window
+    ref = oracle.OracleScene.from_spec(spec)
+    flat = st.copy()
+    flat.denoise, flat.bloom = False, 0
+    conv = flat.copy()
+    conv.spp = min(conv_spp, 4096)
+    parts = max(1, conv_spp // conv.spp)
+    t0 = time.perf_counter()
+    cpu_conv = sum(ref.render(cam, conv, seed=0xC0417E + k, threads=threads, window=window)["linear"]
+                   for k in range(parts)) / parts
+    conv_s = time.perf_counter() - t0
+    cpu_eq = ref.render(cam, flat, seed=7, threads=threads, window=window)["linear"]
+    ctx = bcgx.Context(0)
+    ctx.upload(scene)
+
+    def gpu(settings):
+        return ctx.render_rows(cam, settings, y0, h)[0][:, x0:x0 + w].astype(np.float64)
+
+    gpu_eq = gpu(flat)
+    ctx.set_option("render_engine", 1)
+    one_kernel = gpu(flat)
+    ctx.set_option("render_engine", 0)
+    gpu_conv = 0.0
+    for k in range(parts):
+        gc = conv.copy()
+        gc.seed = 0x600D + k
+        gpu_conv = gpu_conv + gpu(gc)
+    gpu_conv = gpu_conv / parts
+    ctx.close()
+
+    def rmse(a, b):
+        return float(np.sqrt(np.mean((a - b) ** 2)))
+
+    return {"converged": f"oracle (fp64 CPU), {parts * conv.spp} spp ({parts} x {conv.spp}), {w}x{h} pixels at "
+                         f"({x0}, {y0}) of the {st.width}x{st.height} frame, {conv_s:.0f} s on "
+                         f"{threads or os.cpu_count()} threads",
+            "spp": st.spp, "mean_radiance": float(cpu_conv.mean()),
+            "gpu": rmse(gpu_eq, cpu_conv), "gpu_one_kernel": rmse(one_kernel, cpu_conv),
+            "cpu": rmse(cpu_eq, cpu_conv),
+            f"gpu_{parts * conv.spp}spp_vs_converged": rmse(gpu_conv, cpu_conv)}
+
 def run_render(args):
     """Render workloads (one JSON line each): `cornell` = the Cornell-box
     configuration (320x240, 16 spp, 5 bounces, RR from 3, Halton, MIS, power
@@ -387,7 +447,6 @@ def run_render(args):
     if plain:
         line["plain"] = plain
         line["wave_over_plain"] = value / plain["value"]
-    cpu_img = None
     if not args.no_cpu_baseline:
         import oracle
         ref = oracle.OracleScene.from_spec(spec)
@@ -403,29 +462,12 @@ def run_render(args):
                                 "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"{cst.width}x{cst.height} at {cst.spp} spp, {dt:.1f} s"}
         line["roofline"] = _render_roofline(out["stats"], value)
-        if args.rmse and args.workload == "cornell":
-            c16 = st.copy()
-            cpu_img = ref.render(cam, c16, seed=11, threads=0)["linear"]
     if args.rmse:
-        # converged reference: the parity-validated GPU forward at many samples
-        conv = st.copy()
-        conv.denoise, conv.bloom = False, 0
-        plain = conv.copy()
         if args.workload == "cornell":
-            conv.spp = 16384
-            ref_img = ctx.render_frame(cam, conv, want_guides=False, want_rgba=False)["linear"].astype(np.float64)
-            gpu_img = ctx.render_frame(cam, plain, want_guides=False, want_rgba=False)["linear"].astype(np.float64)
-            r = {"reference": "GPU, 16384 spp, full frame", "gpu_16spp": float(np.sqrt(np.mean((gpu_img - ref_img) ** 2)))}
-            if cpu_img is not None:
-                r["cpu_16spp"] = float(np.sqrt(np.mean((cpu_img - ref_img) ** 2)))
-        else:
-            y0, rows = st.height // 2 - 90, 180
-            conv.spp = 2048
-            ref_rows = ctx.render_rows(cam, conv, y0, rows)[0].astype(np.float64)
-            gpu_rows = ctx.render_rows(cam, plain, y0, rows)[0].astype(np.float64)
-            r = {"reference": f"GPU, 2048 spp, rows {y0}-{y0 + rows} of the frame (2560x180 crop)",
-                 f"gpu_{plain.spp}spp": float(np.sqrt(np.mean((gpu_rows - ref_rows) ** 2)))}
-        line["rmse"] = r
+            window = (0, 0, st.width, st.height)  # the whole frame
+        else:  # a crop of spheres, ground and emitters around the frame centre
+            window = (st.width // 2 - 64, st.height // 2 - 36, 128, 72)
+        line["rmse"] = rmse_vs_converged(scene, spec, cam, st, window)
     print(json.dumps(line), flush=True)
     ctx.close()
     return 0
@@ -538,6 +580,14 @@ def run_batch(args):
         line["cpu_baseline"] = {"value": segs / t_all / 1e6, "unit": METRIC, "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"views 0-3 (one per scene: {', '.join(sample)}) at 1 spp, {t_all:.1f} s"}
         line["roofline"] = _render_roofline(agg, value)
+    if args.rmse:
+        # one view of the 500k-triangle scene; a view renders the same image in a
+        # batch as alone (bit-identical), so this is its RMSE in the batch too
+        v = next(i for i, (k, _, _) in enumerate(views) if k == 3)
+        k, cam, st = views[v]
+        window = (st.width // 2 - 32, st.height // 2 - 32, 64, 64)
+        line["rmse"] = {"view": v, "size": f"{st.width}x{st.height}",
+                        **rmse_vs_converged(built[k], specs[k], cam, st, window)}
     print(json.dumps(line), flush=True)
     ctx.close()
     return 0
@@ -615,6 +665,9 @@ def run_diff(args):
                                 "sample": f"oracle forward 512x512 at 4 spp ({dt:.1f} s, "
                                           f"{out['stats']['segments'] / dt / 1e6:.1f} Mseg/s), scaled to 64 spp; "
                                           "an iteration counted as two forwards (forward + replay)"}
+    if args.rmse:  # the forward's image at the initial parameters
+        st = pb.settings
+        line["rmse"] = rmse_vs_converged(scene, pb.spec, pb.cam, st, (st.width // 2 - 24, st.height // 2 - 24, 48, 48))
     print(json.dumps(line), flush=True)
     ctx.close()
     return 0

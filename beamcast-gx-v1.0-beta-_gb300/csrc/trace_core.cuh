@@ -217,27 +217,42 @@ __device__ __forceinline__ TriClass tri_classify(float4 A, float4 E1, float4 E2,
   return c;
 }
 
+// The fp32 tests below spell every product and sum as a round-to-nearest
+// intrinsic. Left to the compiler, a*b - c*d or a dot product may contract
+// into different fused forms in different kernels (the surrounding code
+// steers the choice), and the wave engine's extend kernel and the one-kernel
+// renderer would then round the same test differently. Spelled out, every
+// kernel that inlines a test computes the same bits, at the instruction count
+// contraction gives.
+__device__ __forceinline__ float fdiff(float a, float b, float c, float d) {  // a b - c d
+  return __fmaf_rn(a, b, -__fmul_rn(c, d));
+}
+__device__ __forceinline__ float fdot(float ax, float ay, float az, float bx, float by, float bz) {
+  return __fmaf_rn(az, bz, __fmaf_rn(ay, by, __fmul_rn(ax, bx)));
+}
+
 // Plain fp32 triangle test for rendering (reference thresholds), with the
 // barycentric and distance tests on the numerators (u det, v det, t det
 // against det), so a missed triangle costs no division.
 __device__ __forceinline__ bool tri_hit32(float4 A, float4 E1, float4 E2, const Ray32& r, float tmax, float* t_out) {
-  const float hx = r.dy * E2.z - r.dz * E2.y;
-  const float hy = r.dz * E2.x - r.dx * E2.z;
-  const float hz = r.dx * E2.y - r.dy * E2.x;
-  const float det = E1.x * hx + E1.y * hy + E1.z * hz;
+  const float hx = fdiff(r.dy, E2.z, r.dz, E2.y);
+  const float hy = fdiff(r.dz, E2.x, r.dx, E2.z);
+  const float hz = fdiff(r.dx, E2.y, r.dy, E2.x);
+  const float det = fdot(E1.x, E1.y, E1.z, hx, hy, hz);
   if (fabsf(det) < 1e-10f) return false;
   const float sd = det > 0.0f ? 1.0f : -1.0f, adet = fabsf(det);
-  const float sx = r.ox - A.x, sy = r.oy - A.y, sz = r.oz - A.z;
-  const float un = sd * (sx * hx + sy * hy + sz * hz);
+  const float sx = __fsub_rn(r.ox, A.x), sy = __fsub_rn(r.oy, A.y), sz = __fsub_rn(r.oz, A.z);
+  const float un = sd * fdot(sx, sy, sz, hx, hy, hz);
   if (un < 0.0f || un > adet) return false;
-  const float qx = sy * E1.z - sz * E1.y;
-  const float qy = sz * E1.x - sx * E1.z;
-  const float qz = sx * E1.y - sy * E1.x;
-  const float vn = sd * (r.dx * qx + r.dy * qy + r.dz * qz);
-  if (vn < 0.0f || un + vn > adet) return false;
-  const float tn = sd * (E2.x * qx + E2.y * qy + E2.z * qz);
-  if (tn < r.tmin * adet || tn > tmax * adet) return false;
-  const float t = (E2.x * qx + E2.y * qy + E2.z * qz) / det;
+  const float qx = fdiff(sy, E1.z, sz, E1.y);
+  const float qy = fdiff(sz, E1.x, sx, E1.z);
+  const float qz = fdiff(sx, E1.y, sy, E1.x);
+  const float vn = sd * fdot(r.dx, r.dy, r.dz, qx, qy, qz);
+  if (vn < 0.0f || __fadd_rn(un, vn) > adet) return false;
+  const float eq = fdot(E2.x, E2.y, E2.z, qx, qy, qz);
+  const float tn = sd * eq;
+  if (tn < __fmul_rn(r.tmin, adet) || tn > __fmul_rn(tmax, adet)) return false;
+  const float t = __fdiv_rn(eq, det);
   if (t < r.tmin || t > tmax) return false;
   *t_out = t;
   return true;
@@ -245,18 +260,18 @@ __device__ __forceinline__ bool tri_hit32(float4 A, float4 E1, float4 E2, const 
 
 // Plain fp32 sphere test (sphereHitAccel in fp32) for rendering.
 __device__ __forceinline__ bool sphere_hit32(float4 C, float4 S, const Ray32& r, float tmax, float* t_out) {
-  const float dl2 = r.dx * r.dx + r.dy * r.dy + r.dz * r.dz;
+  const float dl2 = fdot(r.dx, r.dy, r.dz, r.dx, r.dy, r.dz);
   if (!(dl2 > 1e-18f)) return false;
-  const float ocx = r.ox - C.x, ocy = r.oy - C.y, ocz = r.oz - C.z;
-  const float hb = ocx * r.dx + ocy * r.dy + ocz * r.dz;
-  const float cc = (ocx * ocx + ocy * ocy + ocz * ocz) - S.x;
-  const float disc = hb * hb - dl2 * cc;
+  const float ocx = __fsub_rn(r.ox, C.x), ocy = __fsub_rn(r.oy, C.y), ocz = __fsub_rn(r.oz, C.z);
+  const float hb = fdot(ocx, ocy, ocz, r.dx, r.dy, r.dz);
+  const float cc = __fsub_rn(fdot(ocx, ocy, ocz, ocx, ocy, ocz), S.x);
+  const float disc = fdiff(hb, hb, dl2, cc);
   if (disc < 0.0f) return false;
-  const float sq = sqrtf(disc);
-  const float idl2 = 1.0f / dl2;
-  float root = (-hb - sq) * idl2;
+  const float sq = __fsqrt_rn(disc);
+  const float idl2 = __fdiv_rn(1.0f, dl2);
+  float root = __fmul_rn(__fsub_rn(-hb, sq), idl2);
   if (root < r.tmin || root > tmax) {
-    root = (-hb + sq) * idl2;
+    root = __fmul_rn(__fadd_rn(-hb, sq), idl2);
     if (root < r.tmin || root > tmax) return false;
   }
   *t_out = root;

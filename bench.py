@@ -829,7 +829,8 @@ def run_integrators(args):
         frames(big, 1, 3000)
         bt, br = frames(big, 2, 3100)
         clk = clocks.stop()
-        et, er = frames(st, 1, 4000, readback=True)
+        frames(st, 1, 3900, readback=True)  # the first read-back frame after the large one sets up buffers
+        et, er = frames(st, 5, 4000, readback=True)
         value = rays / sum(times) / 1e6
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,

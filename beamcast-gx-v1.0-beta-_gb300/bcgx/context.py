@@ -195,7 +195,8 @@ class Context:
         return self._report(r)
 
     def autotune_render(self, views) -> dict:
-        """views as for render_batch: times the wave sizes on a sample of the batch."""
+        """views as for render_batch: times the extend-kernel variants, then the wave
+        sizes, on a sample of the batch, and keeps the fastest."""
         n = len(views)
         vc = (ViewC * n)()
         for i, (k, cam, st) in enumerate(views):

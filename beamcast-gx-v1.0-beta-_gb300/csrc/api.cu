@@ -464,6 +464,11 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     ctx->render_engine = (int)value;
     return BC_OK;
   }
+  if (n == "render_extend") {
+    if (value < 0 || value > 2) return set_error(ctx, BC_ERR_INVALID_ARG, "render_extend must be 0, 1 or 2");
+    ctx->render_extend = (int)value;
+    return BC_OK;
+  }
   return set_error(ctx, BC_ERR_INVALID_ARG, "unknown option " + n);
 }
 
@@ -478,6 +483,7 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
   if (n == "photon_grid") { *value = ctx->photon_grid; return BC_OK; }
   if (n == "render_graph") { *value = ctx->render_graph; return BC_OK; }
   if (n == "render_engine") { *value = ctx->render_engine; return BC_OK; }
+  if (n == "render_extend") { *value = ctx->render_extend; return BC_OK; }
   return BC_ERR_INVALID_ARG;
 }
 

@@ -6,10 +6,12 @@
 //             and the coherent ray order (raycast_sort 0, 1); plain fp32 mode has
 //             the order only. CUDA events on the context's stream, best of two
 //             runs after one warm-up, on the caller's rays.
-//   render:   paths per wave (render_wave_cap 2^22 .. 2^26) on the caller's
-//             batch, with spp scaled down so one candidate traces at most
-//             2^27 paths. Images do not depend on the wave size, so no candidate
-//             changes a result.
+//   render:   the extend kernel's variant (render_extend 0, 1, 2: register
+//             budget and where the ray lives, i.e. resident blocks per SM) at
+//             the current wave size, then paths per wave (render_wave_cap
+//             2^22 .. 2^26) with the chosen variant, on the caller's batch with
+//             spp scaled down so one candidate traces at most 2^27 paths.
+//             Images depend on neither option, so no candidate changes a result.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -103,6 +105,7 @@ bc_status bc_autotune_raycast(bc_context* ctx, const float* d_rays, int64_t n, b
   rep.raycast_minblocks = ctx->raycast_minblocks;
   rep.raycast_sort = ctx->raycast_sort;
   rep.render_wave_cap = ctx->render_wave_cap;
+  rep.render_extend = ctx->render_extend;
   if (out) *out = rep;
   return BC_OK;
 }
@@ -129,41 +132,70 @@ bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_vi
     sample += (long long)r.s.width * r.s.height * spp;
   }
   const long long keep = ctx->render_wave_cap;
+  const int keep_ext = ctx->render_extend;
   bc_tune_report rep;
   std::memset(&rep, 0, sizeof(rep));
+  // one timed candidate: the second of two renders of the sample (the first
+  // may allocate and capture the wave graph)
+  auto time_render = [&](double* ms) -> bc_status {
+    for (int k = 0; k < 2; k++) {
+      const auto t0 = std::chrono::steady_clock::now();
+      int64_t rays = 0;
+      const bc_status s = render_views(ctx, req, (size_t)px, &rays, nullptr);
+      if (s) return s;
+      *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    rep.n_timed++;
+    if (*ms > rep.worst_ms) rep.worst_ms = *ms;
+    return BC_OK;
+  };
+  auto restore = [&]() {
+    ctx->render_wave_cap = keep;
+    ctx->render_extend = keep_ext;
+  };
+  // stage 1: the extend variant at the current wave size
+  int best_ext = keep_ext;
+  double best_ext_ms = 0.0;
+  for (int var : {1, 0, 2}) {
+    ctx->render_extend = var;
+    double ms = 0.0;
+    if ((st = time_render(&ms))) {
+      restore();
+      return st;
+    }
+    if (var == keep_ext) rep.default_ms = ms;
+    if (best_ext_ms == 0.0 || ms < best_ext_ms) {
+      best_ext_ms = ms;
+      best_ext = var;
+    }
+  }
+  ctx->render_extend = best_ext;
+  // stage 2: the wave size with that variant
   long long best_cap = keep;
+  rep.best_ms = best_ext_ms;
   std::vector<long long> caps;
   for (int lg = 22; lg <= 26; lg++) {
     const long long cap = 1LL << lg;
     if (cap > 2 * sample && lg > 22) break;  // larger waves than the work: the same launches
-    caps.push_back(cap);
+    if (cap != keep) caps.push_back(cap);
   }
-  if (std::find(caps.begin(), caps.end(), keep) == caps.end()) caps.push_back(keep);
   for (const long long cap : caps) {
     ctx->render_wave_cap = cap;
     double ms = 0.0;
-    for (int k = 0; k < 2; k++) {  // the first run may allocate and capture the wave graph
-      const auto t0 = std::chrono::steady_clock::now();
-      int64_t rays = 0;
-      st = render_views(ctx, req, (size_t)px, &rays, nullptr);
-      if (st) {
-        ctx->render_wave_cap = keep;
-        return st;
-      }
-      ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if ((st = time_render(&ms))) {
+      restore();
+      return st;
     }
-    rep.n_timed++;
-    if (cap == keep) rep.default_ms = ms;
-    if (rep.best_ms == 0.0 || ms < rep.best_ms) {
+    if (ms < rep.best_ms) {
       rep.best_ms = ms;
       best_cap = cap;
     }
-    if (ms > rep.worst_ms) rep.worst_ms = ms;
   }
   ctx->render_wave_cap = best_cap;
   rep.raycast_minblocks = ctx->raycast_minblocks;
   rep.raycast_sort = ctx->raycast_sort;
   rep.render_wave_cap = best_cap;
+  rep.render_extend = best_ext;
   if (out) *out = rep;
   return BC_OK;
 }

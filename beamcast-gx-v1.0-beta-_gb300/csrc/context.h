@@ -99,6 +99,7 @@ struct bc_context {
   long long render_wave_cap = 1 << 26;  // paths per wave (bc_set_option "render_wave_cap")
   int render_graph = 1;                 // replay a captured wave graph (bc_set_option "render_graph")
   int render_engine = 0;                // 0: wave engine, 1: one kernel per view (bc_set_option "render_engine")
+  int render_extend = 1;                // k_extend variant 0..2 (bc_set_option "render_extend")
   struct DiffState* diff = nullptr;  // differentiable rendering (diff.cu)
   struct PhotonCache* photons = nullptr;  // photon maps of the photon-mapping integrator (photon.cu)
   int photon_grid = 1;                    // gathers read the dense cell table (bc_set_option "photon_grid")

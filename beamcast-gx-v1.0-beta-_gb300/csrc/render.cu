@@ -252,15 +252,22 @@ __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __r
 
 // ---- extend ----------------------------------------------------------------
 // Persistent: a lane whose ray is done takes the next queue entry at once (one
-// atomic per warp for all lanes that need work). Register budget: 48 (ten
-// 128-thread blocks per SM, 62.5% occupancy; ptxas spills 10 bytes), where
-// unconstrained it takes 51 (nine blocks). The latency-bound walk gains more
-// from the extra warps than the spill costs: Ultra-shaped frame +2.4%, 64-view
-// batch +2.0%.
-template <int STACK, bool SPH>
-__global__ void __launch_bounds__(128, 10) k_extend(SceneView sv, const ViewGPU* __restrict__ views, PathSoA ps,
-                                                const int* __restrict__ queue, WaveCounters* cnt, int cur,
-                                                unsigned* status) {
+// atomic per warp for all lanes that need work). The walk is latency-bound, so
+// resident warps matter; three variants trade registers against them
+// (bc_set_option "render_extend", chosen per workload by bc_autotune_render):
+//   0: the ray in registers, no register budget (51 registers, nine 128-thread
+//      blocks per SM);
+//   1: the ray in registers, 48 registers (ten blocks; ptxas spills 10 bytes);
+//   2: each thread's ray in shared memory, which the triangle tests read (the
+//      node test keeps its per-ray constants in registers): 40 registers
+//      without spills, twelve blocks.
+// All three compute the same hits.
+constexpr int kExtendVariants = 3;
+
+template <int STACK, bool SPH, int VAR>
+__device__ __forceinline__ void extend_body(SceneView sv, const ViewGPU* __restrict__ views, PathSoA ps,
+                                            const int* __restrict__ queue, WaveCounters* cnt, int cur,
+                                            unsigned* status) {
   const int n = *((volatile int*)&cnt->q[cur]);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     atomicAdd(&cnt->rays, (unsigned long long)n);
@@ -271,7 +278,10 @@ __global__ void __launch_bounds__(128, 10) k_extend(SceneView sv, const ViewGPU*
   const unsigned below = (1u << lane) - 1u;
   int path = -1;
   bool exhausted = false;
-  Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
+  __shared__ Ray32 ray_sh[VAR == 2 ? 128 : 1];
+  Ray32 ray_reg;
+  Ray32& r = VAR == 2 ? ray_sh[threadIdx.x] : ray_reg;
+  r = make_ray(0, 0, 0, 0, 0, 0, 0);
   FastClosestLeaf<SPH> leaf(sv, r, 1e30f);
   FastWalker<STACK> w;
   w.reset(r);
@@ -302,6 +312,27 @@ __global__ void __launch_bounds__(128, 10) k_extend(SceneView sv, const ViewGPU*
       path = -1;
     }
   }
+}
+
+// The variants differ only in their launch bounds (variant 0 leaves the
+// register count to the compiler's default heuristic).
+template <int STACK, bool SPH>
+__global__ void __launch_bounds__(128) k_extend(SceneView sv, const ViewGPU* __restrict__ views, PathSoA ps,
+                                                const int* __restrict__ queue, WaveCounters* cnt, int cur,
+                                                unsigned* status) {
+  extend_body<STACK, SPH, 0>(sv, views, ps, queue, cnt, cur, status);
+}
+template <int STACK, bool SPH>
+__global__ void __launch_bounds__(128, 10) k_extend_10(SceneView sv, const ViewGPU* __restrict__ views, PathSoA ps,
+                                                       const int* __restrict__ queue, WaveCounters* cnt, int cur,
+                                                       unsigned* status) {
+  extend_body<STACK, SPH, 1>(sv, views, ps, queue, cnt, cur, status);
+}
+template <int STACK, bool SPH>
+__global__ void __launch_bounds__(128, 12) k_extend_12(SceneView sv, const ViewGPU* __restrict__ views, PathSoA ps,
+                                                       const int* __restrict__ queue, WaveCounters* cnt, int cur,
+                                                       unsigned* status) {
+  extend_body<STACK, SPH, 2>(sv, views, ps, queue, cnt, cur, status);
 }
 
 // ---- shade -----------------------------------------------------------------
@@ -1288,6 +1319,7 @@ static int persistent_grid(const void* fn, int block) {
 
 // Launch shape of one wave; computed before any stream capture.
 struct WaveShape {
+  int ext;  // k_extend variant (render_extend)
   int gen_grid, ext_grid, con_grid, shade_grid, acc_grid;
   int bounces;
   bool lights;
@@ -1297,13 +1329,24 @@ struct WaveShape {
 };
 
 template <int STACK, bool SPH>
-static WaveShape wave_shape(int cap, int bounces, bool lights, const GradArgs* grad) {
-  static int ext = 0, con = 0;
-  if (!ext) ext = persistent_grid((const void*)k_extend<STACK, SPH>, 128);
+static const void* extend_kernel(int var) {
+  switch (var) {
+    case 0: return (const void*)k_extend<STACK, SPH>;
+    case 2: return (const void*)k_extend_12<STACK, SPH>;
+    default: return (const void*)k_extend_10<STACK, SPH>;
+  }
+}
+
+template <int STACK, bool SPH>
+static WaveShape wave_shape(int cap, int bounces, bool lights, const GradArgs* grad, int ext_var) {
+  static int ext[kExtendVariants] = {0, 0, 0}, con = 0;
+  const int var = ext_var >= 0 && ext_var < kExtendVariants ? ext_var : 1;
+  if (!ext[var]) ext[var] = persistent_grid(extend_kernel<STACK, SPH>(var), 128);
   if (!con) con = persistent_grid((const void*)k_connect<STACK, SPH>, 128);
   WaveShape w;
+  w.ext = var;
   w.gen_grid = (cap + 255) / 256;
-  w.ext_grid = ext;
+  w.ext_grid = ext[var];
   w.con_grid = con;
   w.shade_grid = sm_count() * 8;
   w.acc_grid = sm_count() * 8;
@@ -1328,7 +1371,12 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
   // counter, extend zeroes the queue and shadow list its shade fills, shade
   // zeroes the work counters of the next extend and of its connect.
   for (int b = 0; b < w.bounces; b++) {
-    k_extend<STACK, SPH><<<w.ext_grid, 128, 0, st>>>(sc.sv, rb->views, rb->ps, rb->q[cur], c, cur, ctx->d_status);
+    if (w.ext == 0)
+      k_extend<STACK, SPH><<<w.ext_grid, 128, 0, st>>>(sc.sv, rb->views, rb->ps, rb->q[cur], c, cur, ctx->d_status);
+    else if (w.ext == 2)
+      k_extend_12<STACK, SPH><<<w.ext_grid, 128, 0, st>>>(sc.sv, rb->views, rb->ps, rb->q[cur], c, cur, ctx->d_status);
+    else
+      k_extend_10<STACK, SPH><<<w.ext_grid, 128, 0, st>>>(sc.sv, rb->views, rb->ps, rb->q[cur], c, cur, ctx->d_status);
     const GradRec rec = w.grad ? rb->grec : GradRec{nullptr, nullptr, nullptr, 0};
     if (w.alt)
       k_shade<true><<<w.shade_grid, 256, 0, st>>>(rb->views, ctx->ds.n_mats, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1],
@@ -1357,7 +1405,7 @@ static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const Shad
                            const GradArgs* grad, bool recursive, bool alt) {
   RenderBuffers* rb = ctx->rb;
   cudaStream_t st = ctx->stream;
-  WaveShape w = wave_shape<STACK, SPH>(rb->cap, bounces, lights, grad);
+  WaveShape w = wave_shape<STACK, SPH>(rb->cap, bounces, lights, grad, ctx->render_extend);
   w.recursive = recursive;
   w.alt = alt;
   // A wave graph pays for its capture when a render has several waves, or when
@@ -1366,7 +1414,8 @@ static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const Shad
   bool use_graph = ctx->render_graph != 0;
   if (use_graph) {
     // every value the captured launches were given
-    std::vector<uintptr_t> key = {(uintptr_t)STACK, (uintptr_t)SPH, (uintptr_t)bounces, (uintptr_t)lights,
+    std::vector<uintptr_t> key = {(uintptr_t)STACK, (uintptr_t)SPH, (uintptr_t)w.ext, (uintptr_t)w.ext_grid,
+                                  (uintptr_t)bounces, (uintptr_t)lights,
                                   (uintptr_t)rb->cap, (uintptr_t)w.gen_grid, (uintptr_t)rb->q[0], (uintptr_t)rb->q[1],
                                   (uintptr_t)rb->cnt, (uintptr_t)rb->bs, (uintptr_t)rb->views, (uintptr_t)rb->seq_xy,
                                   (uintptr_t)rb->sum, (uintptr_t)(rb->want_sumsq ? rb->sumsq : nullptr),

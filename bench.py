@@ -396,6 +396,8 @@ def run_render(args):
     ctx = bcgx.Context(0)
     if args.wave_cap:
         ctx.set_option("render_wave_cap", args.wave_cap)
+    if args.extend is not None:
+        ctx.set_option("render_extend", args.extend)
     ctx.upload(scene)
     L = bcgx.lib()
     import ctypes as C
@@ -440,7 +442,8 @@ def run_render(args):
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (fp64 primary rays)", "data": "synthetic, seeded",
-            "config": {"workload": workload, "spp": st.spp, "segments_per_frame": rays // max(1, args.steps)},
+            "config": {"workload": workload, "spp": st.spp, "segments_per_frame": rays // max(1, args.steps),
+                       "extend_variant": ctx.get_option("render_extend")},
             "e2e": {"value": e2e_r / e2e_t / 1e6, "unit": METRIC, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": st.width * st.height * 16},
             "gpu_launches": None, "clocks": clk}
@@ -494,6 +497,8 @@ def run_batch(args):
     ctx = bcgx.Context(0)
     if args.wave_cap:
         ctx.set_option("render_wave_cap", args.wave_cap)
+    if args.extend is not None:
+        ctx.set_option("render_extend", args.extend)
     ctx.upload_set(built)
     px = sum(st.width * st.height for _, _, st in views)
     paths = sum(st.width * st.height * st.spp for _, _, st in views)
@@ -550,7 +555,8 @@ def run_batch(args):
                                    "128x128..1920x1080, spp U{4..64}, 8 bounces",
                        "pixels": px, "paths": paths, "segments_per_step": br // max(1, args.steps),
                        "host_bvh_build_s": round(build_s, 2),
-                       "wave_cap": ctx.get_option("render_wave_cap")},
+                       "wave_cap": ctx.get_option("render_wave_cap"),
+                       "extend_variant": ctx.get_option("render_extend")},
             "plain": {"value": plain_v, "unit": METRIC, "ms_per_step": 1e3 * sum(pt) / args.steps,
                       "form": f"{n_views} sequential one-view bc_render_batch calls"},
             "batched_over_plain": value / plain_v,
@@ -903,6 +909,7 @@ def main():
                              "calibration"],
                     help="raycast (default, the headline line) or a render workload")
     ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
+    ap.add_argument("--extend", type=int, default=None, help="render workloads: render_extend variant 0, 1 or 2")
     ap.add_argument("--rmse", action="store_true", help="render workloads: RMSE against a converged image")
     ap.add_argument("--views", type=int, default=64, help="batch workload: number of views")
     ap.add_argument("--adaptive", type=float, default=None,

@@ -49,13 +49,46 @@ def test_autotune_render_keeps_images(gpu_ctx):
     before, _ = gpu_ctx.render_batch(views)
     try:
         rep = gpu_ctx.autotune_render(views)
-        assert rep["n_timed"] >= 1 and rep["render_wave_cap"] >= 1 << 22
+        assert rep["n_timed"] >= 3 and rep["render_wave_cap"] >= 1 << 22
+        assert rep["render_extend"] in (0, 1, 2)
         assert 0 < rep["best_ms"] <= rep["worst_ms"] and rep["default_ms"] > 0
         assert gpu_ctx.get_option("render_wave_cap") == rep["render_wave_cap"]
+        assert gpu_ctx.get_option("render_extend") == rep["render_extend"]
         after, _ = gpu_ctx.render_batch(views)
         assert all(np.array_equal(a, b) for a, b in zip(before, after))
     finally:
         gpu_ctx.set_option("render_wave_cap", 1 << 26)
+        gpu_ctx.set_option("render_extend", 1)
+
+
+@pytest.mark.parametrize("which", ["showcase", "batch_tris"])
+def test_extend_variants_same_images(gpu_ctx, which):
+    """The three closest-hit variants of the wave engine (register budget, ray in
+    registers or shared memory) compute the same hits: images and ray counts are
+    bit-identical. Sphere scene and triangle-only scene."""
+    if which == "showcase":
+        spec, cam = scenes.showcase_scene()
+        st = bcgx.quality("Draft")
+        st.width, st.height, st.spp, st.bounces, st.adaptive_sampling = 128, 80, 6, 6, False
+        gpu_ctx.upload_set([scenes.to_scene(spec)])
+        views = [(0, cam, st)]
+    else:
+        specs, views = scenes.batch_views(n_views=4, sizes=(4000, 9000), max_side=(160, 90), spp_range=(2, 4))
+        gpu_ctx.upload_set([scenes.to_scene(s) for s in specs])
+    out = {}
+    try:
+        for var in (0, 1, 2):
+            gpu_ctx.set_option("render_extend", var)
+            assert gpu_ctx.get_option("render_extend") == var
+            out[var] = gpu_ctx.render_batch(views)
+    finally:
+        gpu_ctx.set_option("render_extend", 1)
+    for var in (0, 2):
+        imgs, rays = out[var]
+        assert rays == out[1][1]
+        assert all(np.array_equal(a, b) for a, b in zip(imgs, out[1][0]))
+    with pytest.raises(bcgx.BCError, match="INVALID_ARG"):
+        gpu_ctx.set_option("render_extend", 3)
 
 
 def test_autotune_argument_errors(gpu_ctx):

@@ -100,6 +100,11 @@ struct WaveCounters {
 // One view of a batch (or the single view of a frame / row chunk).
 struct ViewGPU {
   double origin[3], lower[3], horiz[3], vert[3];
+  // primary-ray constants, from the basis on the host: the lower-left corner
+  // relative to the origin (no cancellation on the device), the reciprocals of
+  // max(W - 1, 1) and max(H - 1, 1), the origin rounded to fp32
+  double base[3], inv_w1, inv_h1;
+  float o32[3];
   long long path_off;  // first global path index of the view
   long long pix_off;   // first pixel of the view's rows in the frame buffers
   int W, H, y0, rows, npix;
@@ -177,7 +182,13 @@ __device__ __forceinline__ int view_of(const ViewGPU* __restrict__ views, int n_
 // ---- generate --------------------------------------------------------------
 // Primary ray of sample s of pixel (x, y) and the path's stream (adaptivePixel's
 // sample loop, renderer.go:1940-1950): Halton / R2 jitter rotated per pixel, or
-// random jitter; fp64 camera arithmetic, rounded to fp32 once.
+// random jitter; fp64 camera arithmetic, rounded to fp32 once. GB300's fp64
+// rate is a small fraction of its fp32 rate, so the per-sample fp64 work is
+// kept short: the pixel coordinate is scaled by a reciprocal instead of being
+// divided, and the direction is (lower - origin) + u horiz + v vert with the
+// first term from the host. Against the reference's operation order this moves
+// the fp64 direction by a few units in its last place, far below the fp32
+// rounding that follows.
 __device__ __forceinline__ void primary_ray(const ViewGPU& V, int x, int y, int s, const double2* __restrict__ seq,
                                             float3* o, float3* d, Pcg32* rng, double* jx, double* jy) {
   *rng = make_path_rng(V.seed, (uint64_t)y * (uint64_t)V.W + (uint64_t)x, (uint64_t)s);
@@ -192,12 +203,12 @@ __device__ __forceinline__ void primary_ray(const ViewGPU& V, int x, int y, int 
     *jx = (double)rng->uniform();
     *jy = (double)rng->uniform();
   }
-  const double u = ((double)x + *jx) / (double)max(V.W - 1, 1);
-  const double vv = ((double)(V.H - 1 - y) + *jy) / (double)max(V.H - 1, 1);
+  const double u = ((double)x + *jx) * V.inv_w1;
+  const double vv = ((double)(V.H - 1 - y) + *jy) * V.inv_h1;
   float dd[3];
 #pragma unroll
-  for (int k = 0; k < 3; k++) dd[k] = (float)(((V.lower[k] + V.horiz[k] * u) + V.vert[k] * vv) - V.origin[k]);
-  *o = f3((float)V.origin[0], (float)V.origin[1], (float)V.origin[2]);
+  for (int k = 0; k < 3; k++) dd[k] = __double2float_rn(fma(V.vert[k], vv, fma(V.horiz[k], u, V.base[k])));
+  *o = f3(V.o32[0], V.o32[1], V.o32[2]);
   *d = f3(dd[0], dd[1], dd[2]);
 }
 
@@ -1571,6 +1582,12 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
       if (built) photon_rays.push_back(built);
     }
     camera_basis(r.cam, (double)V.W / (double)V.H, V.origin, V.lower, V.horiz, V.vert);
+    for (int k = 0; k < 3; k++) {
+      V.base[k] = V.lower[k] - V.origin[k];
+      V.o32[k] = (float)V.origin[k];
+    }
+    V.inv_w1 = 1.0 / (double)std::max(V.W - 1, 1);
+    V.inv_h1 = 1.0 / (double)std::max(V.H - 1, 1);
     V.path_off = total;
     total += (long long)V.npix * V.spp;
     max_bounces = std::max(max_bounces, V.bounces);

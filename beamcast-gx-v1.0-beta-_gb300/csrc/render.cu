@@ -196,9 +196,11 @@ __device__ __forceinline__ void primary_ray(const ViewGPU& V, int x, int y, int 
     double rx, ry;
     pixel_rotation(x, y, &rx, &ry);
     const double2 q = seq[V.seq_off + s];
-    double a = q.x + rx, b = q.y + ry;
-    *jx = a - floor(a);
-    *jy = b - floor(b);
+    // fract(q + r) with q, r in [0, 1): the sum lies in [0, 2), so floor is 0
+    // or 1 and a - 1 is exact (Sterbenz); the same bits as a - floor(a)
+    const double a = q.x + rx, b = q.y + ry;
+    *jx = a >= 1.0 ? a - 1.0 : a;
+    *jy = b >= 1.0 ? b - 1.0 : b;
   } else {
     *jx = (double)rng->uniform();
     *jy = (double)rng->uniform();

@@ -136,7 +136,7 @@ void bc_destroy(bc_context* ctx) {
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_tri, &ctx->d_slot64, &ctx->d_snorm, &ctx->d_slot_prim, &ctx->d_mats,
                     &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ,
                     &ctx->d_kids8, &ctx->d_geom, &ctx->d_build, &ctx->d_build_out, &ctx->d_order[0],
-                    &ctx->d_order[1], &ctx->d_order[2]})
+                    &ctx->d_order[1], &ctx->d_order[2], &ctx->d_rec[0], &ctx->d_rec[1], &ctx->d_rec[2]})
     b->release();
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->d_work) cudaFree(ctx->d_work);
@@ -337,8 +337,14 @@ bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, flo
     if (e) return cuda_status(ctx, e, "ray order buffers");
     order = ctx->d_order[2].p;
   }
+  void* rec = nullptr;
+  if (ctx->raycast_split && ctx->raycast_exact && n > 0) {
+    cudaError_t e = ctx->d_rec[2].ensure(exact_record_bytes(n));
+    if (e) return cuda_status(ctx, e, "ray-cast record buffers");
+    rec = ctx->d_rec[2].p;
+  }
   cudaError_t e = launch_raycast_closest(ctx->ds, (const float4*)d_rays, n, d_t_out, d_prim_out, ctx->d_status,
-                                         ctx->d_work + 2, ctx->raycast_variant, order, st);
+                                         ctx->d_work + 2, ctx->raycast_variant, order, rec, st);
   return cuda_status(ctx, e, "ray-cast launch");
 }
 
@@ -367,6 +373,12 @@ bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out
       if ((e = ctx->d_order[k].ensure(ray_order_bytes(std::min(chunk, n))))) return cuda_status(ctx, e, "ray order buffers");
       order[k] = ctx->d_order[k].p;
     }
+  void* rec[2] = {nullptr, nullptr};
+  if (ctx->raycast_split && ctx->raycast_exact)
+    for (int k = 0; k < 2; k++) {
+      if ((e = ctx->d_rec[k].ensure(exact_record_bytes(std::min(chunk, n))))) return cuda_status(ctx, e, "ray-cast record buffers");
+      rec[k] = ctx->d_rec[k].p;
+    }
   for (int64_t off = 0, c = 0; off < n && e == cudaSuccess; off += chunk, c++) {
     const int64_t m = std::min(chunk, n - off);
     cudaStream_t st = streams[c & 1];
@@ -374,7 +386,8 @@ bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out
     e = cudaMemcpyAsync(dr, rays + 8 * off, (size_t)m * 32, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
       e = launch_raycast_closest(ctx->ds, dr, m, ctx->d_t.as<float>() + off, ctx->d_prim.as<int32_t>() + off,
-                                 ctx->d_status, ctx->d_work + (c & 1), ctx->raycast_variant, order[c & 1], st);
+                                 ctx->d_status, ctx->d_work + (c & 1), ctx->raycast_variant, order[c & 1], rec[c & 1],
+                                 st);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(t_out + off, ctx->d_t.as<float>() + off, (size_t)m * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
@@ -437,6 +450,11 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     ctx->raycast_sort = (int)value;
     return BC_OK;
   }
+  if (n == "raycast_split") {
+    if (value != 0 && value != 1) return set_error(ctx, BC_ERR_INVALID_ARG, "raycast_split must be 0 or 1");
+    ctx->raycast_split = (int)value;
+    return BC_OK;
+  }
   if (n == "photon_grid") {
     if (value != 0 && value != 1) return set_error(ctx, BC_ERR_INVALID_ARG, "photon_grid must be 0 or 1");
     ctx->photon_grid = (int)value;
@@ -479,6 +497,7 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
   if (n == "raycast_exact") { *value = ctx->raycast_exact; return BC_OK; }
   if (n == "render_wave_cap") { *value = ctx->render_wave_cap; return BC_OK; }
   if (n == "raycast_sort") { *value = ctx->raycast_sort; return BC_OK; }
+  if (n == "raycast_split") { *value = ctx->raycast_split; return BC_OK; }
   if (n == "raycast_chunk") { *value = ctx->raycast_chunk; return BC_OK; }
   if (n == "photon_grid") { *value = ctx->photon_grid; return BC_OK; }
   if (n == "render_graph") { *value = ctx->render_graph; return BC_OK; }

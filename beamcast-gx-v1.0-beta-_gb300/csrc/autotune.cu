@@ -2,9 +2,10 @@
 // caller's own work, then keeps the fastest. No counterpart in the reference,
 // whose OpenCL path picks a work-group size once (gpu_opencl_windows.go:285-304).
 //
-//   ray cast: the register budget of the exact kernels (raycast_minblocks 1, 6, 8)
-//             and the coherent ray order (raycast_sort 0, 1); plain fp32 mode has
-//             the order only. CUDA events on the context's stream, best of two
+//   ray cast: the exact kernels' form (raycast_split 1: walk and fp64
+//             settlement passes; 0: one kernel, with register budget
+//             raycast_minblocks 6, 8, 1) and the coherent ray order
+//             (raycast_sort 1, 0); plain fp32 mode has the order only. CUDA events on the context's stream, best of two
 //             runs after one warm-up, on the caller's rays.
 //   render:   the extend kernel's variant (render_extend 0, 1, 2: register
 //             budget and where the ray lives, i.e. resident blocks per SM) at
@@ -67,41 +68,47 @@ bc_status bc_autotune_raycast(bc_context* ctx, const float* d_rays, int64_t n, b
   cudaError_t e = ctx->d_t.ensure((size_t)n * 4);
   if (!e) e = ctx->d_prim.ensure((size_t)n * 4);
   if (e) return cuda_status(ctx, e, "autotune buffers");
-  struct Cand { int minblocks, sort; };
+  struct Cand { int split, minblocks, sort; };
   std::vector<Cand> cands;
   if (ctx->raycast_exact) {
+    for (int so : {1, 0}) cands.push_back(Cand{1, ctx->raycast_minblocks, so});
     for (int mb : {6, 8, 1})
-      for (int so : {1, 0}) cands.push_back(Cand{mb, so});
+      for (int so : {1, 0}) cands.push_back(Cand{0, mb, so});
   } else {
-    cands = {Cand{ctx->raycast_minblocks, 1}, Cand{ctx->raycast_minblocks, 0}};
+    cands = {Cand{ctx->raycast_split, ctx->raycast_minblocks, 1}, Cand{ctx->raycast_split, ctx->raycast_minblocks, 0}};
   }
-  const int keep_mb = ctx->raycast_minblocks, keep_sort = ctx->raycast_sort;
+  const int keep_mb = ctx->raycast_minblocks, keep_sort = ctx->raycast_sort, keep_split = ctx->raycast_split;
   bc_tune_report rep;
   std::memset(&rep, 0, sizeof(rep));
   int best = -1;
   for (size_t i = 0; i < cands.size(); i++) {
+    ctx->raycast_split = cands[i].split;
     ctx->raycast_minblocks = cands[i].minblocks;
     ctx->raycast_variant = ctx->raycast_exact ? cands[i].minblocks : 0;
     ctx->raycast_sort = cands[i].sort;
     float ms = 0.0f;
     bc_status st = time_raycast(ctx, d_rays, n, ctx->d_t.as<float>(), ctx->d_prim.as<int32_t>(), &ms);
     if (st) {  // leave the options as they were
+      ctx->raycast_split = keep_split;
       ctx->raycast_minblocks = keep_mb;
       ctx->raycast_variant = ctx->raycast_exact ? keep_mb : 0;
       ctx->raycast_sort = keep_sort;
       return st;
     }
     rep.n_timed++;
-    if (cands[i].minblocks == keep_mb && cands[i].sort == keep_sort) rep.default_ms = ms;
+    if (cands[i].split == keep_split && cands[i].sort == keep_sort && (keep_split || cands[i].minblocks == keep_mb))
+      rep.default_ms = ms;
     if (best < 0 || ms < rep.best_ms) {
       best = (int)i;
       rep.best_ms = ms;
     }
     if (ms > rep.worst_ms) rep.worst_ms = ms;
   }
+  ctx->raycast_split = cands[best].split;
   ctx->raycast_minblocks = cands[best].minblocks;
   ctx->raycast_variant = ctx->raycast_exact ? cands[best].minblocks : 0;
   ctx->raycast_sort = cands[best].sort;
+  rep.raycast_split = ctx->raycast_split;
   rep.raycast_minblocks = ctx->raycast_minblocks;
   rep.raycast_sort = ctx->raycast_sort;
   rep.render_wave_cap = ctx->render_wave_cap;
@@ -196,6 +203,7 @@ bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_vi
   rep.raycast_sort = ctx->raycast_sort;
   rep.render_wave_cap = best_cap;
   rep.render_extend = best_ext;
+  rep.raycast_split = ctx->raycast_split;
   if (out) *out = rep;
   return BC_OK;
 }

@@ -90,6 +90,8 @@ struct bc_context {
   int raycast_sort = 1;       // trace rays in a spatially coherent order (bc_set_option "raycast_sort")
   long long raycast_chunk = 1 << 21;  // rays per pipelined chunk of bc_raycast (bc_set_option "raycast_chunk")
   bcgx::DevBuf d_order[3];    // ray order scratch: [0], [1] the two streams of bc_raycast, [2] bc_raycast_device
+  int raycast_split = 1;      // exact closest hit as walk + settlement passes (bc_set_option "raycast_split")
+  bcgx::DevBuf d_rec[3];      // per-ray records of the split passes, indexed as d_order
   // ray-cast staging
   bcgx::DevBuf d_rays, d_t, d_prim, d_occ;
   unsigned* d_status = nullptr;

@@ -29,11 +29,14 @@ int stack_variant(int need);
 // `work` is an 8-byte device counter private to this launch's stream (persistent kernels).
 // order_scratch (ray_order_bytes(n) bytes, or NULL): rays are traced in a
 // spatially coherent order (batches of at least kMinOrderedRays rays).
+// rec_scratch (exact_record_bytes(n) bytes, or NULL): the exact closest hit of
+// a triangle-only scene runs as separate walk and fp64 settlement passes.
 constexpr int64_t kMinOrderedRays = 65536;
 size_t ray_order_bytes(int64_t n);
+size_t exact_record_bytes(int64_t n);
 cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int64_t n, float* t_out,
                                    int32_t* prim_out, unsigned* status, unsigned long long* work, int variant,
-                                   void* order_scratch, cudaStream_t st);
+                                   void* order_scratch, void* rec_scratch, cudaStream_t st);
 // Exact any hit.
 cudaError_t launch_raycast_any(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
                                int variant, cudaStream_t st);

@@ -196,6 +196,241 @@ __global__ void __launch_bounds__(128, MINB) k_closest_exact_persistent(SceneVie
   if ((int)lane < parked) settle_parked(sv, rays, q, (int)lane, t_out, prim_out, status);
 }
 
+// ---- exact closest hit in passes: walk, then settle ----------------------------
+// The one-kernel form above keeps the fp64 settlement (and the in-walk fp64
+// re-test of a full contender list) in the walking kernel, whose register
+// allocation then covers the fp64 code: 80 registers with spills at six
+// 128-thread blocks per SM. Split, the walk holds no fp64 code and fits 48
+// registers with a 6-byte spill (ten blocks per SM; 9.74 -> 8.31 ms on the
+// 1M-triangle / 4M-ray cast, settlement included):
+//   pass 1, k_exact_walk: the persistent walk with the fp32 classifier; a
+//     finished ray leaves a record (best certain hit: slot and upper bound of
+//     its distance; the pending contenders: slot and lower bound). A ray with
+//     more contenders than the list holds stops walking and is marked.
+//   pass 2, k_exact_settle: one thread per ray settles its record in fp64 with
+//     triHit's operation order (the same decisions as settle_parked) and writes
+//     the result; marked rays go to a list.
+//   pass 3, k_closest_exact_list: the marked rays, traced again by the
+//     one-kernel exact walk, whose full list falls back to fp64 in the walk.
+// Triangle-only scenes (as the persistent one-kernel form).
+struct ExactRecords {
+  int32_t* bslot;   // [n]: best certain hit, -1 none
+  float* bhi;       // [n]: upper bound of its distance
+  int32_t* npend;   // [n]: pending contenders; kPending + 1: list overflowed
+  int32_t* pslot;   // [kPending * n]
+  float* plo;       // [kPending * n]
+  long long* redo;  // [n]: rays of pass 3
+  unsigned long long* n_redo;
+};
+
+
+size_t up256(size_t b) { return (b + 255) / 256 * 256; }
+
+// Layout of the records in the caller's scratch (exact_record_bytes(n) bytes).
+ExactRecords exact_records(void* p, int64_t n) {
+  auto up = up256;
+  char* q = (char*)p;
+  ExactRecords r;
+  r.n_redo = (unsigned long long*)q;
+  q += 256;
+  r.bslot = (int32_t*)q;
+  q += up((size_t)n * 4);
+  r.bhi = (float*)q;
+  q += up((size_t)n * 4);
+  r.npend = (int32_t*)q;
+  q += up((size_t)n * 4);
+  r.pslot = (int32_t*)q;
+  q += up((size_t)n * 4 * kPending);
+  r.plo = (float*)q;
+  q += up((size_t)n * 4 * kPending);
+  r.redo = (long long*)q;
+  return r;
+}
+
+// ExactClosestLeaf's decisions without its fp64 fallback: where that leaf
+// resolves a contender in fp64 because its list is full, this one marks the
+// ray (npend = kPending + 1) and ends the walk (done).
+struct FilterLeaf {
+  const SceneView& sv;
+  const Ray32& r;
+  float tmax_ray;
+  float tlim;
+  bool done;
+  int32_t bslot;
+  float blo, bhi;
+  int npend;
+  PendEntry pend[kPending];
+
+  __device__ FilterLeaf(const SceneView& s, const Ray32& ray) : sv(s), r(ray) { reset(0.0f); }
+  __device__ __forceinline__ void reset(float tmax) {
+    tmax_ray = tmax;
+    tlim = widen(tmax);
+    done = false;
+    npend = 0;
+    bslot = -1;
+    blo = tmax;
+    bhi = tmax;
+  }
+  __device__ __forceinline__ void overflow() {
+    npend = kPending + 1;
+    done = true;
+  }
+  __device__ __forceinline__ void take_certain(int slot, float lo, float hi) {
+    if (bslot < 0 || hi < blo) {
+      bslot = slot;
+      blo = lo;
+      bhi = hi;
+    } else if (lo > bhi) {
+      return;
+    } else if (npend < kPending) {
+      if (hi < bhi) {
+        pend[npend++] = PendEntry{bslot, blo};
+        bslot = slot;
+        blo = lo;
+        bhi = hi;
+      } else {
+        pend[npend++] = PendEntry{slot, lo};
+      }
+    } else {
+      overflow();
+      return;
+    }
+    tlim = widen(bhi);
+  }
+  __device__ __forceinline__ void operator()(uint32_t ref) {
+    const int cnt = (int)((ref >> 27) & 15u) + 1;
+    const int s0 = (int)(ref & kSlotMask);
+    for (int k = 0; k < cnt && !done; k++) {
+      const int s = s0 + k;
+      const float4 A = __ldg(sv.tri + 3 * s);
+      const float4 E1 = __ldg(sv.tri + 3 * s + 1);
+      const float4 E2 = __ldg(sv.tri + 3 * s + 2);
+      const TriClass tc = tri_classify(A, E1, E2, r, tmax_ray, tlim);
+      if (tc.state == kMiss) continue;
+      const float lo = __fsub_rd(tc.t, tc.et), hi = __fadd_ru(tc.t, tc.et);
+      if (bslot >= 0 && lo > bhi) continue;
+      if (tc.state == kHit) take_certain(s, lo, hi);
+      else if (npend < kPending) pend[npend++] = PendEntry{s, lo};
+      else overflow();
+    }
+  }
+};
+
+template <int STACK>
+__global__ void __launch_bounds__(128, 10) k_exact_walk(SceneView sv, const float4* __restrict__ rays, int64_t n,
+                                                       ExactRecords rec, unsigned* status, unsigned long long* work,
+                                                       const int32_t* __restrict__ perm) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  long long idx = -1;
+  bool exhausted = false;
+  Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
+  FilterLeaf leaf(sv, r);
+  Walker<STACK> w;
+  w.reset(r);
+  for (;;) {
+    const bool need = idx < 0 && !exhausted;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if ((int)lane == leader) base = atomicAdd(work, (unsigned long long)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const unsigned long long my = base + (unsigned long long)__popc(m & below);
+        if (my < (unsigned long long)n) {
+          idx = perm ? (long long)perm[my] : (long long)my;
+          const float4 a = __ldg(rays + 2 * idx), b = __ldg(rays + 2 * idx + 1);
+          r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
+          leaf.reset(b.w);
+          w.reset(r);
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, idx >= 0)) break;
+    if (idx >= 0 && w.step(sv, r, leaf, status)) {
+      rec.bslot[idx] = leaf.bslot;
+      rec.bhi[idx] = leaf.bhi;
+      rec.npend[idx] = leaf.npend;
+      const int np = min(leaf.npend, kPending);
+      for (int j = 0; j < np; j++) {
+        rec.pslot[(size_t)j * n + idx] = leaf.pend[j].slot;
+        rec.plo[(size_t)j * n + idx] = leaf.pend[j].lo;
+      }
+      idx = -1;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) k_exact_settle(SceneView sv, const float4* __restrict__ rays, int64_t n,
+                                                      ExactRecords rec, float* __restrict__ t_out,
+                                                      int32_t* __restrict__ prim_out, unsigned* status) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int np = rec.npend[i];
+    if (np > kPending) {
+      rec.redo[atomicAdd(rec.n_redo, 1ull)] = i;
+      continue;
+    }
+    const float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
+    const D3 o{(double)a.x, (double)a.y, (double)a.z}, d{(double)b.x, (double)b.y, (double)b.z};
+    const double tmin = (double)a.w, tmax = (double)b.w;
+    const int bslot = rec.bslot[i];
+    const float bhi = rec.bhi[i];
+    int win = -1;
+    double wt = 0.0;
+    if (bslot >= 0) {
+      double t;
+      if (tri_hit64(sv.slot64 + 9 * (size_t)bslot, o, d, tmin, tmax, &t)) {
+        win = bslot;
+        wt = t;
+      } else {
+        atomicOr(status, kStatusBound);  // a certain hit must pass its fp64 test
+      }
+    }
+    for (int j = 0; j < np; j++) {
+      const float lo = rec.plo[(size_t)j * n + i];
+      if (bslot >= 0 && lo > bhi) continue;
+      const int sj = rec.pslot[(size_t)j * n + i];
+      double t;
+      if (tri_hit64(sv.slot64 + 9 * (size_t)sj, o, d, tmin, tmax, &t) &&
+          (win < 0 || t < wt || (t == wt && sj > win))) {
+        win = sj;
+        wt = t;
+      }
+    }
+    t_out[i] = win >= 0 ? __double2float_rn(wt) : -1.0f;
+    prim_out[i] = win >= 0 ? __ldg(sv.slot_prim + win) : -1;
+  }
+}
+
+// Pass 3: the listed rays with the one-kernel exact walk. Every lane of a warp
+// runs the same number of iterations (the warp-converged settlement inside
+// closest_hit_exact needs all 32 lanes).
+template <int STACK>
+__global__ void __launch_bounds__(128) k_closest_exact_list(SceneView sv, const float4* __restrict__ rays,
+                                                            ExactRecords rec, float* __restrict__ t_out,
+                                                            int32_t* __restrict__ prim_out, unsigned* status) {
+  const long long cnt = (long long)*((volatile unsigned long long*)rec.n_redo);
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < cnt; base += (long long)gridDim.x * blockDim.x) {
+    const long long k = base + threadIdx.x;
+    const bool active = k < cnt;
+    const long long i = active ? rec.redo[k] : 0;
+    float4 a = make_float4(0, 0, 0, 0), b = a;
+    if (active) {
+      a = __ldg(rays + 2 * i);
+      b = __ldg(rays + 2 * i + 1);
+    }
+    const Ray32 r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
+    const HitResult h = closest_hit_exact<STACK, false>(sv, r, b.w, status, active);
+    if (active) {
+      t_out[i] = h.slot >= 0 ? __double2float_rn(h.t64) : -1.0f;
+      prim_out[i] = h.slot >= 0 ? __ldg(sv.slot_prim + h.slot) : -1;
+    }
+  }
+}
+
 template <int STACK>
 __global__ void __launch_bounds__(128) k_closest_fast_persistent(SceneView sv, const float4* __restrict__ rays,
                                                                  int64_t n, float* __restrict__ t_out,
@@ -352,6 +587,31 @@ cudaError_t closest_stack(const DeviceScene& s, const float4* rays, int64_t n, f
   return cudaGetLastError();
 }
 
+template <int STACK>
+cudaError_t closest_split(const DeviceScene& s, const float4* rays, int64_t n, float* t, int32_t* p, unsigned* status,
+                          unsigned long long* work, const int32_t* perm, void* rec_scratch, cudaStream_t st) {
+  static int blocks = 0;
+  if (!blocks) blocks = persistent_blocks(k_exact_walk<STACK>);
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
+  }
+  const ExactRecords rec = exact_records(rec_scratch, n);
+  cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), st);
+  if (!e) e = cudaMemsetAsync(rec.n_redo, 0, sizeof(unsigned long long), st);
+  if (e) return e;
+  const int64_t grid = (n + 127) / 128;
+  k_exact_walk<STACK><<<(int)std::min<int64_t>(blocks, grid), 128, 0, st>>>(view_of(s), rays, n, rec, status, work,
+                                                                           perm);
+  k_exact_settle<<<(int)std::min<int64_t>((int64_t)sms * 16, grid), 128, 0, st>>>(view_of(s), rays, n, rec, t, p,
+                                                                                 status);
+  k_closest_exact_list<STACK><<<sms * 4, 128, 0, st>>>(view_of(s), rays, rec, t, p, status);
+  return cudaGetLastError();
+}
+
 template <int STACK, int MINB>
 cudaError_t any_stack(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
                       cudaStream_t st) {
@@ -365,7 +625,10 @@ cudaError_t any_stack(const DeviceScene& s, const float4* rays, int64_t n, uint8
 
 template <int STACK>
 cudaError_t closest_var(const DeviceScene& s, const float4* rays, int64_t n, float* t, int32_t* p, unsigned* status,
-                        unsigned long long* work, int variant, const int32_t* perm, cudaStream_t st) {
+                        unsigned long long* work, int variant, const int32_t* perm, void* rec_scratch,
+                        cudaStream_t st) {
+  if (variant != 0 && rec_scratch && !s.has_spheres)
+    return closest_split<STACK>(s, rays, n, t, p, status, work, perm, rec_scratch, st);
   if (variant == 0) {  // fast, not exact
     const int64_t grid = (n + 127) / 128;
     if (s.has_spheres) {
@@ -399,13 +662,17 @@ cudaError_t any_var(const DeviceScene& s, const float4* rays, int64_t n, uint8_t
 
 }  // namespace
 
+size_t exact_record_bytes(int64_t n) {
+  return 256 + 3 * up256((size_t)n * 4) + 2 * up256((size_t)n * 4 * kPending) + up256((size_t)n * 8);
+}
+
 size_t ray_order_bytes(int64_t n) {
   return (size_t)kKeyBins * 4 + (size_t)(kKeyBins / kScanBlock) * 4 + (size_t)n * 8 + 4 * 256;
 }
 
 cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int64_t n, float* t_out,
                                    int32_t* prim_out, unsigned* status, unsigned long long* work, int variant,
-                                   void* order_scratch, cudaStream_t st) {
+                                   void* order_scratch, void* rec_scratch, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   const int32_t* perm = nullptr;
   if (order_scratch && n >= kMinOrderedRays && !s.has_spheres) {
@@ -428,9 +695,9 @@ cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int
     perm = pm;
   }
   switch (stack_variant(s.stack_need)) {
-    case 64: return closest_var<64>(s, rays, n, t_out, prim_out, status, work, variant, perm, st);
-    case 128: return closest_var<128>(s, rays, n, t_out, prim_out, status, work, variant, perm, st);
-    case 256: return closest_var<256>(s, rays, n, t_out, prim_out, status, work, variant, perm, st);
+    case 64: return closest_var<64>(s, rays, n, t_out, prim_out, status, work, variant, perm, rec_scratch, st);
+    case 128: return closest_var<128>(s, rays, n, t_out, prim_out, status, work, variant, perm, rec_scratch, st);
+    case 256: return closest_var<256>(s, rays, n, t_out, prim_out, status, work, variant, perm, rec_scratch, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -195,8 +195,11 @@ def run_gpu(args):
         ctx.set_option("raycast_minblocks", args.minblocks)
     if args.fast:
         ctx.set_option("raycast_exact", 0)
+    if args.split is not None:
+        ctx.set_option("raycast_split", args.split)
     ctx.upload(scene)
     stats = ctx.scene_stats()
+    split = bool(ctx.get_option("raycast_split") and ctx.get_option("raycast_exact"))
 
     stream = torch.cuda.Stream(device=dev)
     d_rays = torch.from_numpy(rays).to(dev)
@@ -282,9 +285,12 @@ def run_gpu(args):
                      "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_ray": bytes_per_ray, **counters},
         "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
-        # per step: the trace kernel, plus the four ray-order kernels (keys, two scans, scatter)
-        "gpu_launches": args.steps * (5 if ctx.get_option("raycast_sort") and N_RAYS >= 65536 else 1),
+        # per step: the trace kernel (split form: walk, settle, re-trace), plus the
+        # four ray-order kernels (keys, two scans, scatter)
+        "gpu_launches": args.steps * ((3 if split else 1) +
+                                      (4 if ctx.get_option("raycast_sort") and N_RAYS >= 65536 else 0)),
         "raycast_minblocks": ctx.get_option("raycast_minblocks"),
+        "raycast_split": ctx.get_option("raycast_split"),
         "raycast_exact": ctx.get_option("raycast_exact"),
         "clocks": clk,
         "kernel_ms": [round(x, 4) for x in kernel_ms],
@@ -904,6 +910,7 @@ def main():
     ap.add_argument("--rays", type=int, default=N_RAYS, help="smaller case for profiling")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
     ap.add_argument("--minblocks", type=int, default=0, help="ray-cast register variant (1, 6, 8; 0 = library default)")
+    ap.add_argument("--split", type=int, default=None, help="ray cast: raycast_split 0 or 1 (default: library default)")
     ap.add_argument("--fast", action="store_true", help="plain fp32 closest hit instead of the exact contract")
     ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch", "diff", "refit", "build", "integrators",
                              "calibration"],

@@ -401,8 +401,16 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
 /*
  * Tuning options of a context (no counterpart in the reference, whose OpenCL
  * path picks a work-group size once, gpu_opencl_windows.go:285-304):
- *   "raycast_minblocks"  1, 6 or 8: register budget of the ray-cast kernels
- *                        (resident 128-thread blocks per SM the allocation must allow).
+ *   "raycast_split"      1 (default): the exact closest hit of a triangle-only
+ *                        scene runs as passes: a walk with fp32 classification only
+ *                        (ten 128-thread blocks per SM), an fp64 settlement pass,
+ *                        and a re-trace of the rays whose contender list overflowed;
+ *                        it holds 52 bytes of device scratch per ray of a call (per
+ *                        chunk for bc_raycast). 0: one kernel walks and settles.
+ *                        Both give the same results.
+ *   "raycast_minblocks"  1, 6 or 8: register budget of the one-kernel ray-cast
+ *                        kernels (resident 128-thread blocks per SM the allocation
+ *                        must allow).
  *   "raycast_exact"      1 (default): bc_raycast is exact as documented there;
  *                        0: plain fp32 closest hit, t = the fp32 distance, with no
  *                        exactness contract near edges and ties.
@@ -447,7 +455,8 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
  * same hits and images.
  *
  * bc_autotune_raycast: device rays as for bc_raycast_device; candidates are
- * raycast_minblocks 6, 8, 1 with raycast_sort 1 and 0 (exact mode; plain fp32
+ * raycast_split 1 with raycast_sort 1 and 0, then raycast_split 0 with
+ * raycast_minblocks 6, 8, 1 and raycast_sort 1 and 0 (exact mode; plain fp32
  * mode: raycast_sort only). Best of two timed runs each (CUDA events).
  * bc_autotune_render: the views as for bc_render_batch; first render_extend
  * 1, 0, 2 at the current wave size, then render_wave_cap 2^22 .. 2^26 (up to
@@ -461,6 +470,7 @@ typedef struct bc_tune_report {
   int32_t n_timed;                          /* candidates timed */
   int32_t render_extend;                    /* option in force after the call */
   double best_ms, default_ms, worst_ms;     /* chosen, the options before the call, slowest */
+  int32_t raycast_split, reserved;          /* option in force after the call */
 } bc_tune_report;
 bc_status bc_autotune_raycast(bc_context* ctx, const float* d_rays, int64_t n, bc_tune_report* out);
 bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_views, bc_tune_report* out);

@@ -23,8 +23,9 @@ def test_autotune_raycast_keeps_results(gpu_ctx):
     torch.cuda.synchronize()
     try:
         rep = gpu_ctx.autotune_raycast(r.data_ptr(), len(rays))
-        assert rep["n_timed"] == 6
+        assert rep["n_timed"] == 8
         assert rep["raycast_minblocks"] in (1, 6, 8) and rep["raycast_sort"] in (0, 1)
+        assert rep["raycast_split"] in (0, 1) and gpu_ctx.get_option("raycast_split") == rep["raycast_split"]
         assert 0 < rep["best_ms"] <= rep["default_ms"] <= rep["worst_ms"]
         assert gpu_ctx.get_option("raycast_minblocks") == rep["raycast_minblocks"]
         assert gpu_ctx.get_option("raycast_sort") == rep["raycast_sort"]
@@ -36,6 +37,7 @@ def test_autotune_raycast_keeps_results(gpu_ctx):
     finally:
         gpu_ctx.set_option("raycast_minblocks", 6)
         gpu_ctx.set_option("raycast_sort", 1)
+        gpu_ctx.set_option("raycast_split", 1)
 
 
 def test_autotune_render_keeps_images(gpu_ctx):

@@ -187,3 +187,58 @@ def test_full_size_c2_properties_and_sample(gpu_ctx, orc):
     assert np.array_equal(p[idx], pr)
     h = pr >= 0
     assert np.all(_ulp_diff(t[idx][h], tr[h].astype(np.float32)) == 0)
+
+
+def _stacked_triangles(n_base=300, copies=6, seed=41):
+    """Large random triangles, each repeated `copies` times with offsets of
+    1e-7 along z (the first two copies coincide): a ray through a stack meets
+    more contenders with overlapping distance intervals than the walk's list
+    holds, which sends it to the third pass of the split form."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.1, 0.9, (n_base, 3))
+    e1 = rng.normal(size=(n_base, 3)) * 0.15
+    e2 = rng.normal(size=(n_base, 3)) * 0.15
+    a = c - (e1 + e2) / 3
+    base = np.concatenate([a, a + e1, a + e2], axis=1)
+    layers = []
+    for k in range(copies):
+        off = np.zeros(9)
+        off[2::3] = max(0, k - 1) * 1e-7
+        layers.append(base + off)
+    sp = scenes.SceneSpec(name="stacked", bvh_mode="SAH", bvh_bins=32, bvh_leaf=4)
+    m = sp.material(scenes.Material(scenes.MAT_DIFFUSE, (0.5, 0.5, 0.5)))
+    sp.triangles(np.concatenate(layers), m)
+    return sp
+
+
+@pytest.mark.parametrize("which", ["random", "stacked", "edge"])
+def test_split_passes_parity(gpu_ctx, orc, which):
+    """raycast_split 1 (the default: walk pass without fp64 code, fp64 settlement
+    pass, and a pass that re-traces rays whose contender list overflowed) returns
+    the same hits and distances as the one-kernel exact form (raycast_split 0),
+    and both match the oracle."""
+    if which == "random":
+        spec = scenes.random_triangles(100_000, seed=scenes.SEED_C2 + 7)
+        rays = scenes.random_rays(262_144, seed=15)
+    elif which == "stacked":
+        spec = _stacked_triangles()
+        rays = scenes.random_rays(131_072, seed=16)
+    else:
+        spec, _, _ = scenes.cornell_box()
+        rng = np.random.default_rng(2)
+        rays = scenes.random_rays(20_000, seed=17)
+        rays[:, 0:3] = rng.uniform(-1, 1, (len(rays), 3))
+        rays[::3, 4 + rng.integers(3)] = 0.0  # zero direction components
+        rays[1::7, 1] = -1.0  # origins on the floor plane
+    gpu_ctx.upload(scenes.to_scene(spec))
+    ref = orc.OracleScene.from_spec(spec)
+    assert gpu_ctx.get_option("raycast_split") == 1
+    _check(gpu_ctx, ref, rays, allow_ties=which != "random")
+    two = gpu_ctx.raycast(rays)
+    try:
+        gpu_ctx.set_option("raycast_split", 0)
+        _check(gpu_ctx, ref, rays, allow_ties=which != "random")
+        one = gpu_ctx.raycast(rays)
+    finally:
+        gpu_ctx.set_option("raycast_split", 1)
+    assert np.array_equal(one[1], two[1]) and np.array_equal(one[0], two[0])

@@ -332,7 +332,7 @@ bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, flo
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   void* order = nullptr;
-  if (ctx->raycast_sort && n >= kMinOrderedRays) {
+  if (ctx->raycast_sort && n >= kMinOrderedRays && n < (int64_t(1) << 31)) {
     cudaError_t e = ctx->d_order[2].ensure(ray_order_bytes(n));
     if (e) return cuda_status(ctx, e, "ray order buffers");
     order = ctx->d_order[2].p;

@@ -675,7 +675,8 @@ cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int
                                    void* order_scratch, void* rec_scratch, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   const int32_t* perm = nullptr;
-  if (order_scratch && n >= kMinOrderedRays && !s.has_spheres) {
+  // the order is a permutation of 32-bit ray indices: batches up to 2^31 - 1 rays
+  if (order_scratch && n >= kMinOrderedRays && n < (int64_t(1) << 31) && !s.has_spheres) {
     char* q = (char*)order_scratch;
     int32_t* bins = (int32_t*)q;
     int32_t* totals = (int32_t*)(q + (size_t)kKeyBins * 4);

@@ -196,7 +196,10 @@ bc_status bc_scene_stats(const bc_context* ctx, int64_t* out, int n_out);
  * Host pointers; copies in and out are part of the call.
  */
 bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out, int32_t* prim_out);
-/* Same on device pointers, enqueued on `stream` (a cudaStream_t, NULL = legacy default); asynchronous. */
+/* Same on device pointers, enqueued on `stream` (a cudaStream_t, NULL = legacy default); asynchronous.
+ * The context's scratch (ray order, per-ray records of the split passes, work
+ * counter) is shared by its calls: calls of one context must not overlap on
+ * different streams. */
 bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, float* d_t_out, int32_t* d_prim_out,
                             void* stream);
 /* Any hit (Scene.Occluded, renderer.go:851-895): occluded_out[i] = 1 if any primitive

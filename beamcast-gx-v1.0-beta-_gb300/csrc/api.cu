@@ -136,7 +136,8 @@ void bc_destroy(bc_context* ctx) {
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_tri, &ctx->d_slot64, &ctx->d_snorm, &ctx->d_slot_prim, &ctx->d_mats,
                     &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ,
                     &ctx->d_kids8, &ctx->d_geom, &ctx->d_build, &ctx->d_build_out, &ctx->d_order[0],
-                    &ctx->d_order[1], &ctx->d_order[2], &ctx->d_rec[0], &ctx->d_rec[1], &ctx->d_rec[2]})
+                    &ctx->d_order[1], &ctx->d_order[2], &ctx->d_rec[0], &ctx->d_rec[1], &ctx->d_rec[2],
+                    &ctx->d_rec_any})
     b->release();
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->d_work) cudaFree(ctx->d_work);
@@ -406,7 +407,14 @@ bc_status bc_occluded_device(bc_context* ctx, const float* d_rays, int64_t n, ui
   if (((uintptr_t)d_rays & 15u) != 0) return set_error(ctx, BC_ERR_INVALID_ARG, "rays must be 16-byte aligned");
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-  cudaError_t e = launch_raycast_any(ctx->ds, (const float4*)d_rays, n, d_out, ctx->d_status, ctx->raycast_variant, st);
+  void* rec = nullptr;
+  if (ctx->raycast_split && n > 0) {
+    cudaError_t e = ctx->d_rec_any.ensure(any_record_bytes(n));
+    if (e) return cuda_status(ctx, e, "any-hit record buffers");
+    rec = ctx->d_rec_any.p;
+  }
+  cudaError_t e = launch_raycast_any(ctx->ds, (const float4*)d_rays, n, d_out, ctx->d_status, ctx->raycast_variant,
+                                     ctx->d_work + 3, rec, st);
   return cuda_status(ctx, e, "any-hit launch");
 }
 
@@ -419,10 +427,15 @@ bc_status bc_occluded(bc_context* ctx, const float* rays, int64_t n, uint8_t* ou
   cudaError_t e;
   if ((e = ctx->d_rays.ensure((size_t)n * 32)) || (e = ctx->d_occ.ensure((size_t)n)))
     return cuda_status(ctx, e, "any-hit buffers");
+  void* rec = nullptr;
+  if (ctx->raycast_split) {
+    if ((e = ctx->d_rec_any.ensure(any_record_bytes(n)))) return cuda_status(ctx, e, "any-hit record buffers");
+    rec = ctx->d_rec_any.p;
+  }
   e = cudaMemcpyAsync(ctx->d_rays.p, rays, (size_t)n * 32, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess)
     e = launch_raycast_any(ctx->ds, ctx->d_rays.as<float4>(), n, ctx->d_occ.as<uint8_t>(), ctx->d_status, ctx->raycast_variant,
-                           ctx->stream);
+                           ctx->d_work + 3, rec, ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, ctx->d_occ.p, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_status(ctx, e, "any hit");

@@ -92,6 +92,7 @@ struct bc_context {
   bcgx::DevBuf d_order[3];    // ray order scratch: [0], [1] the two streams of bc_raycast, [2] bc_raycast_device
   int raycast_split = 1;      // exact closest hit as walk + settlement passes (bc_set_option "raycast_split")
   bcgx::DevBuf d_rec[3];      // per-ray records of the split passes, indexed as d_order
+  bcgx::DevBuf d_rec_any;     // listed rays of the split any-hit passes
   // ray-cast staging
   bcgx::DevBuf d_rays, d_t, d_prim, d_occ;
   unsigned* d_status = nullptr;

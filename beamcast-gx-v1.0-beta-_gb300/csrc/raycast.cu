@@ -431,6 +431,146 @@ __global__ void __launch_bounds__(128) k_closest_exact_list(SceneView sv, const 
   }
 }
 
+// ---- exact any hit in passes -----------------------------------------------------
+// The same split for Scene.Occluded: the walk (no fp64 code) decides a ray when
+// a triangle certainly blocks it or when no triangle might; a ray with
+// undecided ("maybe") triangles is appended to a list with up to kPending of
+// them, which the second pass tests in fp64 (triAnyHit's operation order); a
+// ray with more is re-traced there by the one-kernel exact any-hit walk.
+struct AnyRecords {
+  long long* idx;   // [n] listed rays
+  int32_t* npend;   // [n] maybe-triangles listed; kPending + 1: list overflowed
+  int32_t* pslot;   // [kPending * n]
+  unsigned long long* count;
+};
+
+AnyRecords any_records(void* p, int64_t n) {
+  char* q = (char*)p;
+  AnyRecords r;
+  r.count = (unsigned long long*)q;
+  q += 256;
+  r.idx = (long long*)q;
+  q += up256((size_t)n * 8);
+  r.npend = (int32_t*)q;
+  q += up256((size_t)n * 4);
+  r.pslot = (int32_t*)q;
+  return r;
+}
+
+// ExactAnyLeaf's decisions without its fp64 test: a maybe-triangle is listed.
+struct FilterAnyLeaf {
+  const SceneView& sv;
+  const Ray32& r;
+  float tmax_ray;
+  float tlim;
+  bool done, hit;
+  int npend;
+  int32_t pend[kPending];
+
+  __device__ FilterAnyLeaf(const SceneView& s, const Ray32& ray) : sv(s), r(ray) { reset(0.0f); }
+  __device__ __forceinline__ void reset(float tmax) {
+    tmax_ray = tmax;
+    tlim = widen(tmax);
+    done = false;
+    hit = false;
+    npend = 0;
+  }
+  __device__ __forceinline__ void operator()(uint32_t ref) {
+    const int cnt = (int)((ref >> 27) & 15u) + 1;
+    const int s0 = (int)(ref & kSlotMask);
+    for (int k = 0; k < cnt && !done; k++) {
+      const int s = s0 + k;
+      const float4 A = __ldg(sv.tri + 3 * s);
+      const float4 E1 = __ldg(sv.tri + 3 * s + 1);
+      const float4 E2 = __ldg(sv.tri + 3 * s + 2);
+      const TriClass tc = tri_classify(A, E1, E2, r, tmax_ray, tlim);
+      if (tc.state == kHit) {
+        hit = true;
+        done = true;
+      } else if (tc.state == kMaybe) {
+        if (npend < kPending) {
+          pend[npend++] = s;
+        } else {
+          npend = kPending + 1;
+          done = true;
+        }
+      }
+    }
+  }
+};
+
+template <int STACK>
+__global__ void __launch_bounds__(128, 10) k_any_walk(SceneView sv, const float4* __restrict__ rays, int64_t n,
+                                                      uint8_t* __restrict__ out, AnyRecords rec, unsigned* status,
+                                                      unsigned long long* work) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  long long idx = -1;
+  bool exhausted = false;
+  Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
+  FilterAnyLeaf leaf(sv, r);
+  Walker<STACK> w;
+  w.reset(r);
+  for (;;) {
+    const bool need = idx < 0 && !exhausted;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if ((int)lane == leader) base = atomicAdd(work, (unsigned long long)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const unsigned long long my = base + (unsigned long long)__popc(m & below);
+        if (my < (unsigned long long)n) {
+          idx = (long long)my;
+          const float4 a = __ldg(rays + 2 * idx), b = __ldg(rays + 2 * idx + 1);
+          r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
+          leaf.reset(b.w);
+          w.reset(r);
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, idx >= 0)) break;
+    if (idx >= 0 && w.step(sv, r, leaf, status)) {
+      if (leaf.hit || leaf.npend == 0) {
+        out[idx] = leaf.hit ? 1 : 0;
+      } else {
+        const unsigned long long k = atomicAdd(rec.count, 1ull);
+        rec.idx[k] = idx;
+        rec.npend[k] = leaf.npend;
+        const int np = min(leaf.npend, kPending);
+        for (int j = 0; j < np; j++) rec.pslot[(size_t)j * n + k] = leaf.pend[j];
+      }
+      idx = -1;
+    }
+  }
+}
+
+template <int STACK>
+__global__ void __launch_bounds__(128) k_any_settle(SceneView sv, const float4* __restrict__ rays, int64_t n,
+                                                    uint8_t* __restrict__ out, AnyRecords rec, unsigned* status) {
+  const long long cnt = (long long)*((volatile unsigned long long*)rec.count);
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += (long long)gridDim.x * blockDim.x) {
+    const long long i = rec.idx[k];
+    const float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
+    const int np = rec.npend[k];
+    if (np > kPending) {
+      const Ray32 r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
+      out[i] = any_hit_exact<STACK, false>(sv, r, b.w, status) ? 1 : 0;
+      continue;
+    }
+    const D3 o{(double)a.x, (double)a.y, (double)a.z}, d{(double)b.x, (double)b.y, (double)b.z};
+    bool hit = false;
+    for (int j = 0; j < np && !hit; j++) {
+      double t;
+      hit = tri_hit64(sv.slot64 + 9 * (size_t)rec.pslot[(size_t)j * n + k], o, d, (double)a.w, (double)b.w, &t);
+    }
+    out[i] = hit ? 1 : 0;
+  }
+}
+
 template <int STACK>
 __global__ void __launch_bounds__(128) k_closest_fast_persistent(SceneView sv, const float4* __restrict__ rays,
                                                                  int64_t n, float* __restrict__ t_out,
@@ -612,6 +752,24 @@ cudaError_t closest_split(const DeviceScene& s, const float4* rays, int64_t n, f
   return cudaGetLastError();
 }
 
+template <int STACK>
+cudaError_t any_split(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
+                      unsigned long long* work, void* rec_scratch, cudaStream_t st) {
+  static int blocks = 0;
+  if (!blocks) blocks = persistent_blocks(k_any_walk<STACK>);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const AnyRecords rec = any_records(rec_scratch, n);
+  cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), st);
+  if (!e) e = cudaMemsetAsync(rec.count, 0, sizeof(unsigned long long), st);
+  if (e) return e;
+  const int64_t grid = (n + 127) / 128;
+  k_any_walk<STACK><<<(int)std::min<int64_t>(blocks, grid), 128, 0, st>>>(view_of(s), rays, n, out, rec, status, work);
+  k_any_settle<STACK><<<std::max(sms, 1) * 4, 128, 0, st>>>(view_of(s), rays, n, out, rec, status);
+  return cudaGetLastError();
+}
+
 template <int STACK, int MINB>
 cudaError_t any_stack(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
                       cudaStream_t st) {
@@ -652,7 +810,8 @@ cudaError_t closest_var(const DeviceScene& s, const float4* rays, int64_t n, flo
 
 template <int STACK>
 cudaError_t any_var(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status, int variant,
-                    cudaStream_t st) {
+                    unsigned long long* work, void* rec_scratch, cudaStream_t st) {
+  if (rec_scratch && work && !s.has_spheres) return any_split<STACK>(s, rays, n, out, status, work, rec_scratch, st);
   switch (variant) {
     case 6: return any_stack<STACK, 6>(s, rays, n, out, status, st);
     case 8: return any_stack<STACK, 8>(s, rays, n, out, status, st);
@@ -661,6 +820,10 @@ cudaError_t any_var(const DeviceScene& s, const float4* rays, int64_t n, uint8_t
 }
 
 }  // namespace
+
+size_t any_record_bytes(int64_t n) {
+  return 256 + up256((size_t)n * 8) + up256((size_t)n * 4) + up256((size_t)n * 4 * kPending);
+}
 
 size_t exact_record_bytes(int64_t n) {
   return 256 + 3 * up256((size_t)n * 4) + 2 * up256((size_t)n * 4 * kPending) + up256((size_t)n * 8);
@@ -704,12 +867,12 @@ cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int
 }
 
 cudaError_t launch_raycast_any(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
-                               int variant, cudaStream_t st) {
+                               int variant, unsigned long long* work, void* rec_scratch, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   switch (stack_variant(s.stack_need)) {
-    case 64: return any_var<64>(s, rays, n, out, status, variant, st);
-    case 128: return any_var<128>(s, rays, n, out, status, variant, st);
-    case 256: return any_var<256>(s, rays, n, out, status, variant, st);
+    case 64: return any_var<64>(s, rays, n, out, status, variant, work, rec_scratch, st);
+    case 128: return any_var<128>(s, rays, n, out, status, variant, work, rec_scratch, st);
+    case 256: return any_var<256>(s, rays, n, out, status, variant, work, rec_scratch, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -233,6 +233,19 @@ def run_gpu(args):
     kernel_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(kernel_ms)
 
+    # any hit (bc_occluded_device) over the same rays: reported beside the metric
+    d_occ = torch.empty(N_RAYS, dtype=torch.uint8, device=dev)
+    ev_any = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+    with torch.cuda.stream(stream):
+        ctx.occluded_device(d_rays.data_ptr(), N_RAYS, d_occ.data_ptr(), stream.cuda_stream)
+        for a, b in ev_any:
+            flush.zero_()
+            a.record(stream)
+            ctx.occluded_device(d_rays.data_ptr(), N_RAYS, d_occ.data_ptr(), stream.cuda_stream)
+            b.record(stream)
+    torch.cuda.synchronize()
+    any_ms = sum(a.elapsed_time(b) for a, b in ev_any) / len(ev_any)
+
     # e2e: the host-buffer entry point, pinned host rays, copies inside the region
     h_rays = torch.from_numpy(rays).pin_memory()
     h_np = h_rays.numpy()
@@ -291,6 +304,8 @@ def run_gpu(args):
                                       (4 if ctx.get_option("raycast_sort") and N_RAYS >= 65536 else 0)),
         "raycast_minblocks": ctx.get_option("raycast_minblocks"),
         "raycast_split": ctx.get_option("raycast_split"),
+        "any_hit": {"value": N_RAYS / (any_ms / 1e3) / 1e6, "unit": "Mrays/s", "ms": any_ms,
+                    "call": "bc_occluded_device, same rays, L2 flushed"},
         "raycast_exact": ctx.get_option("raycast_exact"),
         "clocks": clk,
         "kernel_ms": [round(x, 4) for x in kernel_ms],

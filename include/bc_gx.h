@@ -409,8 +409,10 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *                        (ten 128-thread blocks per SM), an fp64 settlement pass,
  *                        and a re-trace of the rays whose contender list overflowed;
  *                        it holds 52 bytes of device scratch per ray of a call (per
- *                        chunk for bc_raycast). 0: one kernel walks and settles.
- *                        Both give the same results.
+ *                        chunk for bc_raycast). The exact any hit likewise: a walk,
+ *                        then fp64 tests of the undecided triangles of the rays
+ *                        the walk could not decide (28 bytes per ray). 0: one
+ *                        kernel walks and settles. Both give the same results.
  *   "raycast_minblocks"  1, 6 or 8: register budget of the one-kernel ray-cast
  *                        kernels (resident 128-thread blocks per SM the allocation
  *                        must allow).

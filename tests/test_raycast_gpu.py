@@ -216,7 +216,7 @@ def test_split_passes_parity(gpu_ctx, orc, which):
     """raycast_split 1 (the default: walk pass without fp64 code, fp64 settlement
     pass, and a pass that re-traces rays whose contender list overflowed) returns
     the same hits and distances as the one-kernel exact form (raycast_split 0),
-    and both match the oracle."""
+    and both match the oracle; the same for the any hit."""
     if which == "random":
         spec = scenes.random_triangles(100_000, seed=scenes.SEED_C2 + 7)
         rays = scenes.random_rays(262_144, seed=15)
@@ -235,10 +235,16 @@ def test_split_passes_parity(gpu_ctx, orc, which):
     assert gpu_ctx.get_option("raycast_split") == 1
     _check(gpu_ctx, ref, rays, allow_ties=which != "random")
     two = gpu_ctx.raycast(rays)
+    occ2 = gpu_ctx.occluded(rays)
     try:
         gpu_ctx.set_option("raycast_split", 0)
         _check(gpu_ctx, ref, rays, allow_ties=which != "random")
         one = gpu_ctx.raycast(rays)
+        occ1 = gpu_ctx.occluded(rays)
     finally:
         gpu_ctx.set_option("raycast_split", 1)
     assert np.array_equal(one[1], two[1]) and np.array_equal(one[0], two[0])
+    # any hit: both forms, the oracle's Occluded, and closest-hit existence agree
+    occ_ref, _ = ref.occluded_f32(rays)
+    assert np.array_equal(occ2, occ1) and np.array_equal(occ2, occ_ref)
+    assert np.array_equal(occ2, two[1] >= 0)

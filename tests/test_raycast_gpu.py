@@ -189,11 +189,12 @@ def test_full_size_c2_properties_and_sample(gpu_ctx, orc):
     assert np.all(_ulp_diff(t[idx][h], tr[h].astype(np.float32)) == 0)
 
 
-def _stacked_triangles(n_base=300, copies=6, seed=41):
-    """Large random triangles, each repeated `copies` times with offsets of
-    1e-7 along z (the first two copies coincide): a ray through a stack meets
-    more contenders with overlapping distance intervals than the walk's list
-    holds, which sends it to the third pass of the split form."""
+def _stacked_triangles(n_base=300, copies=8, seed=41):
+    """Large random triangles, each repeated `copies` times: the first six copies
+    coincide, the others are offset by 1e-7 along z. A ray through a stack meets
+    at least six certain hits with the same distance interval, more contenders
+    than the walk's list holds (four), which sends it to the third pass of the
+    split form."""
     rng = np.random.default_rng(seed)
     c = rng.uniform(0.1, 0.9, (n_base, 3))
     e1 = rng.normal(size=(n_base, 3)) * 0.15
@@ -203,7 +204,7 @@ def _stacked_triangles(n_base=300, copies=6, seed=41):
     layers = []
     for k in range(copies):
         off = np.zeros(9)
-        off[2::3] = max(0, k - 1) * 1e-7
+        off[2::3] = max(0, k - 5) * 1e-7
         layers.append(base + off)
     sp = scenes.SceneSpec(name="stacked", bvh_mode="SAH", bvh_bins=32, bvh_leaf=4)
     m = sp.material(scenes.Material(scenes.MAT_DIFFUSE, (0.5, 0.5, 0.5)))

@@ -1361,8 +1361,10 @@ static WaveShape wave_shape(int cap, int bounces, bool lights, const GradArgs* g
   w.gen_grid = (cap + 255) / 256;
   w.ext_grid = ext[var];
   w.con_grid = con;
-  w.shade_grid = sm_count() * 8;
-  w.acc_grid = sm_count() * 8;
+  // grid-stride kernels at three resident 256-thread blocks per SM (their
+  // register budget): one wave of blocks, no partial last wave
+  w.shade_grid = sm_count() * 3;
+  w.acc_grid = sm_count() * 3;
   w.bounces = bounces;
   w.lights = lights;
   w.grad = grad;
@@ -1415,10 +1417,12 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
 // Runs `n_waves` waves, through one captured CUDA graph when the option allows.
 template <int STACK, bool SPH>
 static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const ShadeScene& sc, int64_t n_waves,
-                           const GradArgs* grad, bool recursive, bool alt) {
+                           int wave_paths, const GradArgs* grad, bool recursive, bool alt) {
   RenderBuffers* rb = ctx->rb;
   cudaStream_t st = ctx->stream;
-  WaveShape w = wave_shape<STACK, SPH>(rb->cap, bounces, lights, grad, ctx->render_extend);
+  // generate's grid covers this render's wave, not the slots a larger earlier
+  // render left allocated
+  WaveShape w = wave_shape<STACK, SPH>(wave_paths, bounces, lights, grad, ctx->render_extend);
   w.recursive = recursive;
   w.alt = alt;
   // A wave graph pays for its capture when a render has several waves, or when
@@ -1703,14 +1707,14 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
     else if (stack == 128) bst = sph ? run_plain<128, true>(ctx, sc, views, alt) : run_plain<128, false>(ctx, sc, views, alt);
     else bst = sph ? run_plain<256, true>(ctx, sc, views, alt) : run_plain<256, false>(ctx, sc, views, alt);
   } else if (stack == 64)
-    bst = sph ? run_waves<64, true>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt)
-              : run_waves<64, false>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt);
+    bst = sph ? run_waves<64, true>(ctx, max_bounces, lights, sc, n_waves, bsh.cap, grad, rec_bounces > 0, alt)
+              : run_waves<64, false>(ctx, max_bounces, lights, sc, n_waves, bsh.cap, grad, rec_bounces > 0, alt);
   else if (stack == 128)
-    bst = sph ? run_waves<128, true>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt)
-              : run_waves<128, false>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt);
+    bst = sph ? run_waves<128, true>(ctx, max_bounces, lights, sc, n_waves, bsh.cap, grad, rec_bounces > 0, alt)
+              : run_waves<128, false>(ctx, max_bounces, lights, sc, n_waves, bsh.cap, grad, rec_bounces > 0, alt);
   else
-    bst = sph ? run_waves<256, true>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt)
-              : run_waves<256, false>(ctx, max_bounces, lights, sc, n_waves, grad, rec_bounces > 0, alt);
+    bst = sph ? run_waves<256, true>(ctx, max_bounces, lights, sc, n_waves, bsh.cap, grad, rec_bounces > 0, alt)
+              : run_waves<256, false>(ctx, max_bounces, lights, sc, n_waves, bsh.cap, grad, rec_bounces > 0, alt);
   if (bst) return bst;
   k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sum, rb->out, rb->adapt.n);
   if (rb->want_sumsq)

@@ -116,6 +116,24 @@ def _make_workload():
     return spec, rays
 
 
+def rank_rays(rank: int, n: int | None = None):
+    """The rays one rank casts: the workload's seeded rays on rank 0, the next
+    seeds on the other ranks (weak scaling: every rank casts its own rays over
+    the replicated scene, with no collective on the data path)."""
+    from bcgx import scenes
+    return scenes.random_rays(N_RAYS if n is None else n, seed=scenes.SEED_C3 + rank)
+
+
+def max_over_ranks(dist, values, device):
+    """Element-wise maximum of per-rank values over the process group (a job's
+    time is its slowest rank's); without a group, the values themselves."""
+    import torch
+    t = torch.tensor([float(v) for v in values], device=device, dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def cpu_baseline(spec, rays, seconds_target=15.0, threads=0):
     """The oracle (fp64 restatement of Scene.Hit) on a bounded sample of rays.
     Returns (Mpath-segments/s, cores, sample description, algorithmic bytes per ray)."""
@@ -189,6 +207,8 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     from bcgx import scenes
     spec, rays = _make_workload()
+    if rank:
+        rays = rank_rays(rank)
     scene = scenes.to_scene(spec)
     ctx = bcgx.Context(local)
     if args.minblocks:
@@ -260,9 +280,7 @@ def run_gpu(args):
     clk = clocks.stop()
 
     if dist:
-        tt = torch.tensor([total_ms, e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms, e2e_s = float(tt[0]), float(tt[1])
+        total_ms, e2e_s = max_over_ranks(dist, [total_ms, e2e_s], dev)
         dist.barrier()
     if rank != 0:
         ctx.close()

@@ -63,7 +63,7 @@ class DiffDescC(C.Structure):
 class TuneReportC(C.Structure):
     _fields_ = [("raycast_minblocks", C.c_int32), ("raycast_sort", C.c_int32), ("render_wave_cap", C.c_int64),
                 ("n_timed", C.c_int32), ("render_extend", C.c_int32), ("best_ms", C.c_double), ("default_ms", C.c_double),
-                ("worst_ms", C.c_double), ("raycast_split", C.c_int32), ("reserved", C.c_int32)]
+                ("worst_ms", C.c_double), ("raycast_split", C.c_int32), ("render_shade_block", C.c_int32)]
 
 
 class PostDescC(C.Structure):

@@ -500,6 +500,11 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     ctx->render_extend = (int)value;
     return BC_OK;
   }
+  if (n == "render_shade_block") {
+    if (value != 128 && value != 256) return set_error(ctx, BC_ERR_INVALID_ARG, "render_shade_block must be 128 or 256");
+    ctx->render_shade_block = (int)value;
+    return BC_OK;
+  }
   return set_error(ctx, BC_ERR_INVALID_ARG, "unknown option " + n);
 }
 
@@ -516,6 +521,7 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
   if (n == "render_graph") { *value = ctx->render_graph; return BC_OK; }
   if (n == "render_engine") { *value = ctx->render_engine; return BC_OK; }
   if (n == "render_extend") { *value = ctx->render_extend; return BC_OK; }
+  if (n == "render_shade_block") { *value = ctx->render_shade_block; return BC_OK; }
   return BC_ERR_INVALID_ARG;
 }
 

@@ -9,7 +9,8 @@
 //             runs after one warm-up, on the caller's rays.
 //   render:   the extend kernel's variant (render_extend 0, 1, 2: register
 //             budget and where the ray lives, i.e. resident blocks per SM) at
-//             the current wave size, then paths per wave (render_wave_cap
+//             the current wave size, the shading kernel's block shape
+//             (render_shade_block 256, 128), then paths per wave (render_wave_cap
 //             2^22 .. 2^26) with the chosen variant, on the caller's batch with
 //             spp scaled down so one candidate traces at most 2^27 paths.
 //             Images depend on neither option, so no candidate changes a result.
@@ -113,6 +114,7 @@ bc_status bc_autotune_raycast(bc_context* ctx, const float* d_rays, int64_t n, b
   rep.raycast_sort = ctx->raycast_sort;
   rep.render_wave_cap = ctx->render_wave_cap;
   rep.render_extend = ctx->render_extend;
+  rep.render_shade_block = ctx->render_shade_block;
   if (out) *out = rep;
   return BC_OK;
 }
@@ -139,7 +141,7 @@ bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_vi
     sample += (long long)r.s.width * r.s.height * spp;
   }
   const long long keep = ctx->render_wave_cap;
-  const int keep_ext = ctx->render_extend;
+  const int keep_ext = ctx->render_extend, keep_sb = ctx->render_shade_block;
   bc_tune_report rep;
   std::memset(&rep, 0, sizeof(rep));
   // one timed candidate: the second of two renders of the sample (the first
@@ -159,6 +161,7 @@ bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_vi
   auto restore = [&]() {
     ctx->render_wave_cap = keep;
     ctx->render_extend = keep_ext;
+    ctx->render_shade_block = keep_sb;
   };
   // stage 1: the extend variant at the current wave size
   int best_ext = keep_ext;
@@ -177,6 +180,22 @@ bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_vi
     }
   }
   ctx->render_extend = best_ext;
+  // stage 1b: the shading kernel's block shape, with that variant
+  int best_sb = keep_sb;
+  {
+    const int other = keep_sb == 128 ? 256 : 128;
+    ctx->render_shade_block = other;
+    double ms = 0.0;
+    if ((st = time_render(&ms))) {
+      restore();
+      return st;
+    }
+    if (ms < best_ext_ms) {
+      best_ext_ms = ms;
+      best_sb = other;
+    }
+    ctx->render_shade_block = best_sb;
+  }
   // stage 2: the wave size with that variant
   long long best_cap = keep;
   rep.best_ms = best_ext_ms;
@@ -203,6 +222,7 @@ bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_vi
   rep.raycast_sort = ctx->raycast_sort;
   rep.render_wave_cap = best_cap;
   rep.render_extend = best_ext;
+  rep.render_shade_block = best_sb;
   rep.raycast_split = ctx->raycast_split;
   if (out) *out = rep;
   return BC_OK;

@@ -103,6 +103,7 @@ struct bc_context {
   int render_graph = 1;                 // replay a captured wave graph (bc_set_option "render_graph")
   int render_engine = 0;                // 0: wave engine, 1: one kernel per view (bc_set_option "render_engine")
   int render_extend = 1;                // k_extend variant 0..2 (bc_set_option "render_extend")
+  int render_shade_block = 256;         // k_shade block size, 128 or 256 (bc_set_option "render_shade_block")
   struct DiffState* diff = nullptr;  // differentiable rendering (diff.cu)
   struct PhotonCache* photons = nullptr;  // photon maps of the photon-mapping integrator (photon.cu)
   int photon_grid = 1;                    // gathers read the dense cell table (bc_set_option "photon_grid")

@@ -739,7 +739,7 @@ __device__ __forceinline__ void unwind_recursive(const ViewGPU& wp, const ShadeS
 }
 
 template <bool ALT>
-__global__ void __launch_bounds__(256, 3) k_shade(const ViewGPU* __restrict__ views, int n_mats, ShadeScene sc,
+__device__ __forceinline__ void shade_body(const ViewGPU* __restrict__ views, int n_mats, ShadeScene sc,
                                                PathSoA ps, const int* __restrict__ qcur, int* __restrict__ qnext,
                                                ShadowSoA sh, WaveCounters* cnt, int cur, int bounce,
                                                float4* __restrict__ guide_nd, uint32_t* __restrict__ guide_c,
@@ -792,6 +792,23 @@ __global__ void __launch_bounds__(256, 3) k_shade(const ViewGPU* __restrict__ vi
     }
   }
 }
+
+// Block shape of the shading kernel (bc_set_option "render_shade_block", chosen
+// per workload by bc_autotune_render): 256 threads at three blocks per SM, or
+// 128 threads at six; the same register budget and resident threads, a
+// different scheduling granularity of the grid-stride loop.
+#define BC_SHADE_ARGS                                                                                       \
+  const ViewGPU *__restrict__ views, int n_mats, ShadeScene sc, PathSoA ps, const int *__restrict__ qcur,  \
+      int *__restrict__ qnext, ShadowSoA sh, WaveCounters *cnt, int cur, int bounce,                       \
+      float4 *__restrict__ guide_nd, uint32_t *__restrict__ guide_c, const uint32_t *__restrict__ guide_jit, \
+      GradRec rec, RecurRec rr, long long sh_cap, unsigned *status
+#define BC_SHADE_PASS views, n_mats, sc, ps, qcur, qnext, sh, cnt, cur, bounce, guide_nd, guide_c, guide_jit, rec, rr, sh_cap, status
+template <bool ALT>
+__global__ void __launch_bounds__(256, 3) k_shade(BC_SHADE_ARGS) { shade_body<ALT>(BC_SHADE_PASS); }
+template <bool ALT>
+__global__ void __launch_bounds__(128, 6) k_shade_128(BC_SHADE_ARGS) { shade_body<ALT>(BC_SHADE_PASS); }
+#undef BC_SHADE_ARGS
+#undef BC_SHADE_PASS
 
 // ---- connect -----------------------------------------------------------------
 template <int STACK, bool SPH>
@@ -1332,7 +1349,8 @@ static int persistent_grid(const void* fn, int block) {
 
 // Launch shape of one wave; computed before any stream capture.
 struct WaveShape {
-  int ext;  // k_extend variant (render_extend)
+  int ext;          // k_extend variant (render_extend)
+  int shade_block;  // k_shade block size (render_shade_block)
   int gen_grid, ext_grid, con_grid, shade_grid, acc_grid;
   int bounces;
   bool lights;
@@ -1351,7 +1369,7 @@ static const void* extend_kernel(int var) {
 }
 
 template <int STACK, bool SPH>
-static WaveShape wave_shape(int cap, int bounces, bool lights, const GradArgs* grad, int ext_var) {
+static WaveShape wave_shape(int cap, int bounces, bool lights, const GradArgs* grad, int ext_var, int shade_block) {
   static int ext[kExtendVariants] = {0, 0, 0}, con = 0;
   const int var = ext_var >= 0 && ext_var < kExtendVariants ? ext_var : 1;
   if (!ext[var]) ext[var] = persistent_grid(extend_kernel<STACK, SPH>(var), 128);
@@ -1361,9 +1379,10 @@ static WaveShape wave_shape(int cap, int bounces, bool lights, const GradArgs* g
   w.gen_grid = (cap + 255) / 256;
   w.ext_grid = ext[var];
   w.con_grid = con;
-  // grid-stride kernels at three resident 256-thread blocks per SM (their
-  // register budget): one wave of blocks, no partial last wave
-  w.shade_grid = sm_count() * 3;
+  // grid-stride kernels at their resident blocks per SM (three of 256 threads,
+  // six of 128: their register budget): one wave of blocks, no partial last wave
+  w.shade_block = shade_block == 128 ? 128 : 256;
+  w.shade_grid = sm_count() * (w.shade_block == 128 ? 6 : 3);
   w.acc_grid = sm_count() * 3;
   w.bounces = bounces;
   w.lights = lights;
@@ -1393,14 +1412,18 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
     else
       k_extend_10<STACK, SPH><<<w.ext_grid, 128, 0, st>>>(sc.sv, rb->views, rb->ps, rb->q[cur], c, cur, ctx->d_status);
     const GradRec rec = w.grad ? rb->grec : GradRec{nullptr, nullptr, nullptr, 0};
-    if (w.alt)
-      k_shade<true><<<w.shade_grid, 256, 0, st>>>(rb->views, ctx->ds.n_mats, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1],
-                                                  rb->sh, c, cur, b, rb->guide_nd, rb->guide_c, rb->guide_jit, rec,
-                                                  rr, rb->sh_cap, ctx->d_status);
-    else
-      k_shade<false><<<w.shade_grid, 256, 0, st>>>(rb->views, ctx->ds.n_mats, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1],
-                                                   rb->sh, c, cur, b, rb->guide_nd, rb->guide_c, rb->guide_jit, rec,
-                                                   rr, rb->sh_cap, ctx->d_status);
+#define BC_SHADE_LAUNCH(KERNEL, BLOCK)                                                                         \
+  KERNEL<<<w.shade_grid, BLOCK, 0, st>>>(rb->views, ctx->ds.n_mats, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1], rb->sh, \
+                                        c, cur, b, rb->guide_nd, rb->guide_c, rb->guide_jit, rec, rr, rb->sh_cap,   \
+                                        ctx->d_status)
+    if (w.shade_block == 128) {
+      if (w.alt) BC_SHADE_LAUNCH(k_shade_128<true>, 128);
+      else BC_SHADE_LAUNCH(k_shade_128<false>, 128);
+    } else {
+      if (w.alt) BC_SHADE_LAUNCH(k_shade<true>, 256);
+      else BC_SHADE_LAUNCH(k_shade<false>, 256);
+    }
+#undef BC_SHADE_LAUNCH
     if (w.lights)
       k_connect<STACK, SPH><<<w.con_grid, 128, 0, st>>>(sc.sv, rb->ps, rb->sh, c, rr, rb->sh_cap, ctx->d_status);
     cur ^= 1;
@@ -1422,7 +1445,7 @@ static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const Shad
   cudaStream_t st = ctx->stream;
   // generate's grid covers this render's wave, not the slots a larger earlier
   // render left allocated
-  WaveShape w = wave_shape<STACK, SPH>(wave_paths, bounces, lights, grad, ctx->render_extend);
+  WaveShape w = wave_shape<STACK, SPH>(wave_paths, bounces, lights, grad, ctx->render_extend, ctx->render_shade_block);
   w.recursive = recursive;
   w.alt = alt;
   // A wave graph pays for its capture when a render has several waves, or when
@@ -1432,6 +1455,7 @@ static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const Shad
   if (use_graph) {
     // every value the captured launches were given
     std::vector<uintptr_t> key = {(uintptr_t)STACK, (uintptr_t)SPH, (uintptr_t)w.ext, (uintptr_t)w.ext_grid,
+                                  (uintptr_t)w.shade_block, (uintptr_t)w.shade_grid,
                                   (uintptr_t)bounces, (uintptr_t)lights,
                                   (uintptr_t)rb->cap, (uintptr_t)w.gen_grid, (uintptr_t)rb->q[0], (uintptr_t)rb->q[1],
                                   (uintptr_t)rb->cnt, (uintptr_t)rb->bs, (uintptr_t)rb->views, (uintptr_t)rb->seq_xy,

@@ -482,7 +482,8 @@ def run_render(args):
             "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (fp64 primary rays)", "data": "synthetic, seeded",
             "config": {"workload": workload, "spp": st.spp, "segments_per_frame": rays // max(1, args.steps),
-                       "extend_variant": ctx.get_option("render_extend")},
+                       "extend_variant": ctx.get_option("render_extend"),
+                       "shade_block": ctx.get_option("render_shade_block")},
             "e2e": {"value": e2e_r / e2e_t / 1e6, "unit": METRIC, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": st.width * st.height * 16},
             "gpu_launches": None, "clocks": clk}
@@ -595,7 +596,8 @@ def run_batch(args):
                        "pixels": px, "paths": paths, "segments_per_step": br // max(1, args.steps),
                        "host_bvh_build_s": round(build_s, 2),
                        "wave_cap": ctx.get_option("render_wave_cap"),
-                       "extend_variant": ctx.get_option("render_extend")},
+                       "extend_variant": ctx.get_option("render_extend"),
+                       "shade_block": ctx.get_option("render_shade_block")},
             "plain": {"value": plain_v, "unit": METRIC, "ms_per_step": 1e3 * sum(pt) / args.steps,
                       "form": f"{n_views} sequential one-view bc_render_batch calls"},
             "batched_over_plain": value / plain_v,

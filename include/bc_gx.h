@@ -444,6 +444,8 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *                        budget (nine 128-thread blocks per SM); 1 (default):
  *                        ray in registers, 48 registers (ten blocks); 2: ray
  *                        in shared memory, 40 registers (twelve blocks).
+ *   "render_shade_block" 256 (default) or 128: threads per block of the wave
+ *                        engine's shading kernel (three or six blocks per SM).
  *   "render_engine"      0 (default): the wave engine; 1: one kernel launch per
  *                        view, one thread per pixel looping over samples and
  *                        bounces (the reference OpenCL kernel's shape, kept as the
@@ -464,8 +466,9 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
  * raycast_minblocks 6, 8, 1 and raycast_sort 1 and 0 (exact mode; plain fp32
  * mode: raycast_sort only). Best of two timed runs each (CUDA events).
  * bc_autotune_render: the views as for bc_render_batch; first render_extend
- * 1, 0, 2 at the current wave size, then render_wave_cap 2^22 .. 2^26 (up to
- * twice the sample's paths) with the chosen variant. Each view's spp is scaled
+ * 1, 0, 2 at the current wave size, then the other render_shade_block, then
+ * render_wave_cap 2^22 .. 2^26 (up to twice the sample's paths) with the
+ * chosen variants. Each view's spp is scaled
  * down so that a candidate traces at most 2^27 paths; the adaptive stop is off
  * while timing. The second of two runs is timed.
  */
@@ -475,7 +478,7 @@ typedef struct bc_tune_report {
   int32_t n_timed;                          /* candidates timed */
   int32_t render_extend;                    /* option in force after the call */
   double best_ms, default_ms, worst_ms;     /* chosen, the options before the call, slowest */
-  int32_t raycast_split, reserved;          /* option in force after the call */
+  int32_t raycast_split, render_shade_block; /* options in force after the call */
 } bc_tune_report;
 bc_status bc_autotune_raycast(bc_context* ctx, const float* d_rays, int64_t n, bc_tune_report* out);
 bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_views, bc_tune_report* out);

@@ -51,8 +51,9 @@ def test_autotune_render_keeps_images(gpu_ctx):
     before, _ = gpu_ctx.render_batch(views)
     try:
         rep = gpu_ctx.autotune_render(views)
-        assert rep["n_timed"] >= 3 and rep["render_wave_cap"] >= 1 << 22
-        assert rep["render_extend"] in (0, 1, 2)
+        assert rep["n_timed"] >= 4 and rep["render_wave_cap"] >= 1 << 22
+        assert rep["render_extend"] in (0, 1, 2) and rep["render_shade_block"] in (128, 256)
+        assert gpu_ctx.get_option("render_shade_block") == rep["render_shade_block"]
         assert 0 < rep["best_ms"] <= rep["worst_ms"] and rep["default_ms"] > 0
         assert gpu_ctx.get_option("render_wave_cap") == rep["render_wave_cap"]
         assert gpu_ctx.get_option("render_extend") == rep["render_extend"]
@@ -61,13 +62,14 @@ def test_autotune_render_keeps_images(gpu_ctx):
     finally:
         gpu_ctx.set_option("render_wave_cap", 1 << 26)
         gpu_ctx.set_option("render_extend", 1)
+        gpu_ctx.set_option("render_shade_block", 256)
 
 
 @pytest.mark.parametrize("which", ["showcase", "batch_tris"])
 def test_extend_variants_same_images(gpu_ctx, which):
     """The three closest-hit variants of the wave engine (register budget, ray in
-    registers or shared memory) compute the same hits: images and ray counts are
-    bit-identical. Sphere scene and triangle-only scene."""
+    registers or shared memory) and the two block shapes of its shading kernel
+    give bit-identical images and ray counts. Sphere scene and triangle-only scene."""
     if which == "showcase":
         spec, cam = scenes.showcase_scene()
         st = bcgx.quality("Draft")
@@ -83,14 +85,19 @@ def test_extend_variants_same_images(gpu_ctx, which):
             gpu_ctx.set_option("render_extend", var)
             assert gpu_ctx.get_option("render_extend") == var
             out[var] = gpu_ctx.render_batch(views)
+        gpu_ctx.set_option("render_shade_block", 128)
+        out["sb128"] = gpu_ctx.render_batch(views)
     finally:
         gpu_ctx.set_option("render_extend", 1)
-    for var in (0, 2):
+        gpu_ctx.set_option("render_shade_block", 256)
+    for var in (0, 2, "sb128"):
         imgs, rays = out[var]
         assert rays == out[1][1]
         assert all(np.array_equal(a, b) for a, b in zip(imgs, out[1][0]))
     with pytest.raises(bcgx.BCError, match="INVALID_ARG"):
         gpu_ctx.set_option("render_extend", 3)
+    with pytest.raises(bcgx.BCError, match="INVALID_ARG"):
+        gpu_ctx.set_option("render_shade_block", 64)
 
 
 def test_autotune_argument_errors(gpu_ctx):

@@ -438,6 +438,37 @@ __device__ __forceinline__ void walk(const SceneView& sv, const Ray32& r, Leaf& 
   }
 }
 
+// A node's hit children, nearest first: the nearest becomes the next node and
+// the others are pushed far-first (entry distance kept for culling at the
+// pop); no hit child: the next node is popped. When no active lane of the warp
+// hit more than one child, the sorting network and the pushes have nothing to
+// do: the single hit child (if any) is picked with selects. Either way each
+// lane visits the same nodes in the same order.
+template <int STACK, class W>
+__device__ __forceinline__ uint32_t order_children(float nr[8], uint32_t ch[8], uint2* st, int& sp, float tlim,
+                                                   unsigned* status, W& walker) {
+  const float kInf = __int_as_float(0x7f800000);
+  int hits = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) hits += nr[k] != kInf ? 1 : 0;
+  if (!__any_sync(__activemask(), hits > 1)) {
+    uint32_t c = kEnd;
+#pragma unroll
+    for (int k = 0; k < 8; k++) c = nr[k] != kInf ? ch[k] : c;
+    return hits ? c : walker.pop(tlim);
+  }
+  sort8(nr, ch);
+  if (nr[0] == kInf) return walker.pop(tlim);
+#pragma unroll
+  for (int k = 7; k >= 1; k--) {
+    if (nr[k] != kInf) {
+      if (sp < STACK) st[sp++] = make_uint2(ch[k], __float_as_uint(nr[k]));
+      else atomicOr(status, kStatusStackOverflow);
+    }
+  }
+  return ch[0];
+}
+
 // The same while-while walk as a resumable per-lane state machine, for
 // persistent kernels that refill a lane with a new ray as soon as its ray is
 // done. step() runs one outer iteration and returns true once the walk of the
@@ -468,19 +499,7 @@ struct Walker {
       float nr[8];
       uint32_t ch[8];
       node_children_fused<true>(sv.nodes + ref, rp, r.tmin, leaf.tlim, nr, ch);
-      sort8(nr, ch);
-      if (nr[0] == __int_as_float(0x7f800000)) {
-        ref = pop(leaf.tlim);
-      } else {
-#pragma unroll
-        for (int k = 7; k >= 1; k--) {
-          if (nr[k] != __int_as_float(0x7f800000)) {
-            if (sp < STACK) st[sp++] = make_uint2(ch[k], __float_as_uint(nr[k]));
-            else atomicOr(status, kStatusStackOverflow);
-          }
-        }
-        ref = ch[0];
-      }
+      ref = order_children<STACK>(nr, ch, st, sp, leaf.tlim, status, *this);
       if (ref != kEnd && (ref & kLeafBit)) {
         if (pending != 0) break;
         pending = ref;
@@ -531,19 +550,7 @@ struct FastWalker {
       float nr[8];
       uint32_t ch[8];
       node_children_fused<false>(sv.nodes + ref, rp, r.tmin, leaf.tlim, nr, ch);
-      sort8(nr, ch);
-      if (nr[0] == __int_as_float(0x7f800000)) {
-        ref = pop(leaf.tlim);
-      } else {
-#pragma unroll
-        for (int k = 7; k >= 1; k--) {
-          if (nr[k] != __int_as_float(0x7f800000)) {
-            if (sp < STACK) st[sp++] = make_uint2(ch[k], __float_as_uint(nr[k]));
-            else atomicOr(status, kStatusStackOverflow);
-          }
-        }
-        ref = ch[0];
-      }
+      ref = order_children<STACK>(nr, ch, st, sp, leaf.tlim, status, *this);
       if (ref != kEnd && (ref & kLeafBit)) {
         if (pending != 0) break;
         pending = ref;

@@ -442,8 +442,9 @@ __device__ __forceinline__ void walk(const SceneView& sv, const Ray32& r, Leaf& 
 // the others are pushed far-first (entry distance kept for culling at the
 // pop); no hit child: the next node is popped. When no active lane of the warp
 // hit more than one child, the sorting network and the pushes have nothing to
-// do: the single hit child (if any) is picked with selects. Either way each
-// lane visits the same nodes in the same order.
+// do: the single hit child (if any) is picked with selects; when none hit more
+// than two, the two are ordered with one comparison (equal distances keep slot
+// order) instead of the network.
 template <int STACK, class W>
 __device__ __forceinline__ uint32_t order_children(float nr[8], uint32_t ch[8], uint2* st, int& sp, float tlim,
                                                    unsigned* status, W& walker) {
@@ -451,11 +452,33 @@ __device__ __forceinline__ uint32_t order_children(float nr[8], uint32_t ch[8], 
   int hits = 0;
 #pragma unroll
   for (int k = 0; k < 8; k++) hits += nr[k] != kInf ? 1 : 0;
-  if (!__any_sync(__activemask(), hits > 1)) {
+  const unsigned am = __activemask();
+  if (!__any_sync(am, hits > 1)) {
     uint32_t c = kEnd;
 #pragma unroll
     for (int k = 0; k < 8; k++) c = nr[k] != kInf ? ch[k] : c;
     return hits ? c : walker.pop(tlim);
+  }
+  if (!__any_sync(am, hits > 2)) {  // at most two: the nearer is next, the other pushed
+    float n0 = kInf, n1 = kInf;
+    uint32_t c0 = kEnd, c1 = kEnd;
+#pragma unroll
+    for (int k = 7; k >= 0; k--) {  // c0: the lowest hit slot, c1: the next one
+      if (nr[k] != kInf) {
+        n1 = n0;
+        c1 = c0;
+        n0 = nr[k];
+        c0 = ch[k];
+      }
+    }
+    if (hits == 0) return walker.pop(tlim);
+    if (hits == 1) return c0;
+    const bool swap = n1 < n0;
+    const float nf = swap ? n0 : n1;
+    const uint32_t cf = swap ? c0 : c1;
+    if (sp < STACK) st[sp++] = make_uint2(cf, __float_as_uint(nf));
+    else atomicOr(status, kStatusStackOverflow);
+    return swap ? c1 : c0;
   }
   sort8(nr, ch);
   if (nr[0] == kInf) return walker.pop(tlim);

@@ -443,7 +443,7 @@ __device__ __forceinline__ void walk(const SceneView& sv, const Ray32& r, Leaf& 
 // pop); no hit child: the next node is popped. When no active lane of the warp
 // hit more than one child, the sorting network and the pushes have nothing to
 // do: the single hit child (if any) is picked with selects; when none hit more
-// than three, they are ordered with three comparisons instead of the network.
+// than four, they are ordered with five comparisons instead of the network.
 template <int STACK, class W>
 __device__ __forceinline__ uint32_t order_children(float nr[8], uint32_t ch[8], uint2* st, int& sp, float tlim,
                                                    unsigned* status, W& walker) {
@@ -458,12 +458,14 @@ __device__ __forceinline__ uint32_t order_children(float nr[8], uint32_t ch[8], 
     for (int k = 0; k < 8; k++) c = nr[k] != kInf ? ch[k] : c;
     return hits ? c : walker.pop(tlim);
   }
-  if (!__any_sync(am, hits > 3)) {  // at most three: ordered with three comparisons
-    float n0 = kInf, n1 = kInf, n2 = kInf;
-    uint32_t c0 = kEnd, c1 = kEnd, c2 = kEnd;
+  if (!__any_sync(am, hits > 4)) {  // at most four: ordered with five comparisons
+    float n0 = kInf, n1 = kInf, n2 = kInf, n3 = kInf;
+    uint32_t c0 = kEnd, c1 = kEnd, c2 = kEnd, c3 = kEnd;
 #pragma unroll
-    for (int k = 7; k >= 0; k--) {  // c0, c1, c2: the hit slots in slot order
+    for (int k = 7; k >= 0; k--) {  // c0..c3: the hit slots in slot order
       if (nr[k] != kInf) {
+        n3 = n2;
+        c3 = c2;
         n2 = n1;
         c2 = c1;
         n1 = n0;
@@ -474,12 +476,14 @@ __device__ __forceinline__ uint32_t order_children(float nr[8], uint32_t ch[8], 
     }
     if (hits == 0) return walker.pop(tlim);
     cswap(n0, c0, n1, c1);
+    cswap(n2, c2, n3, c3);
+    cswap(n0, c0, n2, c2);
+    cswap(n1, c1, n3, c3);
     cswap(n1, c1, n2, c2);
-    cswap(n0, c0, n1, c1);
 #pragma unroll
-    for (int k = 2; k >= 1; k--) {
-      const float nk = k == 2 ? n2 : n1;
-      const uint32_t ck = k == 2 ? c2 : c1;
+    for (int k = 3; k >= 1; k--) {
+      const float nk = k == 3 ? n3 : (k == 2 ? n2 : n1);
+      const uint32_t ck = k == 3 ? c3 : (k == 2 ? c2 : c1);
       if (nk != kInf) {
         if (sp < STACK) st[sp++] = make_uint2(ck, __float_as_uint(nk));
         else atomicOr(status, kStatusStackOverflow);

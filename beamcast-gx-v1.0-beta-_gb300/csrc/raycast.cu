@@ -200,9 +200,9 @@ __global__ void __launch_bounds__(128, MINB) k_closest_exact_persistent(SceneVie
 // The one-kernel form above keeps the fp64 settlement (and the in-walk fp64
 // re-test of a full contender list) in the walking kernel, whose register
 // allocation then covers the fp64 code: 80 registers with spills at six
-// 128-thread blocks per SM. Split, the walk holds no fp64 code and fits 48
-// registers with a 6-byte spill (ten blocks per SM; 9.74 -> 8.31 ms on the
-// 1M-triangle / 4M-ray cast, settlement included):
+// 128-thread blocks per SM. Split, the walk holds no fp64 code and fits 40
+// registers without spills (twelve blocks per SM; 9.74 ms -> 7.71 ms on the
+// 1M-triangle / 4M-ray cast, settlement and ray order included):
 //   pass 1, k_exact_walk: the persistent walk with the fp32 classifier; a
 //     finished ray leaves a record (best certain hit: slot and upper bound of
 //     its distance; the pending contenders: slot and lower bound). A ray with
@@ -317,7 +317,7 @@ struct FilterLeaf {
 };
 
 template <int STACK>
-__global__ void __launch_bounds__(128, 10) k_exact_walk(SceneView sv, const float4* __restrict__ rays, int64_t n,
+__global__ void __launch_bounds__(128, 12) k_exact_walk(SceneView sv, const float4* __restrict__ rays, int64_t n,
                                                        ExactRecords rec, unsigned* status, unsigned long long* work,
                                                        const int32_t* __restrict__ perm) {
   const unsigned lane = threadIdx.x & 31u;
@@ -500,7 +500,7 @@ struct FilterAnyLeaf {
 };
 
 template <int STACK>
-__global__ void __launch_bounds__(128, 10) k_any_walk(SceneView sv, const float4* __restrict__ rays, int64_t n,
+__global__ void __launch_bounds__(128, 12) k_any_walk(SceneView sv, const float4* __restrict__ rays, int64_t n,
                                                       uint8_t* __restrict__ out, AnyRecords rec, unsigned* status,
                                                       unsigned long long* work) {
   const unsigned lane = threadIdx.x & 31u;

@@ -406,7 +406,7 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  * path picks a work-group size once, gpu_opencl_windows.go:285-304):
  *   "raycast_split"      1 (default): the exact closest hit of a triangle-only
  *                        scene runs as passes: a walk with fp32 classification only
- *                        (ten 128-thread blocks per SM), an fp64 settlement pass,
+ *                        (twelve 128-thread blocks per SM), an fp64 settlement pass,
  *                        and a re-trace of the rays whose contender list overflowed;
  *                        it holds 52 bytes of device scratch per ray of a call (per
  *                        chunk for bc_raycast). The exact any hit likewise: a walk,

@@ -76,7 +76,7 @@ int bc_gpu_available(char* reason, size_t reason_len) {
       msg = std::string("CUDA GPU: ") + p.name;
     } else {
       msg = std::string("device 0 (") + p.name + ") is sm_" + std::to_string(p.major) + std::to_string(p.minor) +
-            "; this build targets sm_103a";
+            "; the library is compiled for sm_103a";
     }
   }
   if (reason && reason_len) {

@@ -1,6 +1,6 @@
 """Benchmark of the GB300 hot path (one JSON line on rank 0).
 
-Workload (the ray-cast configuration of the measurement plan): 1,000,000
+Workload (the ray-cast configuration): 1,000,000
 seeded random triangles (centroids U[0,1]^3, edge lengths LogNormal(-5, 0.5)),
 32-bin SAH BVH collapsed to BVH8, 4,194,304 seeded rays (origins U[0,1]^3,
 directions uniform on the sphere), exact closest hit. A step is one ray cast

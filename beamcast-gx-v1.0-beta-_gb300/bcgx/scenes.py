@@ -31,7 +31,8 @@ import numpy as np
 from .scene import MAT_DIFFUSE, MAT_EMISSIVE, MAT_GLASS, MAT_METAL, Material, Scene
 from .settings import Camera, RenderSettings, quality
 
-SEED_C1, SEED_C2, SEED_C3, SEED_C4, SEED_C5 = 0xBEAC0001, 0xBEAC0002, 0xBEAC0003, 0xBEAC0004, 0xBEAC0005
+SEED_CORNELL, SEED_TRIS, SEED_ULTRA, SEED_BATCH, SEED_DIFF = 0xBEAC0001, 0xBEAC0002, 0xBEAC0003, 0xBEAC0004, 0xBEAC0005
+SEED_RAYS = 0xBEAC0003  # the ray-cast workload's rays
 
 
 @dataclass
@@ -103,7 +104,7 @@ def box_tris(center, half):
 
 # ---------------------------------------------------------------------------
 # Workload 1: Cornell-style box, CPU-runnable.
-def cornell_box(seed: int = SEED_C1) -> tuple[SceneSpec, Camera, RenderSettings]:
+def cornell_box(seed: int = SEED_CORNELL) -> tuple[SceneSpec, Camera, RenderSettings]:
     rng = np.random.default_rng(seed)
     sp = SceneSpec(name="cornell-box-c1", bvh_mode="SAH", bvh_bins=32, bvh_leaf=4)
 
@@ -155,7 +156,7 @@ def _unit_vectors(rng, n):
     return v / l[:, None]
 
 
-def random_triangle_verts(n: int, seed: int = SEED_C2, lo=0.0, hi=1.0) -> np.ndarray:
+def random_triangle_verts(n: int, seed: int = SEED_TRIS, lo=0.0, hi=1.0) -> np.ndarray:
     """(n, 9) fp64 triangles; regenerates those AddTriangle would drop (|E1 x E2|^2 < 1e-18)."""
     rng = np.random.default_rng(seed)
     out = np.empty((n, 9), dtype=np.float64)
@@ -180,14 +181,14 @@ def random_triangle_verts(n: int, seed: int = SEED_C2, lo=0.0, hi=1.0) -> np.nda
     return out
 
 
-def random_triangles(n: int = 1_000_000, seed: int = SEED_C2) -> SceneSpec:
+def random_triangles(n: int = 1_000_000, seed: int = SEED_TRIS) -> SceneSpec:
     sp = SceneSpec(name=f"random-tris-{n}", bvh_mode="SAH", bvh_bins=32, bvh_leaf=4)
     m = sp.material(Material(MAT_DIFFUSE, (0.7, 0.7, 0.7)))
     sp.triangles(random_triangle_verts(n, seed), m)
     return sp
 
 
-def random_rays(n: int = 4_194_304, seed: int = SEED_C2 + 1, tmin: float = 1e-4, tmax: float = 1e30) -> np.ndarray:
+def random_rays(n: int = 4_194_304, seed: int = SEED_RAYS, tmin: float = 1e-4, tmax: float = 1e30) -> np.ndarray:
     """(n, 8) float32 ray records (ox, oy, oz, tmin, dx, dy, dz, tmax)."""
     rng = np.random.default_rng(seed)
     r = np.empty((n, 8), dtype=np.float32)
@@ -293,7 +294,7 @@ def _value_noise(p: np.ndarray, seed: int) -> np.ndarray:
     return out
 
 
-def icosphere_grid(seed: int = SEED_C3, n: int = 64, freq: int = 5, spacing: float = 1.0, radius: float = 0.4,
+def icosphere_grid(seed: int = SEED_ULTRA, n: int = 64, freq: int = 5, spacing: float = 1.0, radius: float = 0.4,
                    amplitude: float = 0.05, n_lights: int = 64) -> tuple[SceneSpec, Camera, RenderSettings]:
     """n x n displaced icospheres (20 freq^2 triangles each), a ground quad and n_lights
     emissive quads with LogNormal(1, 1) luminance; spheres are 50% diffuse
@@ -349,7 +350,7 @@ def batch_scene(n_tris: int, seed: int) -> SceneSpec:
     return sp
 
 
-def batch_views(seed: int = SEED_C4, n_views: int = 64, sizes=(10_000, 50_000, 200_000, 500_000),
+def batch_views(seed: int = SEED_BATCH, n_views: int = 64, sizes=(10_000, 50_000, 200_000, 500_000),
                 max_side: tuple[int, int] = (1920, 1080), spp_range: tuple[int, int] = (4, 64), bounces: int = 8):
     """Scenes and views of the batching workload: view v renders scene v mod len(sizes)
     at W = round(128 * r_w^t), H = round(128 * r_h^t), t ~ U[0, 1] (log-uniform from
@@ -391,7 +392,7 @@ class DiffProblem:
     init_params: np.ndarray         # (n_slots + n_lights, 3) float32
 
 
-def diff_scene(seed: int = SEED_C5, n_tris: int = 200_000, n_slots: int = 256, n_lights: int = 8,
+def diff_scene(seed: int = SEED_DIFF, n_tris: int = 200_000, n_slots: int = 256, n_lights: int = 8,
                width: int = 512, height: int = 512, spp: int = 64, bounces: int = 8) -> DiffProblem:
     """Random triangles in the unit cube, each on one of n_slots diffuse
     materials, lit by n_lights emissive quads above the cube and the sky."""

@@ -111,8 +111,8 @@ class ClockSampler:
 
 def _make_workload():
     from bcgx import scenes
-    spec = scenes.random_triangles(N_TRIS, seed=scenes.SEED_C2)
-    rays = scenes.random_rays(N_RAYS, seed=scenes.SEED_C3)
+    spec = scenes.random_triangles(N_TRIS, seed=scenes.SEED_TRIS)
+    rays = scenes.random_rays(N_RAYS, seed=scenes.SEED_RAYS)
     return spec, rays
 
 
@@ -121,7 +121,7 @@ def rank_rays(rank: int, n: int | None = None):
     seeds on the other ranks (weak scaling: every rank casts its own rays over
     the replicated scene, with no collective on the data path)."""
     from bcgx import scenes
-    return scenes.random_rays(N_RAYS if n is None else n, seed=scenes.SEED_C3 + rank)
+    return scenes.random_rays(N_RAYS if n is None else n, seed=scenes.SEED_RAYS + rank)
 
 
 def max_over_ranks(dist, values, device):
@@ -298,7 +298,7 @@ def run_gpu(args):
     avg_ms = total_ms / args.steps
     achieved = bytes_per_ray * N_RAYS / (avg_ms / 1e3) / 1e9
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "raycast_c2_traffic.json")
+    tf = os.path.join(ROOT, "profiles", "k_exact_walk__raycast_1M_tris_4M_rays_traffic.json")
     if os.path.exists(tf):
         with open(tf) as f:
             traffic = json.load(f).get("dram_bytes_per_launch")

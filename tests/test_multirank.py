@@ -54,7 +54,7 @@ def test_two_ranks_gloo():
     # max over ranks, on every rank
     assert out[0][0] == out[1][0] == [2.5, 7.0]
     # rank 0 casts the single-GPU workload's rays; rank 1 its own
-    assert np.array_equal(out[0][1], scenes.random_rays(2048, seed=scenes.SEED_C3))
+    assert np.array_equal(out[0][1], scenes.random_rays(2048, seed=scenes.SEED_RAYS))
     assert not np.array_equal(out[0][1], out[1][1])
     assert out[1][1].shape == (2048, 8)
 

@@ -40,7 +40,7 @@ def _check(ctx, orc_scene, rays, max_ulp=0, allow_ties=False):
 
 
 def test_random_triangles_parity(gpu_ctx, orc):
-    spec = scenes.random_triangles(100_000, seed=scenes.SEED_C2)
+    spec = scenes.random_triangles(100_000, seed=scenes.SEED_TRIS)
     s = scenes.to_scene(spec)
     gpu_ctx.upload(s)
     ref = orc.OracleScene.from_spec(spec)
@@ -167,10 +167,10 @@ def test_empty_and_errors(gpu_ctx, native_lib):
     assert st["slots"] == len(a.prim_kind) and st["stack_need"] <= 256
 
 
-def test_full_size_c2_properties_and_sample(gpu_ctx, orc):
+def test_full_size_raycast_properties_and_sample(gpu_ctx, orc):
     """Workload 2 at full size: 1M triangles, 4M rays. Exact parity on a seeded
     sample of 131072 rays; size-independent properties on all rays."""
-    spec = scenes.random_triangles(1_000_000, seed=scenes.SEED_C2)
+    spec = scenes.random_triangles(1_000_000, seed=scenes.SEED_TRIS)
     s = scenes.to_scene(spec)
     gpu_ctx.upload(s)
     rays = scenes.random_rays(4_194_304)
@@ -219,7 +219,7 @@ def test_split_passes_parity(gpu_ctx, orc, which):
     the same hits and distances as the one-kernel exact form (raycast_split 0),
     and both match the oracle; the same for the any hit."""
     if which == "random":
-        spec = scenes.random_triangles(100_000, seed=scenes.SEED_C2 + 7)
+        spec = scenes.random_triangles(100_000, seed=scenes.SEED_TRIS + 7)
         rays = scenes.random_rays(262_144, seed=15)
     elif which == "stacked":
         spec = _stacked_triangles()

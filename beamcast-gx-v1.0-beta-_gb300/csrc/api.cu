@@ -408,13 +408,18 @@ bc_status bc_occluded_device(bc_context* ctx, const float* d_rays, int64_t n, ui
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   void* rec = nullptr;
+  void* order = nullptr;
   if (ctx->raycast_split && n > 0) {
     cudaError_t e = ctx->d_rec_any.ensure(any_record_bytes(n));
     if (e) return cuda_status(ctx, e, "any-hit record buffers");
     rec = ctx->d_rec_any.p;
+    if (ctx->raycast_sort && n >= kMinOrderedRays && n < (int64_t(1) << 31)) {
+      if ((e = ctx->d_order[2].ensure(ray_order_bytes(n)))) return cuda_status(ctx, e, "ray order buffers");
+      order = ctx->d_order[2].p;
+    }
   }
   cudaError_t e = launch_raycast_any(ctx->ds, (const float4*)d_rays, n, d_out, ctx->d_status, ctx->raycast_variant,
-                                     ctx->d_work + 3, rec, st);
+                                     ctx->d_work + 3, rec, order, st);
   return cuda_status(ctx, e, "any-hit launch");
 }
 
@@ -428,14 +433,19 @@ bc_status bc_occluded(bc_context* ctx, const float* rays, int64_t n, uint8_t* ou
   if ((e = ctx->d_rays.ensure((size_t)n * 32)) || (e = ctx->d_occ.ensure((size_t)n)))
     return cuda_status(ctx, e, "any-hit buffers");
   void* rec = nullptr;
+  void* order = nullptr;
   if (ctx->raycast_split) {
     if ((e = ctx->d_rec_any.ensure(any_record_bytes(n)))) return cuda_status(ctx, e, "any-hit record buffers");
     rec = ctx->d_rec_any.p;
+    if (ctx->raycast_sort && n >= kMinOrderedRays && n < (int64_t(1) << 31)) {
+      if ((e = ctx->d_order[2].ensure(ray_order_bytes(n)))) return cuda_status(ctx, e, "ray order buffers");
+      order = ctx->d_order[2].p;
+    }
   }
   e = cudaMemcpyAsync(ctx->d_rays.p, rays, (size_t)n * 32, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess)
     e = launch_raycast_any(ctx->ds, ctx->d_rays.as<float4>(), n, ctx->d_occ.as<uint8_t>(), ctx->d_status, ctx->raycast_variant,
-                           ctx->d_work + 3, rec, ctx->stream);
+                           ctx->d_work + 3, rec, order, ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, ctx->d_occ.p, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_status(ctx, e, "any hit");

@@ -38,9 +38,11 @@ cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int
                                    int32_t* prim_out, unsigned* status, unsigned long long* work, int variant,
                                    void* order_scratch, void* rec_scratch, cudaStream_t st);
 // Exact any hit. rec_scratch (any_record_bytes(n) bytes) and `work` (as for the
-// closest hit), or NULL: a triangle-only scene runs as walk and fp64 passes.
+// closest hit), or NULL: a triangle-only scene runs as walk and fp64 passes,
+// in the coherent ray order when order_scratch (ray_order_bytes(n)) is given.
 size_t any_record_bytes(int64_t n);
 cudaError_t launch_raycast_any(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
-                               int variant, unsigned long long* work, void* rec_scratch, cudaStream_t st);
+                               int variant, unsigned long long* work, void* rec_scratch, void* order_scratch,
+                               cudaStream_t st);
 
 }  // namespace bcgx

@@ -502,7 +502,8 @@ struct FilterAnyLeaf {
 template <int STACK>
 __global__ void __launch_bounds__(128, 12) k_any_walk(SceneView sv, const float4* __restrict__ rays, int64_t n,
                                                       uint8_t* __restrict__ out, AnyRecords rec, unsigned* status,
-                                                      unsigned long long* work) {
+                                                      unsigned long long* work,
+                                                      const int32_t* __restrict__ perm) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned below = (1u << lane) - 1u;
   long long idx = -1;
@@ -522,7 +523,7 @@ __global__ void __launch_bounds__(128, 12) k_any_walk(SceneView sv, const float4
       if (need) {
         const unsigned long long my = base + (unsigned long long)__popc(m & below);
         if (my < (unsigned long long)n) {
-          idx = (long long)my;
+          idx = perm ? (long long)perm[my] : (long long)my;
           const float4 a = __ldg(rays + 2 * idx), b = __ldg(rays + 2 * idx + 1);
           r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
           leaf.reset(b.w);
@@ -754,7 +755,7 @@ cudaError_t closest_split(const DeviceScene& s, const float4* rays, int64_t n, f
 
 template <int STACK>
 cudaError_t any_split(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
-                      unsigned long long* work, void* rec_scratch, cudaStream_t st) {
+                      unsigned long long* work, void* rec_scratch, const int32_t* perm, cudaStream_t st) {
   static int blocks = 0;
   if (!blocks) blocks = persistent_blocks(k_any_walk<STACK>);
   int dev = 0, sms = 0;
@@ -765,7 +766,7 @@ cudaError_t any_split(const DeviceScene& s, const float4* rays, int64_t n, uint8
   if (!e) e = cudaMemsetAsync(rec.count, 0, sizeof(unsigned long long), st);
   if (e) return e;
   const int64_t grid = (n + 127) / 128;
-  k_any_walk<STACK><<<(int)std::min<int64_t>(blocks, grid), 128, 0, st>>>(view_of(s), rays, n, out, rec, status, work);
+  k_any_walk<STACK><<<(int)std::min<int64_t>(blocks, grid), 128, 0, st>>>(view_of(s), rays, n, out, rec, status, work, perm);
   k_any_settle<STACK><<<std::max(sms, 1) * 4, 128, 0, st>>>(view_of(s), rays, n, out, rec, status);
   return cudaGetLastError();
 }
@@ -810,8 +811,9 @@ cudaError_t closest_var(const DeviceScene& s, const float4* rays, int64_t n, flo
 
 template <int STACK>
 cudaError_t any_var(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status, int variant,
-                    unsigned long long* work, void* rec_scratch, cudaStream_t st) {
-  if (rec_scratch && work && !s.has_spheres) return any_split<STACK>(s, rays, n, out, status, work, rec_scratch, st);
+                    unsigned long long* work, void* rec_scratch, const int32_t* perm, cudaStream_t st) {
+  if (rec_scratch && work && !s.has_spheres)
+    return any_split<STACK>(s, rays, n, out, status, work, rec_scratch, perm, st);
   switch (variant) {
     case 6: return any_stack<STACK, 6>(s, rays, n, out, status, st);
     case 8: return any_stack<STACK, 8>(s, rays, n, out, status, st);
@@ -833,31 +835,41 @@ size_t ray_order_bytes(int64_t n) {
   return (size_t)kKeyBins * 4 + (size_t)(kKeyBins / kScanBlock) * 4 + (size_t)n * 8 + 4 * 256;
 }
 
+// Spatially coherent ray order (see k_ray_keys) into order_scratch; *perm is
+// left NULL when the batch is not ordered (no scratch, fewer than
+// kMinOrderedRays rays, 2^31 rays or more: the order holds 32-bit indices, or a
+// scene with spheres, whose kernels read rays in order).
+static cudaError_t order_rays(const DeviceScene& s, const float4* rays, int64_t n, void* order_scratch,
+                              const int32_t** perm, cudaStream_t st) {
+  *perm = nullptr;
+  if (!order_scratch || n < kMinOrderedRays || n >= (int64_t(1) << 31) || s.has_spheres) return cudaSuccess;
+  char* q = (char*)order_scratch;
+  int32_t* bins = (int32_t*)q;
+  int32_t* totals = (int32_t*)(q + (size_t)kKeyBins * 4);
+  uint32_t* keys = (uint32_t*)(q + (size_t)kKeyBins * 4 + ((kKeyBins / kScanBlock) * 4 + 255) / 256 * 256);
+  int32_t* pm = (int32_t*)((char*)keys + ((size_t)n * 4 + 255) / 256 * 256);
+  cudaError_t e = cudaMemsetAsync(bins, 0, (size_t)kKeyBins * 4, st);
+  if (e) return e;
+  const float3 lo = make_float3(s.lo[0], s.lo[1], s.lo[2]);
+  auto sc = [](float a, float b) { return b > a ? 64.0f / (b - a) : 0.0f; };
+  const float3 scale = make_float3(sc(s.lo[0], s.hi[0]), sc(s.lo[1], s.hi[1]), sc(s.lo[2], s.hi[2]));
+  const unsigned g = (unsigned)((n + 255) / 256);
+  k_ray_keys<<<g, 256, 0, st>>>(rays, n, lo, scale, keys, bins);
+  k_scan_bins<<<kKeyBins / kScanBlock, kScanBlock, 0, st>>>(bins, totals);
+  k_scan_totals<<<1, kScanBlock, 0, st>>>(totals);
+  k_ray_scatter<<<g, 256, 0, st>>>(n, keys, bins, totals, pm);
+  if ((e = cudaGetLastError())) return e;
+  *perm = pm;
+  return cudaSuccess;
+}
+
 cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int64_t n, float* t_out,
                                    int32_t* prim_out, unsigned* status, unsigned long long* work, int variant,
                                    void* order_scratch, void* rec_scratch, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   const int32_t* perm = nullptr;
-  // the order is a permutation of 32-bit ray indices: batches up to 2^31 - 1 rays
-  if (order_scratch && n >= kMinOrderedRays && n < (int64_t(1) << 31) && !s.has_spheres) {
-    char* q = (char*)order_scratch;
-    int32_t* bins = (int32_t*)q;
-    int32_t* totals = (int32_t*)(q + (size_t)kKeyBins * 4);
-    uint32_t* keys = (uint32_t*)(q + (size_t)kKeyBins * 4 + ((kKeyBins / kScanBlock) * 4 + 255) / 256 * 256);
-    int32_t* pm = (int32_t*)((char*)keys + ((size_t)n * 4 + 255) / 256 * 256);
-    cudaError_t e = cudaMemsetAsync(bins, 0, (size_t)kKeyBins * 4, st);
-    if (e) return e;
-    const float3 lo = make_float3(s.lo[0], s.lo[1], s.lo[2]);
-    auto sc = [](float a, float b) { return b > a ? 64.0f / (b - a) : 0.0f; };
-    const float3 scale = make_float3(sc(s.lo[0], s.hi[0]), sc(s.lo[1], s.hi[1]), sc(s.lo[2], s.hi[2]));
-    const unsigned g = (unsigned)((n + 255) / 256);
-    k_ray_keys<<<g, 256, 0, st>>>(rays, n, lo, scale, keys, bins);
-    k_scan_bins<<<kKeyBins / kScanBlock, kScanBlock, 0, st>>>(bins, totals);
-    k_scan_totals<<<1, kScanBlock, 0, st>>>(totals);
-    k_ray_scatter<<<g, 256, 0, st>>>(n, keys, bins, totals, pm);
-    if ((e = cudaGetLastError())) return e;
-    perm = pm;
-  }
+  cudaError_t e = order_rays(s, rays, n, order_scratch, &perm, st);
+  if (e) return e;
   switch (stack_variant(s.stack_need)) {
     case 64: return closest_var<64>(s, rays, n, t_out, prim_out, status, work, variant, perm, rec_scratch, st);
     case 128: return closest_var<128>(s, rays, n, t_out, prim_out, status, work, variant, perm, rec_scratch, st);
@@ -867,12 +879,18 @@ cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int
 }
 
 cudaError_t launch_raycast_any(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,
-                               int variant, unsigned long long* work, void* rec_scratch, cudaStream_t st) {
+                               int variant, unsigned long long* work, void* rec_scratch, void* order_scratch,
+                               cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  const int32_t* perm = nullptr;
+  if (rec_scratch) {  // only the split walk reads rays through the order
+    cudaError_t e = order_rays(s, rays, n, order_scratch, &perm, st);
+    if (e) return e;
+  }
   switch (stack_variant(s.stack_need)) {
-    case 64: return any_var<64>(s, rays, n, out, status, variant, work, rec_scratch, st);
-    case 128: return any_var<128>(s, rays, n, out, status, variant, work, rec_scratch, st);
-    case 256: return any_var<256>(s, rays, n, out, status, variant, work, rec_scratch, st);
+    case 64: return any_var<64>(s, rays, n, out, status, variant, work, rec_scratch, perm, st);
+    case 128: return any_var<128>(s, rays, n, out, status, variant, work, rec_scratch, perm, st);
+    case 256: return any_var<256>(s, rays, n, out, status, variant, work, rec_scratch, perm, st);
     default: return cudaErrorInvalidValue;
   }
 }

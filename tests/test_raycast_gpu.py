@@ -249,3 +249,12 @@ def test_split_passes_parity(gpu_ctx, orc, which):
     occ_ref, _ = ref.occluded_f32(rays)
     assert np.array_equal(occ2, occ1) and np.array_equal(occ2, occ_ref)
     assert np.array_equal(occ2, two[1] >= 0)
+    # the split passes without the coherent ray order give the same answers
+    try:
+        gpu_ctx.set_option("raycast_sort", 0)
+        three = gpu_ctx.raycast(rays)
+        occ3 = gpu_ctx.occluded(rays)
+    finally:
+        gpu_ctx.set_option("raycast_sort", 1)
+    assert np.array_equal(three[1], two[1]) and np.array_equal(three[0], two[0])
+    assert np.array_equal(occ3, occ2)

@@ -66,6 +66,13 @@ class TuneReportC(C.Structure):
                 ("worst_ms", C.c_double), ("raycast_split", C.c_int32), ("render_shade_block", C.c_int32)]
 
 
+class TimingC(C.Structure):
+    _fields_ = [("device_ms", C.c_double), ("launches", C.c_int64), ("extend_launches", C.c_int64),
+                ("kernel_timing", C.c_int32), ("reserved", C.c_int32), ("generate_ms", C.c_double),
+                ("extend_ms", C.c_double), ("shade_ms", C.c_double), ("connect_ms", C.c_double),
+                ("accumulate_ms", C.c_double), ("post_ms", C.c_double), ("other_ms", C.c_double)]
+
+
 class PostDescC(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("render_width", C.c_int32),
                 ("render_height", C.c_int32), ("hbao", C.c_int32), ("hbao_plus", C.c_int32),
@@ -91,6 +98,7 @@ SIGNATURES = [
     ("bc_raycast_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("bc_occluded", C.c_int, [C.c_void_p, f32p, C.c_int64, u8p]),
     ("bc_occluded_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    ("bc_sync", C.c_int, [C.c_void_p, C.c_void_p]),
     ("bc_render_rows", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), C.c_int32, C.c_int32, f32p, u32p, i64p]),
     ("bc_render_frame", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, u32p, u32p, i64p]),
     ("bc_render_moments", C.c_int, [C.c_void_p, P(CameraC), P(SettingsC), f32p, f32p, i64p]),
@@ -109,6 +117,7 @@ SIGNATURES = [
                                           C.c_void_p, C.c_void_p]),
     ("bc_set_option", C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     ("bc_get_option", C.c_int, [C.c_void_p, C.c_char_p, i64p]),
+    ("bc_last_timing", C.c_int, [C.c_void_p, C.POINTER(TimingC)]),
     ("bc_cancel", C.c_int, [C.c_void_p]),
     ("bc_reset_cancel", C.c_int, [C.c_void_p]),
     ("bc_hscene_create", C.c_void_p, []),

@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import DiffDescC, PostDescC, SceneDesc, TuneReportC, ViewC, check, lib, ptr
+from ._lib import DiffDescC, PostDescC, SceneDesc, TimingC, TuneReportC, ViewC, check, lib, ptr
 from .scene import Scene, SceneArrays
 from .settings import Camera, RenderSettings
 
@@ -118,6 +118,18 @@ class Context:
     def occluded_device(self, d_rays: int, n: int, d_out: int, stream: int = 0):
         check(lib().bc_occluded_device(self._h, C.c_void_p(d_rays), int(n), C.c_void_p(d_out),
                                        C.c_void_p(stream) if stream else None), self._h)
+
+    def last_timing(self) -> dict:
+        """Device time of the last render call (bc_last_timing): CUDA events on
+        the context's stream; per-kernel classes when render_timing is 1."""
+        t = TimingC()
+        check(lib().bc_last_timing(self._h, C.byref(t)), self._h)
+        return {name: getattr(t, name) for name, _ in TimingC._fields_ if name != "reserved"}
+
+    def sync(self, stream: int = 0):
+        """Waits for `stream` and raises the kernel status of the device-pointer
+        calls enqueued since the last sync (bc_sync)."""
+        check(lib().bc_sync(self._h, C.c_void_p(stream) if stream else None), self._h)
 
     # -- rendering --
     def render_rows(self, cam: Camera, settings: RenderSettings, y0: int, rows: int, guides: bool = False):

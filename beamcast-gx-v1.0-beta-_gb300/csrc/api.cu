@@ -25,21 +25,35 @@ bc_status cuda_status(bc_context* ctx, cudaError_t e, const char* what) {
   return set_error(ctx, e == cudaErrorMemoryAllocation ? BC_ERR_OOM : BC_ERR_DEVICE, m);
 }
 
-// Reads and clears the kernel status word after the stream has drained.
-bc_status check_kernel_status(bc_context* ctx) {
+// Reads and clears a kernel status word once `stream` has drained.
+bc_status check_status_word(bc_context* ctx, unsigned* d_word, cudaStream_t stream) {
   unsigned h = 0;
-  cudaError_t e = cudaMemcpyAsync(&h, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaError_t e = cudaMemcpyAsync(&h, d_word, sizeof(unsigned), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return cuda_status(ctx, e, "reading kernel status");
   if (h == 0) return BC_OK;
-  cudaMemsetAsync(ctx->d_status, 0, sizeof(unsigned), ctx->stream);
-  cudaStreamSynchronize(ctx->stream);
+  cudaMemsetAsync(d_word, 0, sizeof(unsigned), stream);
+  cudaStreamSynchronize(stream);
   if (h & kStatusStackOverflow)
     return set_error(ctx, BC_ERR_CAPACITY, "traversal stack overflow (scene deeper than the compiled stack)");
   if (h & kStatusTimeout) return set_error(ctx, BC_ERR_TIMEOUT, "a bounded device wait gave up");
   if (h & kStatusCapacity) return set_error(ctx, BC_ERR_CAPACITY, "a device queue exceeded its capacity");
   if (h & kStatusBound) return set_error(ctx, BC_ERR_DEVICE, "fp32 error bound violated by an fp64 re-test");
   return set_error(ctx, BC_ERR_DEVICE, "unknown kernel status");
+}
+
+// Status of the host-buffer calls and renders (their own word, on the context's stream).
+bc_status check_kernel_status(bc_context* ctx) { return check_status_word(ctx, ctx->d_status, ctx->stream); }
+
+// Test hook of the device-pointer calls: ORs bits into their status word on
+// their stream, as a kernel that hit a stack or queue limit would.
+static __global__ void k_raise_status(unsigned* word, unsigned bits) { atomicOr(word, bits); }
+
+static cudaError_t raise_test_status(bc_context* ctx, cudaStream_t st) {
+  if (!ctx->test_status_bits) return cudaSuccess;
+  k_raise_status<<<1, 1, 0, st>>>(ctx->d_status_async, ctx->test_status_bits);
+  ctx->test_status_bits = 0;
+  return cudaGetLastError();
 }
 
 static bc_status upload(bc_context* ctx, DevBuf& b, const void* src, size_t bytes, const char* what) {
@@ -105,8 +119,9 @@ bc_status bc_create(int device_ordinal, bc_context** out) {
   ctx->name = p.name;
   e = cudaSetDevice(device_ordinal);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_status, sizeof(unsigned));
-  if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_status, 2 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, 2 * sizeof(unsigned));
+  if (e == cudaSuccess) ctx->d_status_async = ctx->d_status + 1;
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_work, 64);
   if (e == cudaSuccess) {
     e = cudaMemset(ctx->d_work, 0, 64);
@@ -331,6 +346,7 @@ bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, flo
     return set_error(ctx, BC_ERR_INVALID_ARG, "bad ray-cast arguments");
   if (((uintptr_t)d_rays & 15u) != 0) return set_error(ctx, BC_ERR_INVALID_ARG, "rays must be 16-byte aligned");
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
+  cudaSetDevice(ctx->device);
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   void* order = nullptr;
   if (ctx->raycast_sort && n >= kMinOrderedRays && n < (int64_t(1) << 31)) {
@@ -344,8 +360,9 @@ bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, flo
     if (e) return cuda_status(ctx, e, "ray-cast record buffers");
     rec = ctx->d_rec[2].p;
   }
-  cudaError_t e = launch_raycast_closest(ctx->ds, (const float4*)d_rays, n, d_t_out, d_prim_out, ctx->d_status,
-                                         ctx->d_work + 2, ctx->raycast_variant, order, rec, st);
+  cudaError_t e = launch_raycast_closest(ctx->ds, (const float4*)d_rays, n, d_t_out, d_prim_out,
+                                         ctx->d_status_async, ctx->d_work + 2, ctx->raycast_variant, order, rec, st);
+  if (e == cudaSuccess) e = raise_test_status(ctx, st);
   return cuda_status(ctx, e, "ray-cast launch");
 }
 
@@ -406,6 +423,7 @@ bc_status bc_occluded_device(bc_context* ctx, const float* d_rays, int64_t n, ui
   if (n < 0 || (n > 0 && (!d_rays || !d_out))) return set_error(ctx, BC_ERR_INVALID_ARG, "bad any-hit arguments");
   if (((uintptr_t)d_rays & 15u) != 0) return set_error(ctx, BC_ERR_INVALID_ARG, "rays must be 16-byte aligned");
   if (!ctx->has_scene) return set_error(ctx, BC_ERR_NO_SCENE, "no scene uploaded");
+  cudaSetDevice(ctx->device);
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   void* rec = nullptr;
   void* order = nullptr;
@@ -418,9 +436,16 @@ bc_status bc_occluded_device(bc_context* ctx, const float* d_rays, int64_t n, ui
       order = ctx->d_order[2].p;
     }
   }
-  cudaError_t e = launch_raycast_any(ctx->ds, (const float4*)d_rays, n, d_out, ctx->d_status, ctx->raycast_variant,
-                                     ctx->d_work + 3, rec, order, st);
+  cudaError_t e = launch_raycast_any(ctx->ds, (const float4*)d_rays, n, d_out, ctx->d_status_async,
+                                     ctx->raycast_variant, ctx->d_work + 3, rec, order, st);
+  if (e == cudaSuccess) e = raise_test_status(ctx, st);
   return cuda_status(ctx, e, "any-hit launch");
+}
+
+bc_status bc_sync(bc_context* ctx, void* stream) {
+  if (!ctx) return set_error(nullptr, BC_ERR_INVALID_ARG, "NULL context");
+  cudaSetDevice(ctx->device);
+  return check_status_word(ctx, ctx->d_status_async, stream ? (cudaStream_t)stream : ctx->stream);
 }
 
 bc_status bc_occluded(bc_context* ctx, const float* rays, int64_t n, uint8_t* out) {
@@ -483,6 +508,11 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     ctx->photon_grid = (int)value;
     return BC_OK;
   }
+  if (n == "test_status_bits") {  // test hook: the next device-pointer call raises these status bits
+    if (value < 0 || value > 0xffffffffLL) return set_error(ctx, BC_ERR_INVALID_ARG, "test_status_bits is 32 bits");
+    ctx->test_status_bits = (unsigned)value;
+    return BC_OK;
+  }
   if (n == "raycast_chunk") {
     if (value < 65536 || value > (1LL << 28))
       return set_error(ctx, BC_ERR_INVALID_ARG, "raycast_chunk must be in [65536, 2^28]");
@@ -515,6 +545,11 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     ctx->render_shade_block = (int)value;
     return BC_OK;
   }
+  if (n == "render_timing") {
+    if (value != 0 && value != 1) return set_error(ctx, BC_ERR_INVALID_ARG, "render_timing must be 0 or 1");
+    ctx->render_timing = (int)value;
+    return BC_OK;
+  }
   return set_error(ctx, BC_ERR_INVALID_ARG, "unknown option " + n);
 }
 
@@ -532,7 +567,14 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
   if (n == "render_engine") { *value = ctx->render_engine; return BC_OK; }
   if (n == "render_extend") { *value = ctx->render_extend; return BC_OK; }
   if (n == "render_shade_block") { *value = ctx->render_shade_block; return BC_OK; }
+  if (n == "render_timing") { *value = ctx->render_timing; return BC_OK; }
   return BC_ERR_INVALID_ARG;
+}
+
+bc_status bc_last_timing(const bc_context* ctx, bc_timing* out) {
+  if (!ctx || !out) return BC_ERR_INVALID_ARG;
+  *out = ctx->last_timing;
+  return BC_OK;
 }
 
 bc_status bc_cancel(bc_context* ctx) {

@@ -96,6 +96,10 @@ struct bc_context {
   // ray-cast staging
   bcgx::DevBuf d_rays, d_t, d_prim, d_occ;
   unsigned* d_status = nullptr;
+  // status word of the device-pointer calls (bc_raycast_device, bc_occluded_device),
+  // read and cleared only by bc_sync, so their kernel status reaches their caller
+  unsigned* d_status_async = nullptr;
+  unsigned test_status_bits = 0;  // bc_set_option "test_status_bits": raised by the next device-pointer call
   // work counters of the persistent ray-cast kernels: [0], [1] the two streams of
   // bc_raycast, [2] bc_raycast_device
   unsigned long long* d_work = nullptr;
@@ -104,6 +108,8 @@ struct bc_context {
   int render_engine = 0;                // 0: wave engine, 1: one kernel per view (bc_set_option "render_engine")
   int render_extend = 1;                // k_extend variant 0..2 (bc_set_option "render_extend")
   int render_shade_block = 256;         // k_shade block size, 128 or 256 (bc_set_option "render_shade_block")
+  int render_timing = 0;                // per-kernel events in renders (bc_set_option "render_timing")
+  bc_timing last_timing{};              // bc_last_timing
   struct DiffState* diff = nullptr;  // differentiable rendering (diff.cu)
   struct PhotonCache* photons = nullptr;  // photon maps of the photon-mapping integrator (photon.cu)
   int photon_grid = 1;                    // gathers read the dense cell table (bc_set_option "photon_grid")
@@ -119,6 +125,7 @@ namespace bcgx {
 bc_status set_error(bc_context* ctx, bc_status st, const std::string& msg);
 bc_status cuda_status(bc_context* ctx, cudaError_t e, const char* what);
 bc_status check_kernel_status(bc_context* ctx);
+bc_status check_status_word(bc_context* ctx, unsigned* d_word, cudaStream_t stream);
 void destroy_render_buffers(bc_context* ctx);
 void destroy_diff_state(bc_context* ctx);
 void destroy_post_state(bc_context* ctx);

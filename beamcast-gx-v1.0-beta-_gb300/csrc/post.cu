@@ -244,6 +244,9 @@ float* g_scratch_ptr[kMaxDevices] = {};
 
 // Device address of g_post_scratch for the current device, looked up once per
 // device with that device current (the host-side symbol is not a device address).
+// The cached address belongs to the device's current primary context: after a
+// cudaDeviceReset the module may load elsewhere, so a process that resets a
+// device must not call bc_post_process_noalloc on it again.
 cudaError_t scratch_for_current_device(float** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -269,8 +272,21 @@ extern "C" bc_status bc_post_process_noalloc(int32_t width, int32_t height, cons
   if ((int64_t)width * height > kNoAllocMaxPixels)
     return set_error(nullptr, BC_ERR_INVALID_ARG,
                      "frame exceeds the static scratch of bc_post_process_noalloc (921600 pixels)");
-  if (d_linear_in == d_linear_out)
-    return set_error(nullptr, BC_ERR_INVALID_ARG, "input and output images must not alias");
+  // The passes read their inputs through __restrict__ pointers and ping-pong
+  // through the output: no written image may share a byte with any other image.
+  const size_t n_px = (size_t)width * height;
+  const auto lo = [](const void* p) { return reinterpret_cast<uintptr_t>(p); };
+  const auto overlap = [&](const void* a, size_t abytes, const void* b, size_t bbytes) {
+    return a && b && lo(a) < lo(b) + bbytes && lo(b) < lo(a) + abytes;
+  };
+  const size_t img_bytes = 3 * sizeof(float) * n_px, guide_bytes = 4 * sizeof(float) * n_px;
+  const size_t rgba_bytes = sizeof(uint32_t) * n_px;
+  if (overlap(d_linear_out, img_bytes, d_linear_in, img_bytes) ||
+      overlap(d_linear_out, img_bytes, d_guide_nd, guide_bytes) ||
+      overlap(d_linear_out, img_bytes, d_rgba_out, rgba_bytes) ||
+      overlap(d_rgba_out, rgba_bytes, d_linear_in, img_bytes) ||
+      overlap(d_rgba_out, rgba_bytes, d_guide_nd, guide_bytes))
+    return set_error(nullptr, BC_ERR_INVALID_ARG, "the output buffers must not overlap each other or the inputs");
   if (settings->denoise && !d_guide_nd) return set_error(nullptr, BC_ERR_INVALID_ARG, "denoise needs guides");
   float* scratch = nullptr;
   cudaError_t e = scratch_for_current_device(&scratch);
@@ -285,10 +301,13 @@ extern "C" bc_status bc_post_process_noalloc(int32_t width, int32_t height, cons
   float* sb = scratch + 3 * (size_t)kNoAllocMaxPixels;  // horizontal bloom blur
   const bool bloom = settings->bloom > 0;
   const float* img = d_linear_in;
-  if (settings->denoise) {
+  // A pass count of zero or less (taa and txaa both -2 or below) denoises
+  // nothing: atrousDenoise returns its input unchanged (renderer.go:2229), as
+  // bc_post_process does.
+  const int passes = 2 + std::min(3, std::max(settings->taa, settings->txaa));
+  if (settings->denoise && passes > 0) {
     // a-trous passes ping-pong between the output and scratch A so that the
     // last pass lands in A when bloom follows, else in the output
-    const int passes = 2 + std::min(3, std::max(settings->taa, settings->txaa));
     float* last = bloom ? sa : d_linear_out;
     float* other = bloom ? d_linear_out : sa;
     const float* cur = d_linear_in;

@@ -1127,6 +1127,10 @@ T* carve(char*& p, size_t n) {
   return r;
 }
 
+// Kernel classes of the per-launch device timing (bc_last_timing); kTimeEnd
+// marks the end of the last timed launch.
+enum { kTimeEnd = -1, kTimeGenerate = 0, kTimeExtend, kTimeShade, kTimeConnect, kTimeAccumulate, kTimePost, kTimeOther };
+
 }  // namespace bcgx
 
 struct RenderBuffers {
@@ -1165,6 +1169,29 @@ struct RenderBuffers {
   cudaGraphExec_t graph = nullptr;
   std::vector<uintptr_t> graph_key;
   std::vector<uintptr_t> single_key;  // last single-wave render launched without a graph
+  // Device time of the last render call: CUDA events on the context's stream
+  // around its device work; with render_timing on, one event before every
+  // launch (and one after the last), each interval charged to its launch's class.
+  cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+  std::vector<cudaEvent_t> kev;
+  std::vector<int> kcls;
+  size_t kused = 0;
+  bool ktiming = false;
+  int64_t launches = 0, extend_launches = 0;
+  // marks the start of a launch of class `cls` (kTimeEnd: the end of the last one)
+  void mark(cudaStream_t st, int cls) {
+    if (!ktiming) return;
+    if (kused == kev.size()) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreate(&e) != cudaSuccess) {
+        ktiming = false;  // timing is best effort; the render itself goes on
+        return;
+      }
+      kev.push_back(e);
+    }
+    cudaEventRecord(kev[kused++], st);
+    kcls.push_back(cls);
+  }
 };
 
 namespace bcgx {
@@ -1173,6 +1200,9 @@ void destroy_render_buffers(bc_context* ctx) {
   if (!ctx->rb) return;
   RenderBuffers* rb = ctx->rb;
   if (rb->graph) cudaGraphExecDestroy(rb->graph);
+  if (rb->ev_begin) cudaEventDestroy(rb->ev_begin);
+  if (rb->ev_end) cudaEventDestroy(rb->ev_end);
+  for (cudaEvent_t e : rb->kev) cudaEventDestroy(e);
   rb->paths.release();
   rb->shadow.release();
   rb->queues.release();
@@ -1185,6 +1215,56 @@ void destroy_render_buffers(bc_context* ctx) {
   rb->rrec.release();
   delete rb;
   ctx->rb = nullptr;
+}
+
+// Device timing of a render call (bc_last_timing): events on the context's
+// stream before the call's first and after its last device work.
+static void timing_begin(bc_context* ctx) {
+  RenderBuffers* rb = ctx->rb;
+  if (!rb->ev_begin) cudaEventCreate(&rb->ev_begin);
+  if (!rb->ev_end) cudaEventCreate(&rb->ev_end);
+  rb->ktiming = ctx->render_timing != 0;
+  rb->kused = 0;
+  rb->kcls.clear();
+  rb->launches = rb->extend_launches = 0;
+  if (rb->ev_begin) cudaEventRecord(rb->ev_begin, ctx->stream);
+  rb->mark(ctx->stream, kTimeOther);
+}
+
+static void timing_end(bc_context* ctx) {
+  RenderBuffers* rb = ctx->rb;
+  rb->mark(ctx->stream, kTimeEnd);
+  if (rb->ev_end) cudaEventRecord(rb->ev_end, ctx->stream);
+}
+
+// After the stream has drained: elapsed times into ctx->last_timing.
+static void timing_collect(bc_context* ctx) {
+  RenderBuffers* rb = ctx->rb;
+  bc_timing t;
+  std::memset(&t, 0, sizeof(t));
+  float ms = 0.0f;
+  if (rb->ev_begin && rb->ev_end && cudaEventElapsedTime(&ms, rb->ev_begin, rb->ev_end) == cudaSuccess)
+    t.device_ms = ms;
+  t.launches = rb->launches;
+  t.extend_launches = rb->extend_launches;
+  if (rb->ktiming) {
+    double cls_ms[kTimeOther + 1] = {0, 0, 0, 0, 0, 0, 0};
+    for (size_t i = 0; i + 1 < rb->kused; i++) {
+      const int c = rb->kcls[i];
+      if (c < 0) continue;
+      if (cudaEventElapsedTime(&ms, rb->kev[i], rb->kev[i + 1]) == cudaSuccess) cls_ms[c] += ms;
+    }
+    t.kernel_timing = 1;
+    t.generate_ms = cls_ms[kTimeGenerate];
+    t.extend_ms = cls_ms[kTimeExtend];
+    t.shade_ms = cls_ms[kTimeShade];
+    t.connect_ms = cls_ms[kTimeConnect];
+    t.accumulate_ms = cls_ms[kTimeAccumulate];
+    t.post_ms = cls_ms[kTimePost];
+    t.other_ms = cls_ms[kTimeOther];
+  }
+  cudaGetLastError();  // timing is best effort: a failed event query is not the render's error
+  ctx->last_timing = t;
 }
 
 // Path slots, queues and a shadow queue of sh_cap entries (one per path and
@@ -1398,6 +1478,7 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
   RenderBuffers* rb = ctx->rb;
   WaveCounters* c = rb->cnt;
   const RecurRec rr = w.recursive ? rb->rr : RecurRec{nullptr, nullptr, nullptr, nullptr, 0};
+  rb->mark(st, kTimeGenerate);
   k_generate<<<w.gen_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->q[0], rb->seq_xy, rb->guide_jit, c,
                                          rb->adapt);
   int cur = 0;
@@ -1405,6 +1486,7 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
   // counter, extend zeroes the queue and shadow list its shade fills, shade
   // zeroes the work counters of the next extend and of its connect.
   for (int b = 0; b < w.bounces; b++) {
+    rb->mark(st, kTimeExtend);
     if (w.ext == 0)
       k_extend<STACK, SPH><<<w.ext_grid, 128, 0, st>>>(sc.sv, rb->views, rb->ps, rb->q[cur], c, cur, ctx->d_status);
     else if (w.ext == 2)
@@ -1412,6 +1494,7 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
     else
       k_extend_10<STACK, SPH><<<w.ext_grid, 128, 0, st>>>(sc.sv, rb->views, rb->ps, rb->q[cur], c, cur, ctx->d_status);
     const GradRec rec = w.grad ? rb->grec : GradRec{nullptr, nullptr, nullptr, 0};
+    rb->mark(st, kTimeShade);
 #define BC_SHADE_LAUNCH(KERNEL, BLOCK)                                                                         \
   KERNEL<<<w.shade_grid, BLOCK, 0, st>>>(rb->views, ctx->ds.n_mats, sc, rb->ps, rb->q[cur], rb->q[cur ^ 1], rb->sh, \
                                         c, cur, b, rb->guide_nd, rb->guide_c, rb->guide_jit, rec, rr, rb->sh_cap,   \
@@ -1424,15 +1507,19 @@ static cudaError_t enqueue_wave(bc_context* ctx, const WaveShape& w, const Shade
       else BC_SHADE_LAUNCH(k_shade<false>, 256);
     }
 #undef BC_SHADE_LAUNCH
+    if (w.lights) rb->mark(st, kTimeConnect);
     if (w.lights)
       k_connect<STACK, SPH><<<w.con_grid, 128, 0, st>>>(sc.sv, rb->ps, rb->sh, c, rr, rb->sh_cap, ctx->d_status);
     cur ^= 1;
   }
+  if (w.grad) rb->mark(st, kTimeOther);
   if (w.grad)
     k_gradient<<<gradient_grid(), 256, 3 * w.grad->n_params * sizeof(double), st>>>(rb->bs, rb->views, rb->ps,
                                                                                   rb->grec, *w.grad, sc.mats);
+  rb->mark(st, kTimeAccumulate);
   k_accumulate<<<w.acc_grid, 256, 0, st>>>(rb->bs, rb->views, rb->ps, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr,
                                            rb->adapt, rr);
+  rb->mark(st, kTimeOther);
   k_advance<<<1, 32, 0, st>>>(rb->bs, c);
   return cudaGetLastError();
 }
@@ -1451,7 +1538,9 @@ static bc_status run_waves(bc_context* ctx, int bounces, bool lights, const Shad
   // A wave graph pays for its capture when a render has several waves, or when
   // a single-wave render repeats with the same launches (a frame loop at fixed
   // settings): such a render is captured the second time its key is seen.
-  bool use_graph = ctx->render_graph != 0;
+  bool use_graph = ctx->render_graph != 0 && !rb->ktiming;  // per-launch events need direct launches
+  rb->launches += n_waves * (3 + (int64_t)bounces * (2 + (lights ? 1 : 0)) + (grad ? 1 : 0));
+  rb->extend_launches += n_waves * (int64_t)bounces;
   if (use_graph) {
     // every value the captured launches were given
     std::vector<uintptr_t> key = {(uintptr_t)STACK, (uintptr_t)SPH, (uintptr_t)w.ext, (uintptr_t)w.ext_grid,
@@ -1540,6 +1629,8 @@ static bc_status run_plain(bc_context* ctx, const ShadeScene& sc, const std::vec
       return set_error(ctx, BC_ERR_CANCELLED, "render cancelled");
     }
     const int grid = (views[v].npix + 127) / 128;
+    rb->mark(ctx->stream, kTimeOther);
+    rb->launches++;
     if (alt)
       k_render_plain<STACK, SPH, true><<<grid, 128, 0, ctx->stream>>>(
           rb->views, v, ctx->ds.n_mats, sc, rb->seq_xy, rb->sum, rb->want_sumsq ? rb->sumsq : nullptr, rb->guide_nd,
@@ -1695,6 +1786,7 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
     hq[2 * i] = X[i];
     hq[2 * i + 1] = Y[i];
   }
+  timing_begin(ctx);
   e = cudaMemcpyAsync(rb->table.p, hs, tbytes, cudaMemcpyHostToDevice, ctx->stream);
   if (!e && !X.empty())
     e = cudaMemcpyAsync(rb->seq.p, hq, X.size() * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream);
@@ -1707,6 +1799,7 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
     if (!e && rb->want_sumsq)
       e = cudaMemsetAsync(rb->sumsq + 3 * (size_t)V.pix_off, 0, 3 * sizeof(float) * (size_t)V.npix, ctx->stream);
     if (!e && V.want_guides) {  // invalid guides: depth -1, compact words 0
+      rb->launches++;
       k_clear_guides<<<(V.npix + 255) / 256, 256, 0, ctx->stream>>>(V.npix, rb->guide_nd + V.pix_off,
                                                                     rb->guide_c + 3 * (size_t)V.pix_off);
       e = cudaGetLastError();
@@ -1740,9 +1833,12 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
     bst = sph ? run_waves<256, true>(ctx, max_bounces, lights, sc, n_waves, bsh.cap, grad, rec_bounces > 0, alt)
               : run_waves<256, false>(ctx, max_bounces, lights, sc, n_waves, bsh.cap, grad, rec_bounces > 0, alt);
   if (bst) return bst;
+  rb->mark(ctx->stream, kTimeOther);
   k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sum, rb->out, rb->adapt.n);
   if (rb->want_sumsq)
     k_finish_views<<<sm_count() * 8, 256, 0, ctx->stream>>>(rb->views, n, rb->sumsq, rb->post_tmp, rb->adapt.n);
+  rb->launches += rb->want_sumsq ? 2 : 1;
+  timing_end(ctx);
   e = cudaGetLastError();
   unsigned long long r = 0;
   std::vector<unsigned long long> pr(photon_rays.size(), 0);
@@ -1753,6 +1849,7 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
   if (e) return cuda_status(ctx, e, "render");
   for (unsigned long long v : pr) r += v;  // Start counts the photon map's rays (renderer.go:2809)
   if (rays) *rays = (int64_t)r;
+  timing_collect(ctx);
   return check_kernel_status(ctx);
 }
 
@@ -1855,7 +1952,12 @@ bc_status bc_render_frame(bc_context* ctx, const bc_camera* cam, const bc_settin
   if (st) return st;
   RenderBuffers* rb = ctx->rb;
   const int npix = settings->width * settings->height;
+  rb->mark(ctx->stream, kTimePost);
   if ((st = run_post(ctx, *settings))) return st;
+  // the frame's device time runs to the end of the post stack
+  rb->launches += (settings->denoise ? std::max(0, 2 + std::min(3, std::max(settings->taa, settings->txaa))) : 0) +
+                  (settings->bloom > 0 ? 2 : 0) + 1;
+  timing_end(ctx);
   cudaError_t e = cudaSuccess;
   if (linear_out)
     e = cudaMemcpyAsync(linear_out, rb->out, 3 * sizeof(float) * (size_t)npix, cudaMemcpyDeviceToHost, ctx->stream);
@@ -1866,6 +1968,7 @@ bc_status bc_render_frame(bc_context* ctx, const bc_camera* cam, const bc_settin
     e = cudaMemcpyAsync(rgba_out, rb->rgba, sizeof(uint32_t) * (size_t)npix, cudaMemcpyDeviceToHost, ctx->stream);
   if (!e) e = cudaStreamSynchronize(ctx->stream);
   if (e) return cuda_status(ctx, e, "frame readback");
+  timing_collect(ctx);
   if (rays_out) *rays_out = rays;
   return BC_OK;
 }

@@ -1,28 +1,55 @@
 """Benchmark of the GB300 hot path (one JSON line on rank 0).
 
-Workload (the ray-cast configuration): 1,000,000
-seeded random triangles (centroids U[0,1]^3, edge lengths LogNormal(-5, 0.5)),
-32-bin SAH BVH collapsed to BVH8, 4,194,304 seeded rays (origins U[0,1]^3,
-directions uniform on the sphere), exact closest hit. A step is one ray cast
-of all 4M rays; a path segment is one closest-hit query (the unit the
-reference counts as Rays, renderer.go:1491).
+Default workload, the configuration the metric is quoted on: the
+Ultra-Realism-shaped frame. 2,048,130 seeded triangles (64x64 displaced
+geodesic icospheres, a ground quad, 64 emissive quads with LogNormal(1, 1)
+luminance; spheres 50% diffuse, 50% rough metal with roughness U[0.05, 1]),
+32-bin SAH BVH collapsed to BVH8, 2560x1440, 256 spp, 16 bounces, Russian
+roulette from bounce 6, Halton, MIS, power-weighted lights, no clamp, denoise
+(3 a-trous passes), bloom 1, ACES; the adaptive stop is off (equal spp, as the
+reference's own benchmark recipe sets it, benchmark.go:82). A step is one frame
+through bc_render_frame (render and post stack) with the scene resident in
+HBM and the output left on the device. A path segment is one extension ray,
+the unit the reference counts as Rays (renderer.go:1491).
 
-  value  : Mpath-segments/s over all ranks, rays resident in HBM, device time
-           from CUDA events on the launching stream; L2 flushed between steps.
-  e2e    : the same through the host-buffer C-ABI call bc_raycast (host->device
-           copy of the rays, the kernel, device->host copy of t and prim).
-  roofline: algorithmic bytes per ray from the oracle's binary-BVH traversal
-           counters on the CPU-baseline sample, 32*boxes + 40*tris + 24 + 8,
-           times the rays of one launch, over the average kernel time.
+  value   : Mpath-segments/s of the wave engine: extension rays / device time
+            of the frame (CUDA events the library records on its launching
+            stream before the frame's first and after its last device work,
+            read with bc_last_timing). The path state (64 Mi paths x 104 B)
+            and the scene (~300 MB) exceed L2, so no flush is needed.
+  plain   : the same frames (same seeds, same samples, so equal RMSE) by the
+            one-kernel form: one launch per view, a thread per pixel looping
+            over samples and bounces, the reference OpenCL kernel's shape;
+            wave_over_plain = value / plain.
+  e2e     : bc_render_frame with the linear HDR image and RGBA8 read back into
+            pinned host buffers, wall clock around the call.
+  roofline: the closest-hit kernel k_extend (the dominant kernel): algorithmic
+            bytes per extension query from the oracle's binary-BVH traversal
+            counters on the CPU-baseline sample (32 B per box test, 40 per
+            triangle test, 32 per sphere, 24 ray in + 8 hit out) times the
+            queries of one frame, over k_extend's device time in that frame
+            (events before every launch: option render_timing 1).
+  rmse    : linear radiance on a 128x72 window at the frame centre against a
+            16,384-spp image of that window rendered by the GPU wave engine
+            (whose per-pixel means the oracle parity tests check): the wave
+            engine, the one-kernel form and the oracle at 256 spp.
+  cpu_baseline: the oracle (fp64 restatement of the reference integrator) on
+            the machine's host cores, the full frame at 16 spp.
+  configs : the other configurations measured in the same run: ray cast
+            (Mrays/s), Cornell box, 64-view batch, adjoint s/iter.
 
-Multi-GPU: every rank casts its own 4M rays (weak scaling, no collective on
-the data path); rank 0 reports max-over-ranks time.
-`--impl reference` times the CPU restatement of the reference renderer
-(the oracle port) on the host cores instead, with the same metric.
+Multi-GPU: replicas only (pixels, samples and views are independent): every
+rank renders its own frames (its own seeds), value = all ranks' segments over
+the slowest rank's time. `--impl reference` times the CPU restatement of the
+reference renderer (the oracle port) on the host cores instead.
+`--workload raycast|cornell|batch|diff|refit|build|integrators|calibration`
+prints the line of one other configuration.
 """
 from __future__ import annotations
 
 import argparse
+import copy
+import ctypes as C
 import json
 import os
 import statistics
@@ -38,8 +65,16 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 N_TRIS = 1_000_000
 N_RAYS = 4_194_304
 METRIC = "Mpath-segments/s"
+RAY_METRIC = "Mrays/s"
 WORKLOAD = "raycast: 1M random tris (32-bin SAH -> BVH8), 4M random rays, exact closest hit"
 DATA = "synthetic, seeded (tris seed 0xBEAC0002, rays seed 0xBEAC0003)"
+ULTRA_WORKLOAD = ("ultra-realism shape: 2,048,130 tris (64x64 displaced icospheres + ground + 64 emissive quads), "
+                  "2560x1440, 256 spp, 16 bounces, RR from bounce 6, Halton, MIS, power lights, denoise x3, "
+                  "bloom 1, ACES; adaptive stop off (equal spp)")
+ULTRA_DATA = "synthetic, seeded (scene seed 0xBEAC0003)"
+CPU_SPP_ULTRA = 16   # oracle sample of the frame for cpu_baseline (about 10 s on 16 cores)
+REF_SPP_ULTRA = 2    # oracle sample per step of the reference arm
+CONVERGED_SPP = 16384
 
 
 def _dist_env():
@@ -136,7 +171,7 @@ def max_over_ranks(dist, values, device):
 
 def cpu_baseline(spec, rays, seconds_target=15.0, threads=0):
     """The oracle (fp64 restatement of Scene.Hit) on a bounded sample of rays.
-    Returns (Mpath-segments/s, cores, sample description, algorithmic bytes per ray)."""
+    Returns (Mrays/s, cores, sample description, algorithmic bytes per ray)."""
     import numpy as np
     import oracle
     ref = oracle.OracleScene.from_spec(spec)
@@ -159,7 +194,7 @@ def cpu_baseline(spec, rays, seconds_target=15.0, threads=0):
         {"box_tests_per_ray": boxes / m, "tri_tests_per_ray": tris / m}
 
 
-def run_reference(args):
+def run_reference_raycast(args):
     ws, rank, _ = _dist_env()
     if rank != 0:
         return 0
@@ -182,18 +217,31 @@ def run_reference(args):
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = per_step * args.steps / total / 1e6
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+    line = {"impl": "reference", "metric": RAY_METRIC, "value": value, "unit": RAY_METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
             "config": {"workload": WORKLOAD, "rays_per_step": per_step, "triangles": N_TRIS},
-            "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": RAY_METRIC, "cores": cores, "kind": "port",
                              "sample": f"{per_step} seeded rays of the 4M-ray set per step"},
-            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": RAY_METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
 def run_gpu(args):
+    line = measure_raycast(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def measure_raycast(args, cpu_seconds=15.0):
+    """The ray-cast configuration: 1M seeded random triangles (32-bin SAH ->
+    BVH8), 4,194,304 seeded rays, exact closest hit. A step is one
+    bc_raycast_device over all rays resident in HBM (ray ordering, the walk
+    pass, the fp64 settlement pass, the re-trace pass); value = Mrays/s from
+    CUDA events on the launching stream, L2 flushed between steps. Returns the
+    JSON line on rank 0, None on the other ranks."""
     import numpy as np
     import torch
     import bcgx
@@ -286,7 +334,7 @@ def run_gpu(args):
         ctx.close()
         if dist:
             dist.destroy_process_group()
-        return 0
+        return None
 
     value = ws * N_RAYS * args.steps / (total_ms / 1e3) / 1e6
     e2e_value = ws * N_RAYS / e2e_s / 1e6
@@ -294,7 +342,7 @@ def run_gpu(args):
     if args.no_cpu_baseline:
         cpu_v, cores, sample, bytes_per_ray, counters = None, 0, "skipped", float("nan"), {}
     else:
-        cpu_v, cores, sample, bytes_per_ray, counters = cpu_baseline(spec, rays)
+        cpu_v, cores, sample, bytes_per_ray, counters = cpu_baseline(spec, rays, seconds_target=cpu_seconds)
     avg_ms = total_ms / args.steps
     achieved = bytes_per_ray * N_RAYS / (avg_ms / 1e3) / 1e9
     traffic = None
@@ -303,19 +351,19 @@ def run_gpu(args):
         with open(tf) as f:
             traffic = json.load(f).get("dram_bytes_per_launch")
     line = {
-        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "metric": RAY_METRIC, "value": value, "unit": RAY_METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": avg_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 traversal + f64 re-test", "data": DATA,
         "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays_per_gpu": N_RAYS,
                    "l2": "flushed between steps (256 MiB write)", "bvh8_nodes": stats["nodes8"],
                    "bvh8_depth": stats["depth8"], "scene_bytes": stats["device_bytes"]},
         "autotune": tune,
-        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": N_RAYS * 32,
+        "e2e": {"value": e2e_value, "unit": RAY_METRIC, "h2d_bytes_per_step": N_RAYS * 32,
                 "d2h_bytes_per_step": N_RAYS * 8},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_ray": bytes_per_ray, **counters},
-        "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": cpu_v, "unit": RAY_METRIC, "cores": cores, "kind": "port", "sample": sample},
         # per step: the trace kernel (split form: walk, settle, re-trace), plus the
         # four ray-order kernels (keys, two scans, scatter)
         "gpu_launches": args.steps * ((3 if split else 1) +
@@ -328,11 +376,10 @@ def run_gpu(args):
         "clocks": clk,
         "kernel_ms": [round(x, 4) for x in kernel_ms],
     }
-    print(json.dumps(line), flush=True)
     ctx.close()
     if dist:
         dist.destroy_process_group()
-    return 0
+    return line
 
 
 def _render_roofline(stats, mseg_per_s):
@@ -410,13 +457,13 @@ def rmse_vs_converged(scene, spec, cam, st, window, conv_spp=CONVERGED_SPP, thre
             "cpu": rmse(cpu_eq, cpu_conv),
             f"gpu_{parts * conv.spp}spp_vs_converged": rmse(gpu_conv, cpu_conv)}
 
-def run_render(args):
-    """Render workloads (one JSON line each): `cornell` = the Cornell-box
-    configuration (320x240, 16 spp, 5 bounces, RR from 3, Halton, MIS, power
-    lights); `ultra` = the Ultra-Realism-shaped frame (2560x1440, 256 spp,
-    16 bounces, RR from 6, 2,048,130 triangles, denoise 3 passes, bloom, ACES).
-    value = extension rays (path segments) / device-resident frame time (no
-    readback); e2e = the same frame with the linear image and RGBA8 read back."""
+def measure_render(args):
+    """The Cornell-box configuration (320x240, 16 spp, 5 bounces, RR from 3,
+    Halton, MIS, power lights; `args.workload == "cornell"`), or the Ultra-shaped
+    frame with wall-clock timing (`"ultra-wall"`). value = extension rays (path
+    segments) / wall time of the synchronous frame call without readback (the
+    device is idle before and after); e2e = the same frame with the linear
+    image and RGBA8 read back. Returns the JSON line."""
     import numpy as np
     import bcgx
     from bcgx import scenes
@@ -494,7 +541,7 @@ def run_render(args):
         import oracle
         ref = oracle.OracleScene.from_spec(spec)
         cst = st.copy()
-        if args.workload == "ultra":  # bounded sample: the full frame at 4 spp
+        if args.workload != "cornell":  # bounded sample: the full frame at 4 spp
             cst.spp = 4
         else:  # the Cornell frame is tiny: several frames' worth of samples
             cst.spp = 512
@@ -511,12 +558,349 @@ def run_render(args):
         else:  # a crop of spheres, ground and emitters around the frame centre
             window = (st.width // 2 - 64, st.height // 2 - 36, 128, 72)
         line["rmse"] = rmse_vs_converged(scene, spec, cam, st, window)
-    print(json.dumps(line), flush=True)
     ctx.close()
+    return line
+
+
+def run_render(args):
+    print(json.dumps(measure_render(args)), flush=True)
     return 0
 
 
-def run_batch(args):
+def sum_over_ranks(dist, values, device):
+    """Element-wise sum of per-rank values over the process group."""
+    import torch
+    t = torch.tensor([float(v) for v in values], device=device, dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return [float(x) for x in t]
+
+
+def _frame_call(ctx, cam, st, seed, lin=None, rgba=None):
+    """One bc_render_frame call; returns (wall seconds, extension rays, bc_last_timing)."""
+    import bcgx
+    q = st.copy()
+    q.seed = seed
+    cc, sc = cam.c(), q.c()
+    rays = C.c_int64(0)
+    L = bcgx.lib()
+    t0 = time.perf_counter()
+    bcgx._lib.check(L.bc_render_frame(ctx.handle, C.byref(cc), C.byref(sc), bcgx._lib.ptr(lin, C.c_float), None,
+                                      bcgx._lib.ptr(rgba, C.c_uint32), C.byref(rays)), ctx.handle)
+    wall = time.perf_counter() - t0
+    return wall, rays.value, ctx.last_timing()
+
+
+def rmse_gpu_converged(ctx, ref, cam, st, window, conv_spp=CONVERGED_SPP, threads=0):
+    """RMSE of linear HDR radiance (post passes off) over a pixel window
+    (x0, y0, w, h) against a converged image of that window rendered by the GPU
+    wave engine at conv_spp samples per pixel (effectiveSPP caps a render at
+    4096, renderer.go:2395-2417, so it is the mean of conv_spp / 4096 renders
+    with distinct seeds). Reported at the configuration's spp for the wave
+    engine, the one-kernel form (the same samples: equal RMSE by construction)
+    and the oracle (an independent seed), each independent of the converged
+    image's seeds."""
+    import numpy as np
+    x0, y0, w, h = window
+    flat = st.copy()
+    flat.denoise, flat.bloom = False, 0
+
+    def gpu(settings):
+        return ctx.render_rows(cam, settings, y0, h)[0][:, x0:x0 + w].astype(np.float64)
+
+    conv = flat.copy()
+    conv.spp = min(conv_spp, 4096)
+    parts = max(1, conv_spp // conv.spp)
+    t0 = time.perf_counter()
+    acc = 0.0
+    for k in range(parts):
+        q = conv.copy()
+        q.seed = 0xC0417E + k
+        acc = acc + gpu(q)
+    conv_img = acc / parts
+    conv_s = time.perf_counter() - t0
+    eq = flat.copy()
+    eq.seed = 7
+    wave = gpu(eq)
+    ctx.set_option("render_engine", 1)
+    try:
+        plain = gpu(eq)
+    finally:
+        ctx.set_option("render_engine", 0)
+    t0 = time.perf_counter()
+    cpu = ref.render(cam, eq, seed=8, threads=threads, window=window)["linear"]
+    cpu_s = time.perf_counter() - t0
+
+    def rmse(a, b):
+        return float(np.sqrt(np.mean((a - b) ** 2)))
+
+    return {"converged": f"GPU wave engine, {parts * conv.spp} spp ({parts} x {conv.spp}), {w}x{h} pixels at "
+                         f"({x0}, {y0}) of the {st.width}x{st.height} frame, {conv_s:.1f} s",
+            "spp": st.spp, "mean_radiance": float(conv_img.mean()),
+            "gpu": rmse(wave, conv_img), "gpu_one_kernel": rmse(plain, conv_img), "cpu": rmse(cpu, conv_img),
+            "cpu_seconds": round(cpu_s, 2)}
+
+
+def _kernel_roofline(stats, t, segments):
+    """k_extend's roofline: algorithmic bytes per extension query (oracle
+    binary-BVH counters: 32 B per box test, 40 per triangle test, 32 per
+    sphere test, 24 ray in + 8 hit out) times the frame's queries, over the
+    kernel's device time in that frame."""
+    queries = max(1, stats["segments"] + stats["shadow"])
+    per_query = (32 * stats["boxes"] + 40 * stats["tris"] + 32 * stats["spheres"]) / queries + 32
+    peak, kind = _peaks()
+    achieved = per_query * segments / (t["extend_ms"] / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "k_extend__ultra_2560x1440_traffic.json")
+    if os.path.exists(tf) and t["extend_launches"]:
+        with open(tf) as f:
+            per_seg = json.load(f).get("dram_bytes_per_segment")
+        if per_seg:
+            traffic = per_seg * segments / t["extend_launches"]
+    return {"kernel": "k_extend", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_kind": kind,
+            "algorithmic_bytes_per_query": per_query,
+            "algorithmic_bytes_per_launch": per_query * segments / max(1, t["extend_launches"]),
+            "avg_launch_ms": t["extend_ms"] / max(1, t["extend_launches"]),
+            "box_tests_per_query": stats["boxes"] / queries, "tri_tests_per_query": stats["tris"] / queries}
+
+
+def _extras(args):
+    """The other configurations, measured in the same run with fewer steps."""
+    out = {}
+    a = copy.copy(args)
+    a.steps, a.warmup, a.rmse, a.autotune = max(3, min(args.steps, 10)), 3, False, False
+    try:
+        r = measure_raycast(a, cpu_seconds=3.0)
+        out["raycast"] = {k: r[k] for k in ("metric", "value", "unit", "ms_per_step", "e2e", "roofline",
+                                             "cpu_baseline", "any_hit", "gpu_launches", "clocks")}
+        out["raycast"]["workload"] = r["config"]["workload"]
+    except Exception as e:  # an extra line never hides the headline
+        out["raycast"] = {"error": repr(e)}
+    try:
+        c = copy.copy(a)
+        c.workload, c.steps, c.plain_steps = "cornell", max(10, a.steps), 2
+        r = measure_render(c)
+        out["cornell"] = {k: r.get(k) for k in ("metric", "value", "unit", "ms_per_step", "e2e", "plain",
+                                                 "wave_over_plain", "cpu_baseline", "clocks")}
+        out["cornell"]["workload"] = r["config"]["workload"]
+    except Exception as e:
+        out["cornell"] = {"error": repr(e)}
+    try:
+        b = copy.copy(a)
+        b.steps, b.warmup, b.plain_steps, b.views = 2, 1, 1, 64
+        r = measure_batch(b)
+        out["batch"] = {k: r.get(k) for k in ("metric", "value", "unit", "ms_per_step", "e2e", "plain",
+                                               "batched_over_plain", "plain_one_kernel", "batched_over_one_kernel",
+                                               "cpu_baseline", "clocks")}
+        out["batch"]["workload"] = r["config"]["workload"]
+    except Exception as e:
+        out["batch"] = {"error": repr(e)}
+    try:
+        d = copy.copy(a)
+        d.steps, d.warmup = 5, 1
+        r = measure_diff(d)
+        out["adjoint"] = {k: r.get(k) for k in ("metric", "value", "unit", "forward_s", "backward_s",
+                                                 "loss_first_last", "cpu_baseline", "clocks")}
+        out["adjoint"]["workload"] = r["config"]["workload"]
+    except Exception as e:
+        out["adjoint"] = {"error": repr(e)}
+    return out
+
+
+def measure_ultra(args):
+    """The headline line (see the module docstring); None on ranks other than 0."""
+    import numpy as np
+    import torch
+    import bcgx
+    from bcgx import scenes
+    ws, rank, local = _dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    spec, cam, st = scenes.icosphere_grid()
+    if args.spp:
+        st.spp = args.spp
+    if args.adaptive is not None:  # the preset's own adaptive stop (threshold), off for equal-spp measurement
+        st.adaptive_sampling, st.adaptive_threshold = True, args.adaptive
+    t0 = time.perf_counter()
+    scene = scenes.to_scene(spec)
+    build_s = time.perf_counter() - t0
+    ctx = bcgx.Context(local)
+    if args.wave_cap:
+        ctx.set_option("render_wave_cap", args.wave_cap)
+    if args.extend is not None:
+        ctx.set_option("render_extend", args.extend)
+    ctx.upload(scene)
+    stats = ctx.scene_stats()
+    W, H = st.width, st.height
+    seed0 = 0x5EED0000 + 7919 * rank  # every rank renders its own samples
+    for k in range(args.warmup):
+        _frame_call(ctx, cam, st, seed0 + k)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    dev_ms, walls, rays, launches = [], [], 0, 0
+    for k in range(args.steps):
+        w, r, t = _frame_call(ctx, cam, st, seed0 + 1000 + k)
+        dev_ms.append(t["device_ms"])
+        walls.append(w)
+        rays += r
+        launches += t["launches"]
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    # device time per kernel class of one more frame (an event before every launch)
+    ctx.set_option("render_timing", 1)
+    try:
+        _, kr, kt = _frame_call(ctx, cam, st, seed0 + 1000)
+    finally:
+        ctx.set_option("render_timing", 0)
+    # the plain one-kernel form on the first timed frames' seeds: the same samples
+    plain = None
+    if args.plain_steps > 0:
+        ctx.set_option("render_engine", 1)
+        try:
+            _frame_call(ctx, cam, st, seed0 + 999)
+            pms, pr = [], 0
+            for k in range(args.plain_steps):
+                _, r, t = _frame_call(ctx, cam, st, seed0 + 1000 + k)
+                pms.append(t["device_ms"])
+                pr += r
+        finally:
+            ctx.set_option("render_engine", 0)
+        plain = {"value": pr / sum(pms) / 1e3, "unit": METRIC, "ms_per_step": sum(pms) / len(pms),
+                 "steps": len(pms), "segments_per_step": pr // len(pms),
+                 "form": "one kernel launch per view, thread per pixel looping over samples and bounces "
+                         "(the reference OpenCL kernel's shape), same seeds as the first timed frames"}
+    # e2e: the reference-facing call with host outputs (pinned), copies inside the region
+    lin = torch.empty((H, W, 3), dtype=torch.float32).pin_memory().numpy()
+    rgba = torch.empty((H, W), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    _frame_call(ctx, cam, st, seed0 + 4000, lin, rgba)
+    e2e_steps = max(1, min(args.steps, 3))
+    ew, er = [], 0
+    for k in range(e2e_steps):
+        w, r, _ = _frame_call(ctx, cam, st, seed0 + 5000 + k, lin, rgba)
+        ew.append(w)
+        er += r
+    total_ms, e2e_s = sum(dev_ms), sum(ew)
+    all_rays, all_e2e_rays = float(rays), float(er)
+    if dist:
+        total_ms, e2e_s = max_over_ranks(dist, [total_ms, e2e_s], dev)
+        all_rays, all_e2e_rays = sum_over_ranks(dist, [rays, er], dev)
+        dist.barrier()
+    if rank != 0:
+        ctx.close()
+        if dist:
+            dist.destroy_process_group()
+        return None
+    value = all_rays / (total_ms / 1e3) / 1e6
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 primary rays)", "data": ULTRA_DATA,
+            "config": {"workload": ULTRA_WORKLOAD, "spp": st.spp, "segments_per_step": rays // args.steps,
+                       "triangles": spec.n_triangles(), "bvh8_nodes": stats["nodes8"],
+                       "scene_bytes": stats["device_bytes"], "host_bvh_build_s": round(build_s, 2),
+                       "l2": "not flushed: path state (64 Mi paths x 104 B) and scene exceed the 126 MB L2",
+                       "wave_cap": ctx.get_option("render_wave_cap"),
+                       "extend_variant": ctx.get_option("render_extend"),
+                       "shade_block": ctx.get_option("render_shade_block"),
+                       "parallelism": f"replicas x{ws}"},
+            "wall_ms_per_step": 1e3 * sum(walls) / args.steps,
+            "e2e": {"value": all_e2e_rays / e2e_s / 1e6,
+                    "unit": METRIC, "steps": e2e_steps,
+                    "h2d_bytes_per_step": C.sizeof(bcgx._lib.CameraC) + C.sizeof(bcgx._lib.SettingsC),
+                    "d2h_bytes_per_step": W * H * 16,
+                    "call": "bc_render_frame, linear HDR + RGBA8 into pinned host buffers, wall clock"},
+            "gpu_launches": launches,
+            "kernel_times_ms": {k: round(kt[k], 3) for k in ("device_ms", "generate_ms", "extend_ms", "shade_ms",
+                                                              "connect_ms", "accumulate_ms", "post_ms", "other_ms")},
+            "kernel_share": {k[:-3]: round(kt[k] / max(1e-9, kt["device_ms"]), 4)
+                             for k in ("generate_ms", "extend_ms", "shade_ms", "connect_ms", "accumulate_ms",
+                                       "post_ms", "other_ms")},
+            "clocks": clk,
+            "frame_ms": [round(x, 2) for x in dev_ms]}
+    if plain:
+        line["plain"] = plain
+        line["wave_over_plain"] = value / plain["value"]
+    ref = None
+    if not args.no_cpu_baseline:
+        import oracle
+        ref = oracle.OracleScene.from_spec(spec)
+        cst = st.copy()
+        cst.spp = CPU_SPP_ULTRA
+        t0 = time.perf_counter()
+        out = ref.render(cam, cst, seed=7, threads=0)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": out["stats"]["segments"] / dt / 1e6, "unit": METRIC,
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"the full {W}x{H} frame at {cst.spp} spp, {dt:.1f} s"}
+        line["roofline"] = _kernel_roofline(out["stats"], kt, kr)
+        line["frame_roofline"] = _render_roofline(out["stats"], value)
+    if not args.no_rmse and ref is not None:
+        line["rmse"] = rmse_gpu_converged(ctx, ref, cam, st, (W // 2 - 64, H // 2 - 36, 128, 72))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    if ws == 1 and not args.no_extras:
+        line["configs"] = _extras(args)
+    return line
+
+
+def run_headline(args):
+    line = measure_ultra(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_reference_ultra(args):
+    """The reference arm on the headline configuration: the oracle (the
+    reference's CPU integrator restated in C++ fp64) on all host cores; a step
+    is the full 2560x1440 frame at REF_SPP_ULTRA spp with a new seed."""
+    ws, rank, _ = _dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    from bcgx import scenes
+    spec, cam, st = scenes.icosphere_grid()
+    ref = oracle.OracleScene.from_spec(spec)
+    cores = os.cpu_count() or 1
+    cst = st.copy()
+    cst.spp = REF_SPP_ULTRA
+    for k in range(args.warmup):
+        ref.render(cam, cst, seed=100 + k, threads=0)
+    times, segs = [], 0
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        out = ref.render(cam, cst, seed=1000 + k, threads=0)
+        times.append(time.perf_counter() - t0)
+        segs += out["stats"]["segments"]
+    value = segs / sum(times) / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": ULTRA_DATA,
+            "config": {"workload": ULTRA_WORKLOAD, "spp_per_step": cst.spp, "segments_per_step": segs // args.steps},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                             "sample": f"the full {cst.width}x{cst.height} frame at {cst.spp} spp per step"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_reference(args):
+    if args.workload == "raycast":
+        return run_reference_raycast(args)
+    return run_reference_ultra(args)
+
+
+def measure_batch(args):
     """Batching workload: 4 resident scenes (10k / 50k / 200k / 500k random
     triangles + one emissive quad each), 64 views (log-uniform 128x128 ..
     1920x1080, spp U{4..64}, 8 bounces). Batched form = one bc_render_batch
@@ -635,12 +1019,16 @@ def run_batch(args):
         window = (st.width // 2 - 32, st.height // 2 - 32, 64, 64)
         line["rmse"] = {"view": v, "size": f"{st.width}x{st.height}",
                         **rmse_vs_converged(built[k], specs[k], cam, st, window)}
-    print(json.dumps(line), flush=True)
     ctx.close()
+    return line
+
+
+def run_batch(args):
+    print(json.dumps(measure_batch(args)), flush=True)
     return 0
 
 
-def run_diff(args):
+def measure_diff(args):
     """Differentiation workload: 200k random triangles on 256 diffuse material
     slots + 8 emissive quads, 512x512, 64 spp, 8 bounces (Russian roulette
     off). Target = the true parameters at 1024 spp (rendered once, untimed).
@@ -715,8 +1103,12 @@ def run_diff(args):
     if args.rmse:  # the forward's image at the initial parameters
         st = pb.settings
         line["rmse"] = rmse_vs_converged(scene, pb.spec, pb.cam, st, (st.width // 2 - 24, st.height // 2 - 24, 48, 48))
-    print(json.dumps(line), flush=True)
     ctx.close()
+    return line
+
+
+def run_diff(args):
+    print(json.dumps(measure_diff(args)), flush=True)
     return 0
 
 
@@ -941,18 +1333,22 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--tris", type=int, default=N_TRIS, help="smaller case for profiling")
-    ap.add_argument("--rays", type=int, default=N_RAYS, help="smaller case for profiling")
+    ap.add_argument("--tris", type=int, default=N_TRIS, help="ray cast: smaller case for profiling")
+    ap.add_argument("--rays", type=int, default=N_RAYS, help="ray cast: smaller case for profiling")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
+    ap.add_argument("--no-rmse", action="store_true", help="headline: skip the RMSE leg")
+    ap.add_argument("--no-extras", action="store_true", help="headline: skip the other configurations")
     ap.add_argument("--minblocks", type=int, default=0, help="ray-cast register variant (1, 6, 8; 0 = library default)")
     ap.add_argument("--split", type=int, default=None, help="ray cast: raycast_split 0 or 1 (default: library default)")
     ap.add_argument("--fast", action="store_true", help="plain fp32 closest hit instead of the exact contract")
-    ap.add_argument("--workload", default="raycast", choices=["raycast", "cornell", "ultra", "batch", "diff", "refit", "build", "integrators",
-                             "calibration"],
-                    help="raycast (default, the headline line) or a render workload")
+    ap.add_argument("--workload", default="ultra",
+                    choices=["ultra", "raycast", "cornell", "ultra-wall", "batch", "diff", "refit", "build",
+                             "integrators", "calibration"],
+                    help="ultra (default: the headline line) or another configuration")
     ap.add_argument("--spp", type=int, default=0, help="override spp of a render workload")
     ap.add_argument("--extend", type=int, default=None, help="render workloads: render_extend variant 0, 1 or 2")
-    ap.add_argument("--rmse", action="store_true", help="render workloads: RMSE against a converged image")
+    ap.add_argument("--rmse", action="store_true",
+                    help="cornell/batch/diff: RMSE against an oracle-converged image (slow)")
     ap.add_argument("--views", type=int, default=64, help="batch workload: number of views")
     ap.add_argument("--adaptive", type=float, default=None,
                     help="render workloads: turn the adaptive stop on with this threshold (Ultra preset: 8e-5)")
@@ -967,21 +1363,10 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
-    if args.workload == "batch":
-        return run_batch(args)
-    if args.workload == "diff":
-        return run_diff(args)
-    if args.workload == "refit":
-        return run_refit(args)
-    if args.workload == "build":
-        return run_build(args)
-    if args.workload == "integrators":
-        return run_integrators(args)
-    if args.workload == "calibration":
-        return run_calibration(args)
-    if args.workload != "raycast":
-        return run_render(args)
-    return run_gpu(args)
+    runners = {"ultra": run_headline, "raycast": run_gpu, "cornell": run_render, "ultra-wall": run_render,
+               "batch": run_batch, "diff": run_diff, "refit": run_refit, "build": run_build,
+               "integrators": run_integrators, "calibration": run_calibration}
+    return runners[args.workload](args)
 
 
 if __name__ == "__main__":

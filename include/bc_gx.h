@@ -196,16 +196,27 @@ bc_status bc_scene_stats(const bc_context* ctx, int64_t* out, int n_out);
  * Host pointers; copies in and out are part of the call.
  */
 bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out, int32_t* prim_out);
-/* Same on device pointers, enqueued on `stream` (a cudaStream_t, NULL = legacy default); asynchronous.
- * The context's scratch (ray order, per-ray records of the split passes, work
- * counter) is shared by its calls: calls of one context must not overlap on
- * different streams. */
+/* Same on device pointers, enqueued on `stream` (a cudaStream_t; NULL = the
+ * context's own stream) on the context's device; asynchronous. The returned
+ * status covers the arguments and the launch; what the kernels find while they
+ * run (a traversal stack or record limit) goes to a status word of the
+ * device-pointer calls that bc_sync() returns. The context's scratch (ray
+ * order, per-ray records of the split passes, work counter) is shared by its
+ * calls: calls of one context must not overlap on different streams. */
 bc_status bc_raycast_device(bc_context* ctx, const float* d_rays, int64_t n, float* d_t_out, int32_t* d_prim_out,
                             void* stream);
 /* Any hit (Scene.Occluded, renderer.go:851-895): occluded_out[i] = 1 if any primitive
  * is hit within [tmin, tmax], fp64-exact like bc_raycast. */
 bc_status bc_occluded(bc_context* ctx, const float* rays, int64_t n, uint8_t* occluded_out);
 bc_status bc_occluded_device(bc_context* ctx, const float* d_rays, int64_t n, uint8_t* d_occluded_out, void* stream);
+/* Waits for `stream` (NULL = the context's own stream) and returns the kernel
+ * status of the bc_raycast_device / bc_occluded_device calls enqueued since the
+ * last bc_sync (BC_OK, or the error a kernel flagged: BC_ERR_CAPACITY for a
+ * traversal stack or queue limit, BC_ERR_TIMEOUT, BC_ERR_DEVICE), then clears
+ * it. That status never surfaces through another call. Replaces the blocking
+ * read after each OpenCL enqueue (gpu_opencl_windows.go:671-690), whose error
+ * becomes the render's (clErr, 180-185). */
+bc_status bc_sync(bc_context* ctx, void* stream);
 
 /* ---- rendering ---------------------------------------------------------- */
 
@@ -390,12 +401,15 @@ bc_status bc_post_process(bc_context* ctx, int32_t width, int32_t height, const 
  * enqueued. It calls no cudaMalloc, cudaFree or allocating library routine.
  * Its scratch is a static device array of two images of at most 921,600 pixels
  * (22 MB), which every GPU that loads the library holds until the process
- * exits; larger frames are rejected with BC_ERR_INVALID_ARG, as are aliased
- * input and output. Every call shares that array: calls that overlap on the
+ * exits; larger frames are rejected with BC_ERR_INVALID_ARG, and so are
+ * output buffers (linear or RGBA) that share any byte with each other or with
+ * an input. Every call shares that array: calls that overlap on the
  * GPU (different streams, or devices sharing it across threads without
  * ordering) race on it. The first call on each device looks up the array's
  * device address (cudaGetSymbolAddress) with that device current; make that
- * first call before any stream capture.
+ * first call before any stream capture. The address is kept for the life of
+ * the process: do not call this entry point on a device after cudaDeviceReset
+ * on it.
  */
 bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_linear_in, const float* d_guide_nd,
                                   const bc_settings* settings, float* d_linear_out, uint32_t* d_rgba_out,
@@ -446,6 +460,9 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *                        in shared memory, 40 registers (twelve blocks).
  *   "render_shade_block" 256 (default) or 128: threads per block of the wave
  *                        engine's shading kernel (three or six blocks per SM).
+ *   "render_timing"      0 (default); 1: the renders record an event before every
+ *                        kernel launch (no captured graph) for bc_last_timing's
+ *                        per-kernel times; images are the same.
  *   "render_engine"      0 (default): the wave engine; 1: one kernel launch per
  *                        view, one thread per pixel looping over samples and
  *                        bounces (the reference OpenCL kernel's shape, kept as the
@@ -482,6 +499,28 @@ typedef struct bc_tune_report {
 } bc_tune_report;
 bc_status bc_autotune_raycast(bc_context* ctx, const float* d_rays, int64_t n, bc_tune_report* out);
 bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_views, bc_tune_report* out);
+
+/*
+ * Device time of the last render call of the context (bc_render_rows,
+ * bc_render_frame, bc_render_moments, bc_render_batch, bc_forward,
+ * bc_backward): CUDA events recorded on the context's stream before its first
+ * and after its last device work (render, and the post stack for
+ * bc_render_frame). With the option "render_timing" 1 the wave engine launches
+ * without its captured graph and records an event before every kernel, and the
+ * per-class fields give the device time between consecutive events, charged to
+ * the kernel launched at the first of them. A photon-map build that a render
+ * starts runs before its first event and is not counted. No reference counterpart (the
+ * reference times whole renders on the host, benchmark.go:103-135).
+ */
+typedef struct bc_timing {
+  double device_ms;         /* whole call */
+  int64_t launches;         /* kernels the call launched */
+  int64_t extend_launches;  /* of which closest-hit launches of the wave engine */
+  int32_t kernel_timing;    /* 1: the per-class times below were measured */
+  int32_t reserved;
+  double generate_ms, extend_ms, shade_ms, connect_ms, accumulate_ms, post_ms, other_ms;
+} bc_timing;
+bc_status bc_last_timing(const bc_context* ctx, bc_timing* out);
 
 /* Request cancellation of the running or next render of ctx; safe from any thread. */
 bc_status bc_cancel(bc_context* ctx);

@@ -52,7 +52,7 @@ def test_struct_layouts_match_the_header(native_lib, tmp_path):
     from bcgx import _lib
     pairs = [("bc_scene_desc", _lib.SceneDesc), ("bc_camera", _lib.CameraC), ("bc_settings", _lib.SettingsC),
              ("bc_view", _lib.ViewC), ("bc_diff_desc", _lib.DiffDescC), ("bc_post_desc", _lib.PostDescC),
-             ("bc_tune_report", _lib.TuneReportC)]
+             ("bc_tune_report", _lib.TuneReportC), ("bc_timing", _lib.TimingC)]
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "bc_gx.h"', "int main(void) {"]
     for cname, py in pairs:
         lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')

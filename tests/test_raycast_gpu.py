@@ -258,3 +258,42 @@ def test_split_passes_parity(gpu_ctx, orc, which):
         gpu_ctx.set_option("raycast_sort", 1)
     assert np.array_equal(three[1], two[1]) and np.array_equal(three[0], two[0])
     assert np.array_equal(occ3, occ2)
+
+
+def test_device_call_status_reaches_its_own_sync(gpu_ctx, native_lib):
+    """A kernel status raised during bc_raycast_device / bc_occluded_device is
+    returned by that call's bc_sync, and no later unrelated call sees it. The
+    status bit is raised by the test hook "test_status_bits" (a one-thread
+    kernel ORs it into the device-pointer calls' status word on their stream),
+    as a traversal stack overflow would; nothing faults."""
+    torch = pytest.importorskip("torch")
+    import bcgx
+    spec = scenes.random_triangles(20_000, seed=21)
+    gpu_ctx.upload(scenes.to_scene(spec))
+    rays = scenes.random_rays(4096, seed=22)
+    dev = torch.device("cuda", 0)
+    d_rays = torch.from_numpy(rays).to(dev)
+    d_t = torch.empty(len(rays), dtype=torch.float32, device=dev)
+    d_p = torch.empty(len(rays), dtype=torch.int32, device=dev)
+    d_o = torch.empty(len(rays), dtype=torch.uint8, device=dev)
+    s = torch.cuda.Stream(device=dev)
+    torch.cuda.synchronize()
+    # clean calls: sync is OK
+    gpu_ctx.raycast_device(d_rays.data_ptr(), len(rays), d_t.data_ptr(), d_p.data_ptr(), s.cuda_stream)
+    gpu_ctx.sync(s.cuda_stream)
+    kStatusStackOverflow = 1
+    for call in ("closest", "any"):
+        gpu_ctx.set_option("test_status_bits", kStatusStackOverflow)
+        if call == "closest":
+            gpu_ctx.raycast_device(d_rays.data_ptr(), len(rays), d_t.data_ptr(), d_p.data_ptr(), s.cuda_stream)
+        else:
+            gpu_ctx.occluded_device(d_rays.data_ptr(), len(rays), d_o.data_ptr(), s.cuda_stream)
+        # an unrelated host call in between does not pick the bit up
+        t_h, p_h = gpu_ctx.raycast(rays)
+        with pytest.raises(bcgx.BCError) as e:
+            gpu_ctx.sync(s.cuda_stream)
+        assert e.value.status == 9  # BC_ERR_CAPACITY: the stack-overflow status of this call
+        gpu_ctx.sync(s.cuda_stream)  # cleared by the sync that returned it
+        torch.cuda.synchronize()
+        if call == "closest":  # the results themselves are unaffected by the hook
+            assert np.array_equal(d_p.cpu().numpy(), p_h)

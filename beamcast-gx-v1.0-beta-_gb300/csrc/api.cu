@@ -149,7 +149,7 @@ void bc_destroy(bc_context* ctx) {
   destroy_post_state(ctx);
   destroy_photon_state(ctx);
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_tri, &ctx->d_slot64, &ctx->d_snorm, &ctx->d_slot_prim, &ctx->d_mats,
-                    &ctx->d_lights, &ctx->d_lpdf, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ,
+                    &ctx->d_lights, &ctx->d_lpdf, &ctx->d_bin, &ctx->d_rays, &ctx->d_t, &ctx->d_prim, &ctx->d_occ,
                     &ctx->d_kids8, &ctx->d_geom, &ctx->d_build, &ctx->d_build_out, &ctx->d_order[0],
                     &ctx->d_order[1], &ctx->d_order[2], &ctx->d_rec[0], &ctx->d_rec[1], &ctx->d_rec[2],
                     &ctx->d_rec_any})
@@ -201,7 +201,8 @@ static bc_status install_scene(bc_context* ctx, const PackedScene& ps, const std
       (st = upload(ctx, ctx->d_mats, ps.mats.data(), ps.mats.size() * sizeof(MatGPU), "material upload")) ||
       (st = upload(ctx, ctx->d_lights, ps.lights.data(), ps.lights.size() * sizeof(LightGPU), "light upload")) ||
       (st = upload(ctx, ctx->d_lpdf, ps.light_pdf_by_prim.data(), ps.light_pdf_by_prim.size() * sizeof(float),
-                   "light pdf upload")))
+                   "light pdf upload")) ||
+      (st = upload(ctx, ctx->d_bin, ps.bin.data(), ps.bin.size() * sizeof(BinNode), "binary BVH upload")))
     return st;
   // The host arrays of `ps` may die once this returns: drain the copies first.
   e = cudaStreamSynchronize(ctx->stream);
@@ -215,6 +216,8 @@ static bc_status install_scene(bc_context* ctx, const PackedScene& ps, const std
   ds.mats = ctx->d_mats.as<MatGPU>();
   ds.lights = ctx->d_lights.as<LightGPU>();
   ds.light_pdf_by_prim = ctx->d_lpdf.as<float>();
+  ds.bin = ctx->d_bin.as<BinNode>();
+  ds.n_bin = (int32_t)ps.bin.size();
   ds.n_mats = (int32_t)ps.mats.size();
   ds.n_lights = ranges.empty() ? 0 : ranges[0].n_lights;  // the single-view calls see scene 0
   ds.n_prims = ps.n_prims;
@@ -232,7 +235,8 @@ static bc_status install_scene(bc_context* ctx, const PackedScene& ps, const std
   ctx->stats[5] = (int64_t)(ps.nodes.size() * sizeof(Node8) + ps.tri.size() * sizeof(F4) +
                             ps.slot64.size() * sizeof(double) + ps.snorm.size() * sizeof(F4) +
                             slots * sizeof(int32_t) + ps.mats.size() * sizeof(MatGPU) +
-                            ps.lights.size() * sizeof(LightGPU) + ps.light_pdf_by_prim.size() * sizeof(float));
+                            ps.lights.size() * sizeof(LightGPU) + ps.light_pdf_by_prim.size() * sizeof(float) +
+                            ps.bin.size() * sizeof(BinNode));
   ctx->mat_kind.assign(ps.mats.size(), 0);
   for (size_t i = 0; i < ps.mats.size(); i++) ctx->mat_kind[i] = (int8_t)ps.mats[i].kind;
   ctx->mat_is_light.assign(ps.mats.size(), 0);

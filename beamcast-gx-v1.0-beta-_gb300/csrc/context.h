@@ -73,7 +73,7 @@ struct bc_context {
   bool has_scene = false;
   uint64_t scene_id = 0, topo_rev = 0, geom_rev = 0;
   bcgx::DeviceScene ds;
-  bcgx::DevBuf d_nodes, d_tri, d_slot64, d_snorm, d_slot_prim, d_mats, d_lights, d_lpdf;
+  bcgx::DevBuf d_nodes, d_tri, d_slot64, d_snorm, d_slot_prim, d_mats, d_lights, d_lpdf, d_bin;
   std::vector<bcgx::SceneRange> ranges;  // scenes of the resident set (one for bc_scene_upload)
   bool is_set = false;                    // resident scenes came from bc_scene_set_upload
   bcgx::GeomInfo geom;                    // geometry-only updates (refit.cu)

@@ -16,6 +16,8 @@ struct DeviceScene {
   const MatGPU* mats = nullptr;
   const LightGPU* lights = nullptr;
   const float* light_pdf_by_prim = nullptr;
+  const BinNode* bin = nullptr;  // the caller's binary BVH of scene 0 (exact-tie replay)
+  int32_t n_bin = 0;
   int32_t n_mats = 0, n_lights = 0, n_prims = 0;
   int32_t stack_need = 0;
   bool has_spheres = false;

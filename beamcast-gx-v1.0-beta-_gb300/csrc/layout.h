@@ -44,6 +44,20 @@ struct alignas(16) Node8 {
 };
 static_assert(sizeof(Node8) == 96, "Node8 must be 96 bytes");
 
+// The caller's binary BVH node (Scene.Nodes, renderer.go:109-118) as the
+// reference traverses it: fp64 box, children (-1 for leaves), leaf range in
+// Order. Only rays whose closest hit is an exact fp64 tie read these: they are
+// re-walked with the reference's own traversal so the tie resolves as it does.
+struct alignas(16) BinNode {
+  double lo[3], hi[3];
+  int32_t left, right, start, count;
+};
+static_assert(sizeof(BinNode) == 64, "BinNode must be 64 bytes");
+
+// Result marker of a ray-cast pass for a ray whose closest fp64 distance is
+// shared by several primitives; the tie pass replaces it by the reference's answer.
+constexpr int32_t kTieMark = -2;
+
 struct alignas(16) F4 {
   float x, y, z, w;
 };

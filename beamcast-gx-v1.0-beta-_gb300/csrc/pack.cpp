@@ -243,6 +243,22 @@ void pack_lights(const bc_scene_desc& d, PackedScene* ps) {
 
 }  // namespace
 
+void pack_binary(const bc_scene_desc& d, std::vector<BinNode>* out) {
+  out->resize(d.n_nodes);
+  for (int32_t i = 0; i < d.n_nodes; i++) {
+    BinNode& b = (*out)[i];
+    for (int k = 0; k < 3; k++) {
+      b.lo[k] = d.node_box[6 * (size_t)i + k];
+      b.hi[k] = d.node_box[6 * (size_t)i + 3 + k];
+    }
+    const bool leaf = d.node_count[i] > 0;
+    b.left = leaf ? -1 : d.node_left[i];
+    b.right = leaf ? -1 : d.node_right[i];
+    b.start = leaf ? d.node_start[i] : 0;
+    b.count = leaf ? d.node_count[i] : 0;
+  }
+}
+
 bc_status pack_scene(const bc_scene_desc& d, PackedScene* out, std::string* err) {
   bc_status st = validate(d, err);
   if (st != BC_OK) return st;
@@ -251,6 +267,7 @@ bc_status pack_scene(const bc_scene_desc& d, PackedScene* out, std::string* err)
     out->n_binary = d.n_nodes;
     pack_slots(d, out);
     collapse(d, out);
+    pack_binary(d, &out->bin);
     pack_materials(d, out);
     pack_lights(d, out);
     for (int k = 0; k < 3; k++) {
@@ -301,6 +318,7 @@ bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::v
     }
     out->tri.insert(out->tri.end(), ps.tri.begin(), ps.tri.end());
     out->slot64.insert(out->slot64.end(), ps.slot64.begin(), ps.slot64.end());
+    if (k == 0) out->bin = std::move(ps.bin);  // the ray-cast entry points trace scene 0
     const int32_t n_mats = (int32_t)ps.mats.size();
     for (F4 f : ps.snorm) {
       int32_t m;

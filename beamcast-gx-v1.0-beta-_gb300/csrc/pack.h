@@ -17,6 +17,7 @@ struct PackedScene {
   std::vector<F4> snorm;         // 1 per slot
   std::vector<int32_t> slot_prim;
   std::vector<int32_t> kids8;    // 8 per node: binary node index of each child (-1: empty slot)
+  std::vector<BinNode> bin;      // the caller's binary BVH (scene 0 of a set), for exact-tie replay
   std::vector<MatGPU> mats;
   std::vector<LightGPU> lights;
   std::vector<float> light_pdf_by_prim;
@@ -45,6 +46,8 @@ bc_status pack_scene(const bc_scene_desc& d, PackedScene* out, std::string* err)
 // `ranges[k]` tells where each scene starts. stack_need is the maximum.
 bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::vector<SceneRange>* ranges,
                          std::string* err);
+// The caller's binary BVH as BinNode records (validated descriptor).
+void pack_binary(const bc_scene_desc& d, std::vector<BinNode>* out);
 // Sphere-light records and per-primitive light selection pdfs of a scene.
 void pack_scene_lights(const bc_scene_desc& d, PackedScene* out);
 

@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(128, MINB) k_closest_exact(SceneView sv, const
   if (!active) return;
   if (h.slot >= 0) {
     t_out[i] = __double2float_rn(h.t64);
-    prim_out[i] = __ldg(sv.slot_prim + h.slot);
+    prim_out[i] = h.tie ? kTieMark : __ldg(sv.slot_prim + h.slot);
   } else {
     t_out[i] = -1.0f;
     prim_out[i] = -1;
@@ -75,6 +75,8 @@ __global__ void __launch_bounds__(128) k_closest_fast(SceneView sv, const float4
 // per-warp queue in shared memory; when 32 are parked, the warp settles them
 // in fp64 with every lane active. Triangle-only scenes (spheres settle at
 // once and use the kernels above).
+constexpr int kParkTie = 0x100;  // npend flag: the walk already compared two equal fp64 distances
+
 struct ParkQueue {
   long long idx[32];
   int bslot[32];
@@ -104,22 +106,25 @@ __device__ __forceinline__ void settle_parked(const SceneView& sv, const float4*
       atomicOr(status, kStatusBound);  // a certain hit must pass its fp64 test
     }
   }
-  const int np = q.npend[k];
+  const int np = q.npend[k] & 0xff;
+  bool tie = (q.npend[k] & kParkTie) != 0;
 #pragma unroll
   for (int j = 0; j < kPending; j++) {
     if (j < np && !(bslot >= 0 && q.plo[j][k] > bhi)) {
       const int sj = q.pslot[j][k];
       double t;
-      if (tri_hit64(sv.slot64 + 9 * (size_t)sj, o, d, tmin, tmax, &t) &&
-          (win < 0 || t < wt || (t == wt && sj > win))) {
-        win = sj;
-        wt = t;
+      if (tri_hit64(sv.slot64 + 9 * (size_t)sj, o, d, tmin, tmax, &t)) {
+        tie = tie || (win >= 0 && t == wt);
+        if (win < 0 || t < wt || (t == wt && sj > win)) {
+          win = sj;
+          wt = t;
+        }
       }
     }
   }
   if (win >= 0) {
     t_out[i] = __double2float_rn(wt);
-    prim_out[i] = __ldg(sv.slot_prim + win);
+    prim_out[i] = tie ? kTieMark : __ldg(sv.slot_prim + win);
   } else {
     t_out[i] = -1.0f;
     prim_out[i] = -1;
@@ -181,7 +186,7 @@ __global__ void __launch_bounds__(128, MINB) k_closest_exact_persistent(SceneVie
         q.idx[k] = idx;
         q.bslot[k] = leaf.best.slot;
         q.bhi[k] = leaf.best.hi;
-        q.npend[k] = leaf.npend;
+        q.npend[k] = leaf.npend | (leaf.tie ? kParkTie : 0);
 #pragma unroll
         for (int j = 0; j < kPending; j++) {
           q.pslot[j][k] = leaf.pend[j].slot;
@@ -380,6 +385,7 @@ __global__ void __launch_bounds__(128) k_exact_settle(SceneView sv, const float4
     const float bhi = rec.bhi[i];
     int win = -1;
     double wt = 0.0;
+    bool tie = false;
     if (bslot >= 0) {
       double t;
       if (tri_hit64(sv.slot64 + 9 * (size_t)bslot, o, d, tmin, tmax, &t)) {
@@ -394,14 +400,16 @@ __global__ void __launch_bounds__(128) k_exact_settle(SceneView sv, const float4
       if (bslot >= 0 && lo > bhi) continue;
       const int sj = rec.pslot[(size_t)j * n + i];
       double t;
-      if (tri_hit64(sv.slot64 + 9 * (size_t)sj, o, d, tmin, tmax, &t) &&
-          (win < 0 || t < wt || (t == wt && sj > win))) {
-        win = sj;
-        wt = t;
+      if (tri_hit64(sv.slot64 + 9 * (size_t)sj, o, d, tmin, tmax, &t)) {
+        tie = tie || (win >= 0 && t == wt);
+        if (win < 0 || t < wt || (t == wt && sj > win)) {
+          win = sj;
+          wt = t;
+        }
       }
     }
     t_out[i] = win >= 0 ? __double2float_rn(wt) : -1.0f;
-    prim_out[i] = win >= 0 ? __ldg(sv.slot_prim + win) : -1;
+    prim_out[i] = win >= 0 ? (tie ? kTieMark : __ldg(sv.slot_prim + win)) : -1;
   }
 }
 
@@ -426,7 +434,7 @@ __global__ void __launch_bounds__(128) k_closest_exact_list(SceneView sv, const 
     const HitResult h = closest_hit_exact<STACK, false>(sv, r, b.w, status, active);
     if (active) {
       t_out[i] = h.slot >= 0 ? __double2float_rn(h.t64) : -1.0f;
-      prim_out[i] = h.slot >= 0 ? __ldg(sv.slot_prim + h.slot) : -1;
+      prim_out[i] = h.slot >= 0 ? (h.tie ? kTieMark : __ldg(sv.slot_prim + h.slot)) : -1;
     }
   }
 }
@@ -689,6 +697,158 @@ __global__ void k_ray_scatter(int64_t n, const uint32_t* __restrict__ keys, int3
   perm[totals[k / kScanBlock] + atomicAdd(&bins[k], 1)] = (int32_t)i;
 }
 
+// ---- exact ties: the reference's own walk ------------------------------------
+// A ray marked kTieMark has its closest fp64 distance shared by two or more
+// primitives. Which of them the reference returns depends on its traversal
+// order: triHit accepts t == closest (renderer.go:702), so the last one tested
+// at that distance wins. Such a ray is walked again here exactly as Scene.Hit
+// walks the caller's binary BVH (renderer.go:777-849): a 16-entry stack of
+// (node, entry distance); a popped entry at or beyond the closest hit is
+// skipped (796); a leaf tests its primitives in Order (800-808); both children
+// are box-tested against the closest hit and pushed far first, the left one
+// nearer on equal entry distances (828-839); with the stack full, the
+// recursive descent of hitRecursive (815-826, 914-939) takes the left subtree,
+// then the right one, each node box-tested when it is reached. Arithmetic is
+// fp64 in the reference's operation order: prepareRay and HitAccel
+// (renderer.go:59-81, 147-210), triHit and sphereHitAccel.
+constexpr int kReplayDepth = 256;  // pending subtrees of the recursive descent
+
+struct Accel64 {
+  D3 o, inv;
+  bool zx, zy, zz;
+};
+
+// One slab of HitAccel: an axis with |d| < 1e-15 only checks the origin.
+__device__ __forceinline__ bool slab64(bool zero, double o, double inv, double mn, double mx, double* near,
+                                       double* far) {
+  if (zero) return !(o < mn || o > mx);
+  double t0 = __dmul_rn(__dsub_rn(mn, o), inv);
+  double t1 = __dmul_rn(__dsub_rn(mx, o), inv);
+  if (inv < 0) {
+    const double x = t0;
+    t0 = t1;
+    t1 = x;
+  }
+  if (t0 > *near) *near = t0;
+  if (t1 < *far) *far = t1;
+  return !(*far <= *near);
+}
+
+__device__ __forceinline__ bool box64(const BinNode* __restrict__ b, const Accel64& a, double tmin, double tmax,
+                                      double* near_out) {
+  double near = tmin, far = tmax;
+  if (!slab64(a.zx, a.o.x, a.inv.x, __ldg(&b->lo[0]), __ldg(&b->hi[0]), &near, &far)) return false;
+  if (!slab64(a.zy, a.o.y, a.inv.y, __ldg(&b->lo[1]), __ldg(&b->hi[1]), &near, &far)) return false;
+  if (!slab64(a.zz, a.o.z, a.inv.z, __ldg(&b->lo[2]), __ldg(&b->hi[2]), &near, &far)) return false;
+  *near_out = near;
+  return true;
+}
+
+// A leaf's primitives in Order; each accepted hit becomes the closest.
+__device__ __forceinline__ void leaf64(const SceneView& sv, const BinNode* __restrict__ b, D3 o, D3 d, double tmin,
+                                       double* closest, int* best) {
+  const int s0 = __ldg(&b->start), cnt = __ldg(&b->count);
+  for (int k = 0; k < cnt; k++) {
+    const int s = s0 + k;
+    const bool sphere = __ldg(reinterpret_cast<const float*>(sv.tri + 3 * (size_t)s + 2) + 3) < 0.0f;
+    double t;
+    const bool hit = sphere ? sphere_hit64(sv.slot64 + 9 * (size_t)s, o, d, tmin, *closest, &t)
+                            : tri_hit64(sv.slot64 + 9 * (size_t)s, o, d, tmin, *closest, &t);
+    if (hit) {
+      *closest = t;
+      *best = s;
+    }
+  }
+}
+
+// Returns the winning slot (-1: miss) and its distance.
+__device__ int replay_closest(const SceneView& sv, const BinNode* __restrict__ bin, D3 o, D3 d, double tmin,
+                              double tmax, double* t_out, unsigned* status) {
+  Accel64 a;
+  a.o = o;
+  a.zx = fabs(d.x) < 1e-15;
+  a.zy = fabs(d.y) < 1e-15;
+  a.zz = fabs(d.z) < 1e-15;
+  a.inv.x = a.zx ? 0.0 : __ddiv_rn(1.0, d.x);
+  a.inv.y = a.zy ? 0.0 : __ddiv_rn(1.0, d.y);
+  a.inv.z = a.zz ? 0.0 : __ddiv_rn(1.0, d.z);
+  double closest = tmax;
+  int best = -1;
+  double root_near;
+  if (!box64(bin, a, tmin, tmax, &root_near)) return -1;
+  int sn[16];
+  double sd[16];
+  int dfs[kReplayDepth];
+  int sp = 1;
+  sn[0] = 0;
+  sd[0] = root_near;
+  while (sp > 0) {
+    sp--;
+    if (sd[sp] >= closest) continue;
+    const BinNode* n = bin + sn[sp];
+    if (__ldg(&n->count) > 0) {
+      leaf64(sv, n, o, d, tmin, &closest, &best);
+      continue;
+    }
+    const int l = __ldg(&n->left), r = __ldg(&n->right);
+    double ln = 0.0, rn = 0.0;
+    const bool lok = box64(bin + l, a, tmin, closest, &ln);
+    const bool rok = box64(bin + r, a, tmin, closest, &rn);
+    if (!lok && !rok) continue;
+    if (sp + 2 > 16) {  // hitRecursive on the left child, then on the right one
+      int dp = 0;
+      if (rok) dfs[dp++] = r;
+      if (lok) dfs[dp++] = l;
+      while (dp > 0) {
+        const BinNode* m = bin + dfs[--dp];
+        double mn;
+        if (!box64(m, a, tmin, closest, &mn)) continue;
+        if (__ldg(&m->count) > 0) {
+          leaf64(sv, m, o, d, tmin, &closest, &best);
+          continue;
+        }
+        if (dp + 2 > kReplayDepth) {  // a tree deeper than the replay holds: report, never guess
+          atomicOr(status, kStatusStackOverflow);
+          return -1;
+        }
+        dfs[dp++] = __ldg(&m->right);
+        dfs[dp++] = __ldg(&m->left);
+      }
+      continue;
+    }
+    if (lok && rok) {
+      if (ln <= rn) {
+        sn[sp] = r; sd[sp++] = rn;
+        sn[sp] = l; sd[sp++] = ln;
+      } else {
+        sn[sp] = l; sd[sp++] = ln;
+        sn[sp] = r; sd[sp++] = rn;
+      }
+    } else if (lok) {
+      sn[sp] = l; sd[sp++] = ln;
+    } else {
+      sn[sp] = r; sd[sp++] = rn;
+    }
+  }
+  *t_out = closest;
+  return best;
+}
+
+__global__ void __launch_bounds__(128) k_tie_replay(SceneView sv, const BinNode* __restrict__ bin,
+                                                    const float4* __restrict__ rays, int64_t n,
+                                                    float* __restrict__ t_out, int32_t* __restrict__ prim_out,
+                                                    unsigned* status) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if (prim_out[i] != kTieMark) continue;
+    const float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
+    const D3 o{(double)a.x, (double)a.y, (double)a.z}, d{(double)b.x, (double)b.y, (double)b.z};
+    double t = 0.0;
+    const int s = replay_closest(sv, bin, o, d, (double)a.w, (double)b.w, &t, status);
+    t_out[i] = s >= 0 ? __double2float_rn(t) : -1.0f;
+    prim_out[i] = s >= 0 ? __ldg(sv.slot_prim + s) : -1;
+  }
+}
+
 template <class K>
 int persistent_blocks(K kernel) {
   int dev = 0, sms = 0, per = 0;
@@ -871,11 +1031,24 @@ cudaError_t launch_raycast_closest(const DeviceScene& s, const float4* rays, int
   cudaError_t e = order_rays(s, rays, n, order_scratch, &perm, st);
   if (e) return e;
   switch (stack_variant(s.stack_need)) {
-    case 64: return closest_var<64>(s, rays, n, t_out, prim_out, status, work, variant, perm, rec_scratch, st);
-    case 128: return closest_var<128>(s, rays, n, t_out, prim_out, status, work, variant, perm, rec_scratch, st);
-    case 256: return closest_var<256>(s, rays, n, t_out, prim_out, status, work, variant, perm, rec_scratch, st);
+    case 64: e = closest_var<64>(s, rays, n, t_out, prim_out, status, work, variant, perm, rec_scratch, st); break;
+    case 128: e = closest_var<128>(s, rays, n, t_out, prim_out, status, work, variant, perm, rec_scratch, st); break;
+    case 256: e = closest_var<256>(s, rays, n, t_out, prim_out, status, work, variant, perm, rec_scratch, st); break;
     default: return cudaErrorInvalidValue;
   }
+  if (e || variant == 0) return e;  // the plain fp32 form makes no tie promise
+  if (!s.bin) return cudaErrorInvalidValue;  // every uploaded scene carries its binary tree
+  // exact ties: rays the passes above marked are walked again as the reference walks them
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
+  }
+  k_tie_replay<<<(int)std::min<int64_t>((int64_t)sms * 4, (n + 127) / 128), 128, 0, st>>>(view_of(s), s.bin, rays, n,
+                                                                                        t_out, prim_out, status);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_raycast_any(const DeviceScene& s, const float4* rays, int64_t n, uint8_t* out, unsigned* status,

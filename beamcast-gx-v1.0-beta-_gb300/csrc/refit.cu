@@ -55,6 +55,15 @@ __global__ void k_refit_nodes(int n8, const int32_t* __restrict__ kids8, const d
   nodes[k] = nd;
 }
 
+__global__ void k_refit_binary(int m, const double* __restrict__ box, BinNode* __restrict__ bin) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  for (int k = 0; k < 3; k++) {
+    bin[i].lo[k] = box[6 * (size_t)i + k];
+    bin[i].hi[k] = box[6 * (size_t)i + 3 + k];
+  }
+}
+
 static bc_status put(bc_context* ctx, double* dst, const double* src, size_t n) {
   if (!n) return BC_OK;
   cudaError_t e = cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
@@ -99,6 +108,8 @@ bc_status update_geometry(bc_context* ctx, const bc_scene_desc& d) {
       const_cast<float4*>(ctx->ds.snorm));
   k_refit_nodes<<<(gi.n_node8 + 127) / 128, 128, 0, ctx->stream>>>(gi.n_node8, ctx->d_kids8.as<int32_t>(), g.box,
                                                                   const_cast<Node8*>(ctx->ds.nodes));
+  if (ctx->ds.n_bin == (int32_t)m)  // the binary boxes the exact-tie replay walks
+    k_refit_binary<<<(int)((m + 255) / 256), 256, 0, ctx->stream>>>((int)m, g.box, const_cast<BinNode*>(ctx->ds.bin));
   if ((e = cudaGetLastError())) return cuda_status(ctx, e, "geometry update");
   // sphere lights follow their spheres (and the caller's light distribution)
   PackedScene lp;

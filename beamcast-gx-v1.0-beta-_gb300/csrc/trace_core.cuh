@@ -12,9 +12,10 @@
 //    statistical, so a 1-ulp change of a distance is immaterial there.
 //
 // Closest-hit tie rule: triHit accepts t <= closest (renderer.go:702), so at
-// bit-identical fp64 distances the later-tested primitive wins. Within a
-// leaf that is the later Order slot, and the EXACT walk applies "later slot
-// wins" across leaves as well.
+// bit-identical fp64 distances the primitive the reference's traversal tests
+// last wins. The EXACT walk visits the tree in its own order, so it flags a
+// ray whose best fp64 distance it sees twice (HitResult.tie); the ray-cast
+// passes then replay the reference's binary walk for that ray alone.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -290,6 +291,7 @@ struct HitResult {
   int32_t slot;   // -1 on a miss
   float t32;      // fast mode distance
   double t64;     // exact mode distance
+  bool tie;       // exact mode: another primitive had the same fp64 distance as a best hit
 };
 
 constexpr uint32_t kEnd = 0x7fffffffu;  // "no node": bit 31 clear and above any node index
@@ -637,6 +639,7 @@ struct ExactClosestLeaf {
   float tmax_ray;
   float tlim;
   bool done;
+  bool tie;  // two contenders compared equal in fp64
   Contender best;
   int npend;
   PendEntry pend[kPending];
@@ -649,6 +652,7 @@ struct ExactClosestLeaf {
     tmax_ray = tmax;
     tlim = widen(tmax);
     done = false;
+    tie = false;
     npend = 0;
     best.slot = -1;
     best.lo = tmax;
@@ -677,7 +681,10 @@ struct ExactClosestLeaf {
         atomicOr(status, kStatusBound);  // a certain hit must pass its fp64 test
         best = c;
       } else if (c.t64 < best.t64 || (c.t64 == best.t64 && c.slot > best.slot)) {
+        tie = tie || c.t64 == best.t64;
         best = c;
+      } else {
+        tie = tie || c.t64 == best.t64;
       }
     }
     tlim = widen(best.hi);
@@ -766,9 +773,10 @@ struct ExactClosestLeaf {
         c.hi = __int_as_float(0x7f800000);
         c.t64 = 0.0;
         c.exact = false;
-        if (resolve(c) &&
-            (win.slot < 0 || c.t64 < win.t64 || (c.t64 == win.t64 && c.slot > win.slot)))
-          win = c;
+        if (resolve(c)) {
+          if (win.slot >= 0 && c.t64 == win.t64) tie = true;
+          if (win.slot < 0 || c.t64 < win.t64 || (c.t64 == win.t64 && c.slot > win.slot)) win = c;
+        }
       }
     }
     best = win;
@@ -786,6 +794,7 @@ __device__ __forceinline__ HitResult closest_hit_exact(const SceneView& sv, cons
   h.slot = active ? leaf.best.slot : -1;
   h.t32 = 0.0f;
   h.t64 = h.slot >= 0 ? leaf.best.t64 : -1.0;
+  h.tie = h.slot >= 0 && leaf.tie;
   return h;
 }
 
@@ -901,6 +910,7 @@ __device__ __forceinline__ HitResult closest_hit_fast(const SceneView& sv, const
   h.slot = leaf.best_slot;
   h.t32 = leaf.best_t;
   h.t64 = 0.0;
+  h.tie = false;
   return h;
 }
 

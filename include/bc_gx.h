@@ -191,8 +191,10 @@ bc_status bc_scene_stats(const bc_context* ctx, int64_t* out, int n_out);
  * Semantics are those of Scene.Hit (renderer.go:777-849) evaluated in fp64 on
  * the fp32 ray: prim_out[i] is the Scene primitive index of the nearest hit
  * (-1 on a miss) and t_out[i] = float32(t_fp64) (-1 on a miss). Exact: the hit
- * index equals the fp64 CPU path's; distinct primitives at bit-identical fp64
- * distances resolve to the later slot in Scene.Order.
+ * index equals the fp64 CPU path's, exact ties included: a ray whose nearest
+ * fp64 distance several primitives share is walked again over the caller's
+ * binary BVH as Scene.Hit walks it, so it gets the primitive the reference
+ * keeps (the last one tested at that distance, renderer.go:702, 800-808).
  * Host pointers; copies in and out are part of the call.
  */
 bc_status bc_raycast(bc_context* ctx, const float* rays, int64_t n, float* t_out, int32_t* prim_out);

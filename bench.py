@@ -34,7 +34,7 @@ the unit the reference counts as Rays (renderer.go:1491).
             (whose per-pixel means the oracle parity tests check): the wave
             engine, the one-kernel form and the oracle at 256 spp.
   cpu_baseline: the oracle (fp64 restatement of the reference integrator) on
-            the machine's host cores, the full frame at 16 spp.
+            the machine's host cores, the full frame at 32 spp.
   configs : the other configurations measured in the same run: ray cast
             (Mrays/s), Cornell box, 64-view batch, adjoint s/iter.
 
@@ -72,7 +72,7 @@ ULTRA_WORKLOAD = ("ultra-realism shape: 2,048,130 tris (64x64 displaced icospher
                   "2560x1440, 256 spp, 16 bounces, RR from bounce 6, Halton, MIS, power lights, denoise x3, "
                   "bloom 1, ACES; adaptive stop off (equal spp)")
 ULTRA_DATA = "synthetic, seeded (scene seed 0xBEAC0003)"
-CPU_SPP_ULTRA = 16   # oracle sample of the frame for cpu_baseline (about 10 s on 16 cores)
+CPU_SPP_ULTRA = 32   # oracle sample of the frame for cpu_baseline (about 13 s on 16 cores)
 REF_SPP_ULTRA = 2    # oracle sample per step of the reference arm
 CONVERGED_SPP = 16384
 

@@ -6,7 +6,7 @@ GPU against the fp64 oracle's restatement.
   emission by emission; an emission's path can split only at an fp32-vs-fp64
   boundary decision. Checked: the photon counts, the per-emission deposits and
   the photons themselves (position, normal, flux) for the emissions that match.
-* Images: per-pixel z-tests at equal spp against the oracle, and common random
+* Images: z-tests of 2x2 pixel blocks at 256 spp against the oracle (zstats.py), and common random
   numbers (same seed): the recursive integrator draws its light samples after
   the subtree below each vertex, as the reference's recursion does, and the
   GPU defers them in the same order, so CRN replays hold for it too.
@@ -16,6 +16,7 @@ import pytest
 
 import bcgx
 from bcgx import scenes
+from zstats import assert_parity
 
 pytestmark = pytest.mark.gpu
 
@@ -29,16 +30,6 @@ def _settings(integrator, w=96, h=64, spp=8, bounces=5, level=1, sampler="Halton
     st.firefly_clamp, st.rr_depth, st.adaptive_sampling = 0.0, 3, False
     st.integrator, st.photon_mapping, st.seed = integrator, level, seed
     return st
-
-
-def _z_frac(m_g, q_g, m_c, q_c, n):
-    v_g = np.maximum(q_g - m_g * m_g, 0) * n / (n - 1)
-    v_c = np.maximum(q_c - m_c * m_c, 0) * n / (n - 1)
-    se = np.sqrt(v_g / n + v_c / n)
-    live = se > 1e-6
-    z = (m_g[live] - m_c[live]) / se[live]
-    gse = np.sqrt(v_g.mean() / (n * m_g.size) * 4 + v_c.mean() / (n * m_c.size) * 4)
-    return float(np.mean(np.abs(z) > 3)), (m_g.mean() - m_c.mean()) / max(gse, 1e-12)
 
 
 @pytest.fixture(scope="module")
@@ -111,15 +102,13 @@ def test_common_random_numbers(gpu_ctx, cornell, integrator):
 def test_statistical_parity(gpu_ctx, orc, integrator, which):
     spec, cam = {"cornell_ref": scenes.cornell_reference_scene, "showcase": scenes.showcase_scene}[which]()
     gpu_ctx.upload(scenes.to_scene(spec))
-    st = _settings(integrator, w=128, h=80, spp=24, bounces=6, level=2, seed=5)
+    st = _settings(integrator, w=128, h=80, spp=256, bounces=6, level=2, seed=5)
     m_g, q_g, _ = gpu_ctx.render_moments(cam, st)
     # independent pixel samples (seed 6) over the same photon map (emission seed 5):
     # a photon map is one draw for the whole frame, so the pixels' sample
     # variance does not cover a difference of maps
     out = orc.OracleScene.from_spec(spec).render(cam, st, seed=6, threads=0, photon_seed=5)
-    frac, gz = _z_frac(m_g.astype(np.float64), q_g.astype(np.float64), out["linear"], out["sumsq"], st.spp)
-    assert frac < 0.015, f"{frac:.4f} beyond 3 sigma"
-    assert abs(gz) < 4, f"global mean z = {gz:.2f}"
+    assert_parity(f"{integrator} {which}", m_g, q_g, st.spp, out["linear"], out["sumsq"], st.spp)
 
 
 def test_research_integrators_smoke(gpu_ctx):

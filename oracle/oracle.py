@@ -99,8 +99,35 @@ _SIG = [
 _lib = None
 
 
+REF_TREE = "/root/reference"  # the reference's sources, where this repository is built from them
+HX_LIB = os.path.join(HERE, "_ref", "libhxref.so")
+
+
 def build():
     subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if os.path.isdir(os.path.join(REF_TREE, "source", "src")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"], check=True)
+
+
+def hx_reference_closest(verts9, rays8):
+    """Closest hit of the reference's own C++ code (beamcast::hx::PackedScene,
+    built by `make -C oracle ref` into _ref/), or None when it was not built.
+    verts9: (n, 9) triangle vertices; rays8: (m, 8) float32 rays. Returns
+    (t float32, prim int32) in the triangles' numbering."""
+    if not os.path.exists(HX_LIB):
+        return None
+    L = C.CDLL(HX_LIB)
+    f = L.hxref_closest
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_int32),
+                  C.POINTER(C.c_float)]
+    v = np.ascontiguousarray(verts9, dtype=np.float64).reshape(-1, 9)
+    r = np.ascontiguousarray(rays8, dtype=np.float32).reshape(-1, 8)
+    prim = np.empty(len(r), np.int32)
+    t = np.empty(len(r), np.float32)
+    if f(len(v), _p(v, C.c_double), len(r), _p(r, C.c_float), _p(prim, C.c_int32), _p(t, C.c_float)) != 0:
+        raise RuntimeError("the reference's closest hit threw")
+    return t, prim
 
 
 def lib():

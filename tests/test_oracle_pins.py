@@ -4,12 +4,14 @@ The reference's ray sets come from Go math/rand seeds; equivalent rays are
 drawn here from numpy with the same construction formulas.
 """
 import math
+import os
 import struct
 
 import numpy as np
 import pytest
 
 from bcgx import scenes
+from conftest import ROOT
 
 
 def bits(x):
@@ -270,3 +272,29 @@ def test_window_render_equals_frame(orc):
     assert np.array_equal(full["sumsq"][7:20, 10:31], win["sumsq"])
     with pytest.raises(ValueError):
         s.render(cam, st, window=(60, 0, 10, 4))
+
+
+def test_triangle_closest_hit_against_the_reference_cpp(orc):
+    """The oracle's Scene.Hit restatement (fp64 triHit, renderer.go:684-711,
+    over the 32-bin SAH tree) against the closest hit of the reference's own C++
+    engine (beamcast::hx::PackedScene::hit, source/src/hx.cpp:237-270: fp32
+    Moller-Trumbore at hx.cpp:223-231 over its own BVH), on seeded random
+    triangles and rays. The fixture holds the reference's answers
+    (tests/golden/make_hx_golden.py); where the reference library is built here
+    (oracle/_ref) it is run as well and must reproduce the fixture. The two tests
+    differ only in precision (fp32 against fp64) and in their det threshold and
+    t-range ends, which random rays do not meet: every ray has the same hit
+    index, and t agrees to fp32 rounding of an ill-conditioned test."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "hx_closest.npz"))
+    verts = scenes.random_triangle_verts(int(g["n_tris"]), int(g["tri_seed"]))
+    rays = scenes.random_rays(int(g["n_rays"]), seed=int(g["ray_seed"]))
+    live = orc.hx_reference_closest(verts, rays)
+    if live is not None:
+        assert np.array_equal(live[1], g["prim"]) and np.array_equal(live[0], g["t"])
+    spec = scenes.random_triangles(int(g["n_tris"]), int(g["tri_seed"]))
+    t_o, p_o, _ = orc.OracleScene.from_spec(spec).hit_f32(rays)
+    assert np.array_equal(p_o, g["prim"])
+    hit = p_o >= 0
+    assert hit.sum() > 5000
+    rel = np.abs(t_o[hit] - g["t"][hit]) / np.abs(t_o[hit])
+    assert rel.max() < 2e-4 and np.percentile(rel, 99.9) < 2e-5

@@ -217,7 +217,9 @@ __global__ void __launch_bounds__(128, MINB) k_closest_exact_persistent(SceneVie
 //     the result; marked rays go to a list.
 //   pass 3, k_closest_exact_list: the marked rays, traced again by the
 //     one-kernel exact walk, whose full list falls back to fp64 in the walk.
-// Triangle-only scenes (as the persistent one-kernel form).
+// Triangle-only scenes (as the persistent one-kernel form). The rays and the
+// records pass through L2 once each way, so the walk and the settlement read
+// and write them evict-first (ld/st.global.cs): L2 stays with the scene.
 struct ExactRecords {
   int32_t* bslot;   // [n]: best certain hit, -1 none
   float* bhi;       // [n]: upper bound of its distance
@@ -345,7 +347,7 @@ __global__ void __launch_bounds__(128, 12) k_exact_walk(SceneView sv, const floa
         const unsigned long long my = base + (unsigned long long)__popc(m & below);
         if (my < (unsigned long long)n) {
           idx = perm ? (long long)perm[my] : (long long)my;
-          const float4 a = __ldg(rays + 2 * idx), b = __ldg(rays + 2 * idx + 1);
+          const float4 a = __ldcs(rays + 2 * idx), b = __ldcs(rays + 2 * idx + 1);
           r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
           leaf.reset(b.w);
           w.reset(r);
@@ -356,13 +358,13 @@ __global__ void __launch_bounds__(128, 12) k_exact_walk(SceneView sv, const floa
     }
     if (!__any_sync(0xffffffffu, idx >= 0)) break;
     if (idx >= 0 && w.step(sv, r, leaf, status)) {
-      rec.bslot[idx] = leaf.bslot;
-      rec.bhi[idx] = leaf.bhi;
-      rec.npend[idx] = leaf.npend;
+      __stcs(rec.bslot + idx, leaf.bslot);
+      __stcs(rec.bhi + idx, leaf.bhi);
+      __stcs(rec.npend + idx, leaf.npend);
       const int np = min(leaf.npend, kPending);
       for (int j = 0; j < np; j++) {
-        rec.pslot[(size_t)j * n + idx] = leaf.pend[j].slot;
-        rec.plo[(size_t)j * n + idx] = leaf.pend[j].lo;
+        __stcs(rec.pslot + (size_t)j * n + idx, leaf.pend[j].slot);
+        __stcs(rec.plo + (size_t)j * n + idx, leaf.pend[j].lo);
       }
       idx = -1;
     }
@@ -373,16 +375,16 @@ __global__ void __launch_bounds__(128) k_exact_settle(SceneView sv, const float4
                                                       ExactRecords rec, float* __restrict__ t_out,
                                                       int32_t* __restrict__ prim_out, unsigned* status) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int np = rec.npend[i];
+    const int np = __ldcs(rec.npend + i);
     if (np > kPending) {
       rec.redo[atomicAdd(rec.n_redo, 1ull)] = i;
       continue;
     }
-    const float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
+    const float4 a = __ldcs(rays + 2 * i), b = __ldcs(rays + 2 * i + 1);
     const D3 o{(double)a.x, (double)a.y, (double)a.z}, d{(double)b.x, (double)b.y, (double)b.z};
     const double tmin = (double)a.w, tmax = (double)b.w;
-    const int bslot = rec.bslot[i];
-    const float bhi = rec.bhi[i];
+    const int bslot = __ldcs(rec.bslot + i);
+    const float bhi = __ldcs(rec.bhi + i);
     int win = -1;
     double wt = 0.0;
     bool tie = false;
@@ -396,9 +398,9 @@ __global__ void __launch_bounds__(128) k_exact_settle(SceneView sv, const float4
       }
     }
     for (int j = 0; j < np; j++) {
-      const float lo = rec.plo[(size_t)j * n + i];
+      const float lo = __ldcs(rec.plo + (size_t)j * n + i);
       if (bslot >= 0 && lo > bhi) continue;
-      const int sj = rec.pslot[(size_t)j * n + i];
+      const int sj = __ldcs(rec.pslot + (size_t)j * n + i);
       double t;
       if (tri_hit64(sv.slot64 + 9 * (size_t)sj, o, d, tmin, tmax, &t)) {
         tie = tie || (win >= 0 && t == wt);
@@ -532,7 +534,7 @@ __global__ void __launch_bounds__(128, 12) k_any_walk(SceneView sv, const float4
         const unsigned long long my = base + (unsigned long long)__popc(m & below);
         if (my < (unsigned long long)n) {
           idx = perm ? (long long)perm[my] : (long long)my;
-          const float4 a = __ldg(rays + 2 * idx), b = __ldg(rays + 2 * idx + 1);
+          const float4 a = __ldcs(rays + 2 * idx), b = __ldcs(rays + 2 * idx + 1);
           r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);
           leaf.reset(b.w);
           w.reset(r);
@@ -563,7 +565,7 @@ __global__ void __launch_bounds__(128) k_any_settle(SceneView sv, const float4* 
   const long long cnt = (long long)*((volatile unsigned long long*)rec.count);
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += (long long)gridDim.x * blockDim.x) {
     const long long i = rec.idx[k];
-    const float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
+    const float4 a = __ldcs(rays + 2 * i), b = __ldcs(rays + 2 * i + 1);
     const int np = rec.npend[k];
     if (np > kPending) {
       const Ray32 r = make_ray(a.x, a.y, a.z, b.x, b.y, b.z, a.w);

@@ -158,6 +158,23 @@ struct BatchState {
 constexpr float kPi = 3.14159265358979323846f;
 constexpr int kMaxBounces = 1024;  // a wave is one launch sequence of max(bounces) steps
 
+// The path state streams through L2 once per kernel (tens of bytes per path,
+// gigabytes per wave), so its loads and stores are marked evict-first
+// (ld.global.cs / st.global.cs): L2 stays with the BVH nodes and triangle
+// records the walks reuse.
+__device__ __forceinline__ float sld(const float* p) { return __ldcs(p); }
+__device__ __forceinline__ int32_t sld(const int32_t* p) { return __ldcs(p); }
+__device__ __forceinline__ uint32_t sld(const uint32_t* p) { return __ldcs(p); }
+__device__ __forceinline__ uint64_t sld(const uint64_t* p) {
+  return __ldcs(reinterpret_cast<const unsigned long long*>(p));
+}
+__device__ __forceinline__ void sst(float* p, float v) { __stcs(p, v); }
+__device__ __forceinline__ void sst(int32_t* p, int32_t v) { __stcs(p, v); }
+__device__ __forceinline__ void sst(uint32_t* p, uint32_t v) { __stcs(p, v); }
+__device__ __forceinline__ void sst(uint64_t* p, uint64_t v) {
+  __stcs(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
+}
+
 __device__ __forceinline__ int warp_reserve(int* counter, bool pred) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned mask = __ballot_sync(0xffffffffu, pred);
@@ -248,17 +265,17 @@ __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __r
   Pcg32 rng;
   double jx, jy;
   primary_ray(V, x, y, s, seq, &o, &d, &rng, &jx, &jy);
-  ps.ox[i] = o.x; ps.oy[i] = o.y; ps.oz[i] = o.z;
-  ps.dx[i] = d.x; ps.dy[i] = d.y; ps.dz[i] = d.z;
-  ps.tx[i] = 1.0f; ps.ty[i] = 1.0f; ps.tz[i] = 1.0f;
-  ps.lx[i] = 0.0f; ps.ly[i] = 0.0f; ps.lz[i] = 0.0f;
-  ps.ppdf[i] = 0.0f;
-  ps.flags[i] = 0u;
-  ps.rs[i] = rng.state;
-  ps.ri[i] = rng.inc;
-  ps.view[i] = v;
-  ps.pix[i] = p;
-  ps.samp[i] = s;
+  sst(ps.ox + i, o.x); sst(ps.oy + i, o.y); sst(ps.oz + i, o.z);
+  sst(ps.dx + i, d.x); sst(ps.dy + i, d.y); sst(ps.dz + i, d.z);
+  sst(ps.tx + i, 1.0f); sst(ps.ty + i, 1.0f); sst(ps.tz + i, 1.0f);
+  sst(ps.lx + i, 0.0f); sst(ps.ly + i, 0.0f); sst(ps.lz + i, 0.0f);
+  sst(ps.ppdf + i, 0.0f);
+  sst(ps.flags + i, 0u);
+  sst(ps.rs + i, rng.state);
+  sst(ps.ri + i, rng.inc);
+  sst(ps.view + i, (int32_t)v);
+  sst(ps.pix + i, (int32_t)p);
+  sst(ps.samp + i, (int32_t)s);
   queue[slot] = i;
   if (s == 0 && V.want_guides) guide_jit[V.pix_off + p] = jitter_word(jx, jy);
 }
@@ -310,9 +327,10 @@ __device__ __forceinline__ void extend_body(SceneView sv, const ViewGPU* __restr
         const int my = base + __popc(m & below);
         if (my < n) {
           path = queue[my];
-          r = make_ray(ps.ox[path], ps.oy[path], ps.oz[path], ps.dx[path], ps.dy[path], ps.dz[path], 1e-4f);
+          r = make_ray(sld(ps.ox + path), sld(ps.oy + path), sld(ps.oz + path), sld(ps.dx + path),
+                       sld(ps.dy + path), sld(ps.dz + path), 1e-4f);
           leaf.reset(1e30f);
-          w.reset(r, views[ps.view[path]].root);
+          w.reset(r, views[sld(ps.view + path)].root);
         } else {
           exhausted = true;
         }
@@ -320,8 +338,8 @@ __device__ __forceinline__ void extend_body(SceneView sv, const ViewGPU* __restr
     }
     if (!__any_sync(0xffffffffu, path >= 0)) break;
     if (path >= 0 && w.step(sv, r, leaf, status)) {
-      ps.hit_t[path] = leaf.best_t;
-      ps.hit_slot[path] = leaf.best_slot;
+      sst(ps.hit_t + path, leaf.best_t);
+      sst(ps.hit_slot + path, (int32_t)leaf.best_slot);
       path = -1;
     }
   }
@@ -382,26 +400,30 @@ struct SoAPath {
   uint32_t flags;
   float ppdf;
   __device__ SoAPath(const PathSoA& p, int i) : ps(p), path(i) {
-    o = f3(ps.ox[i], ps.oy[i], ps.oz[i]);
-    d = f3(ps.dx[i], ps.dy[i], ps.dz[i]);
-    tp = f3(ps.tx[i], ps.ty[i], ps.tz[i]);
-    L = f3(ps.lx[i], ps.ly[i], ps.lz[i]);
+    o = f3(sld(ps.ox + i), sld(ps.oy + i), sld(ps.oz + i));
+    d = f3(sld(ps.dx + i), sld(ps.dy + i), sld(ps.dz + i));
+    tp = f3(sld(ps.tx + i), sld(ps.ty + i), sld(ps.tz + i));
+    L = f3(sld(ps.lx + i), sld(ps.ly + i), sld(ps.lz + i));
   }
   __device__ __forceinline__ void load_vertex() {  // only a path that hit a valid material needs these
-    rng.state = ps.rs[path];
-    rng.inc = ps.ri[path];
-    flags = ps.flags[path];
-    ppdf = ps.ppdf[path];
+    rng.state = sld(ps.rs + path);
+    rng.inc = sld(ps.ri + path);
+    flags = sld(ps.flags + path);
+    ppdf = sld(ps.ppdf + path);
   }
-  __device__ __forceinline__ float3 prev() const { return f3(ps.px[path], ps.py[path], ps.pz[path]); }
-  __device__ __forceinline__ void set_prev(float3 p) { ps.px[path] = p.x; ps.py[path] = p.y; ps.pz[path] = p.z; }
+  __device__ __forceinline__ float3 prev() const {
+    return f3(sld(ps.px + path), sld(ps.py + path), sld(ps.pz + path));
+  }
+  __device__ __forceinline__ void set_prev(float3 p) {
+    sst(ps.px + path, p.x); sst(ps.py + path, p.y); sst(ps.pz + path, p.z);
+  }
   __device__ __forceinline__ void store_continuation(float3 no, float3 nd) {
-    ps.ox[path] = no.x; ps.oy[path] = no.y; ps.oz[path] = no.z;
-    ps.dx[path] = nd.x; ps.dy[path] = nd.y; ps.dz[path] = nd.z;
-    ps.tx[path] = tp.x; ps.ty[path] = tp.y; ps.tz[path] = tp.z;
-    ps.flags[path] = flags;
-    ps.ppdf[path] = ppdf;
-    ps.rs[path] = rng.state;
+    sst(ps.ox + path, no.x); sst(ps.oy + path, no.y); sst(ps.oz + path, no.z);
+    sst(ps.dx + path, nd.x); sst(ps.dy + path, nd.y); sst(ps.dz + path, nd.z);
+    sst(ps.tx + path, tp.x); sst(ps.ty + path, tp.y); sst(ps.tz + path, tp.z);
+    sst(ps.flags + path, flags);
+    sst(ps.ppdf + path, ppdf);
+    sst(ps.rs + path, rng.state);
   }
 };
 
@@ -574,7 +596,9 @@ __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, cons
           nd_dir = rand_cos_hemisphere(N, rng);
           flags |= 1u;
           ppdf = fmaxf(0.0f, dot3(N, nd_dir)) / kPi;
-          s.set_prev(p);
+          // prevPoint feeds only lightDirectionalPDF of a sphere light hit,
+          // which is 0 for a view without sphere lights
+          if (wp.n_lights > 0) s.set_prev(p);
           no = p + N * 2e-4f;
         } else if (kind == BC_MAT_METAL) {
           const float rough = fminf(fmaxf(M.rough, 0.0f), 1.0f);
@@ -753,23 +777,25 @@ __device__ __forceinline__ void shade_body(const ViewGPU* __restrict__ views, in
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
     const int idx = base + threadIdx.x;
-    const int path = idx < n ? qcur[idx] : -1;
+    const int path = idx < n ? __ldcs(qcur + idx) : -1;
     VertexOut out;
     out.alive = false;
     out.shadow = false;
     if (path >= 0) {
-      const ViewGPU& wp = views[ps.view[path]];
+      const ViewGPU& wp = views[sld(ps.view + path)];
       SoAPath s(ps, path);
       GuideOut gd{guide_nd, guide_c, guide_jit, -1};
       if (bounce == 0 && wp.want_guides && ps.samp[path] == 0) gd.px = wp.pix_off + ps.pix[path];
+      const float hit_t = sld(ps.hit_t + path);
+      const int hit_slot = sld(ps.hit_slot + path);
       if (ALT && wp.integrator == BC_INTEGRATOR_RECURSIVE) {
-        const bool ended = shade_recursive(wp, n_mats, sc, s, ps.hit_t[path], ps.hit_slot[path], bounce, gd, rr, path);
+        const bool ended = shade_recursive(wp, n_mats, sc, s, hit_t, hit_slot, bounce, gd, rr, path);
         out.alive = !ended;
         if (ended) unwind_recursive(wp, sc, s.rng, rr, path, bounce, sh, cnt, sh_cap, status);
       } else {
-        shade_vertex<ALT>(wp, n_mats, sc, s, ps.hit_t[path], ps.hit_slot[path], bounce, gd, out);
+        shade_vertex<ALT>(wp, n_mats, sc, s, hit_t, hit_slot, bounce, gd, out);
       }
-      ps.lx[path] = s.L.x; ps.ly[path] = s.L.y; ps.lz[path] = s.L.z;
+      sst(ps.lx + path, s.L.x); sst(ps.ly + path, s.L.y); sst(ps.lz + path, s.L.z);
       if (rec.m) {
         const size_t r = (size_t)bounce * rec.cap + path;
         rec.m[r] = out.rec_m;
@@ -778,7 +804,7 @@ __device__ __forceinline__ void shade_body(const ViewGPU* __restrict__ views, in
       }
     }
     const int qn = warp_reserve(&cnt->q[cur ^ 1], out.alive);
-    if (out.alive) qnext[qn] = path;
+    if (out.alive) __stcs(qnext + qn, path);
     const int qs = warp_reserve(&cnt->shadow, out.shadow);
     if (out.shadow) {
       if (qs < sh_cap) {
@@ -912,7 +938,7 @@ __global__ void k_accumulate(const BatchState* __restrict__ bs, const ViewGPU* _
       bool stop = false;
       for (int s = s_lo; s < s_hi && !stop; s++) {
         const long long i = V.path_off + (long long)s * V.npix + p - w0;
-        float3 L = f3(ps.lx[i], ps.ly[i], ps.lz[i]);
+        float3 L = f3(sld(ps.lx + i), sld(ps.ly + i), sld(ps.lz + i));
         if (V.integrator == BC_INTEGRATOR_RECURSIVE)  // the visible light samples, deepest vertex first
           for (int b = rr.nb[i] - 1; b >= 0; b--) {
             const float4 A = rr.a[(size_t)b * rr.cap + i];

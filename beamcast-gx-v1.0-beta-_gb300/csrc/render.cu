@@ -187,6 +187,34 @@ __device__ __forceinline__ int warp_reserve(int* counter, bool pred) {
   return base + __popc(mask & ((1u << lane) - 1u));
 }
 
+// Queue slots for a block's surviving paths, in thread order, with one atomic
+// per block on the queue counter (per warp, the shading kernel's grid would
+// put hundreds of thousands of atomics on that one word every bounce). Every
+// thread of the block calls it; returns -1 where `alive` is false.
+template <int BLOCK>
+__device__ __forceinline__ int block_reserve(int* counter, bool alive) {
+  constexpr int kWarps = BLOCK / 32;
+  __shared__ int wbase[kWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned m = __ballot_sync(0xffffffffu, alive);
+  if (lane == 0) wbase[warp] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < kWarps; w++) {
+      const int c = wbase[w];
+      wbase[w] = s;
+      s += c;
+    }
+    const int base = s ? atomicAdd(counter, s) : 0;
+    for (int w = 0; w < kWarps; w++) wbase[w] += base;
+  }
+  __syncthreads();
+  const int pos = alive ? wbase[warp] + __popc(m & ((1u << lane) - 1u)) : -1;
+  __syncthreads();  // the next call rewrites wbase
+  return pos;
+}
+
 __device__ __forceinline__ int view_of(const ViewGPU* __restrict__ views, int n_views, long long g) {
   int lo = 0, hi = n_views - 1;  // last view with path_off <= g
   while (lo < hi) {
@@ -762,7 +790,7 @@ __device__ __forceinline__ void unwind_recursive(const ViewGPU& wp, const ShadeS
   rr.nb[path] = last + 1;
 }
 
-template <bool ALT>
+template <bool ALT, int BLOCK>
 __device__ __forceinline__ void shade_body(const ViewGPU* __restrict__ views, int n_mats, ShadeScene sc,
                                                PathSoA ps, const int* __restrict__ qcur, int* __restrict__ qnext,
                                                ShadowSoA sh, WaveCounters* cnt, int cur, int bounce,
@@ -803,7 +831,7 @@ __device__ __forceinline__ void shade_body(const ViewGPU* __restrict__ views, in
         rec.nb[path] = bounce + 1;
       }
     }
-    const int qn = warp_reserve(&cnt->q[cur ^ 1], out.alive);
+    const int qn = block_reserve<BLOCK>(&cnt->q[cur ^ 1], out.alive);
     if (out.alive) __stcs(qnext + qn, path);
     const int qs = warp_reserve(&cnt->shadow, out.shadow);
     if (out.shadow) {
@@ -830,9 +858,9 @@ __device__ __forceinline__ void shade_body(const ViewGPU* __restrict__ views, in
       GradRec rec, RecurRec rr, long long sh_cap, unsigned *status
 #define BC_SHADE_PASS views, n_mats, sc, ps, qcur, qnext, sh, cnt, cur, bounce, guide_nd, guide_c, guide_jit, rec, rr, sh_cap, status
 template <bool ALT>
-__global__ void __launch_bounds__(256, 3) k_shade(BC_SHADE_ARGS) { shade_body<ALT>(BC_SHADE_PASS); }
+__global__ void __launch_bounds__(256, 3) k_shade(BC_SHADE_ARGS) { shade_body<ALT, 256>(BC_SHADE_PASS); }
 template <bool ALT>
-__global__ void __launch_bounds__(128, 6) k_shade_128(BC_SHADE_ARGS) { shade_body<ALT>(BC_SHADE_PASS); }
+__global__ void __launch_bounds__(128, 6) k_shade_128(BC_SHADE_ARGS) { shade_body<ALT, 128>(BC_SHADE_PASS); }
 #undef BC_SHADE_ARGS
 #undef BC_SHADE_PASS
 

@@ -11,7 +11,7 @@
 //             budget and where the ray lives, i.e. resident blocks per SM) at
 //             the current wave size, the shading kernel's block shape
 //             (render_shade_block 256, 128), then paths per wave (render_wave_cap
-//             2^22 .. 2^26) with the chosen variant, on the caller's batch with
+//             2^22 .. 2^27) with the chosen variant, on the caller's batch with
 //             spp scaled down so one candidate traces at most 2^27 paths.
 //             Images depend on neither option, so no candidate changes a result.
 #include <algorithm>
@@ -200,7 +200,7 @@ bc_status bc_autotune_render(bc_context* ctx, const bc_view* views, int32_t n_vi
   long long best_cap = keep;
   rep.best_ms = best_ext_ms;
   std::vector<long long> caps;
-  for (int lg = 22; lg <= 26; lg++) {
+  for (int lg = 22; lg <= 27; lg++) {
     const long long cap = 1LL << lg;
     if (cap > 2 * sample && lg > 22) break;  // larger waves than the work: the same launches
     if (cap != keep) caps.push_back(cap);

@@ -285,7 +285,7 @@ __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __r
     p = (int)(local - (long long)s * views[v].npix);
     if (views[v].adaptive && (ad.n[views[v].pix_off + p] & kPixDone)) live = false;
   }
-  const int slot = warp_reserve(&cnt->q[0], live);
+  const int slot = block_reserve<256>(&cnt->q[0], live);  // launched with 256-thread blocks
   if (!live) return;
   const ViewGPU& V = views[v];
   const int x = p % V.W, y = V.y0 + p / V.W;

@@ -447,7 +447,7 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *                        between two streams, so one chunk's copies overlap
  *                        another's kernel.
  *   "render_wave_cap"    paths in flight per wave of the renderer, 4096 .. 2^27
- *                        (default 2^26: ~160 bytes of device memory per path,
+ *                        (default 2^27: ~160 bytes of device memory per path,
  *                        allocated up to what a render needs); images do not
  *                        depend on it. Each wave ends in a latency-bound tail of
  *                        long paths, so larger waves render faster.
@@ -486,7 +486,7 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
  * mode: raycast_sort only). Best of two timed runs each (CUDA events).
  * bc_autotune_render: the views as for bc_render_batch; first render_extend
  * 1, 0, 2 at the current wave size, then the other render_shade_block, then
- * render_wave_cap 2^22 .. 2^26 (up to twice the sample's paths) with the
+ * render_wave_cap 2^22 .. 2^27 (up to twice the sample's paths) with the
  * chosen variants. Each view's spp is scaled
  * down so that a candidate traces at most 2^27 paths; the adaptive stop is off
  * while timing. The second of two runs is timed.

@@ -848,8 +848,8 @@ __device__ __forceinline__ void shade_body(const ViewGPU* __restrict__ views, in
 }
 
 // Block shape of the shading kernel (bc_set_option "render_shade_block", chosen
-// per workload by bc_autotune_render): 256 threads at three blocks per SM, or
-// 128 threads at six; the same register budget and resident threads, a
+// per workload by bc_autotune_render): 256 threads at four blocks per SM, or
+// 128 threads at eight; the same 64-register budget and resident threads, a
 // different scheduling granularity of the grid-stride loop.
 #define BC_SHADE_ARGS                                                                                       \
   const ViewGPU *__restrict__ views, int n_mats, ShadeScene sc, PathSoA ps, const int *__restrict__ qcur,  \
@@ -858,9 +858,9 @@ __device__ __forceinline__ void shade_body(const ViewGPU* __restrict__ views, in
       GradRec rec, RecurRec rr, long long sh_cap, unsigned *status
 #define BC_SHADE_PASS views, n_mats, sc, ps, qcur, qnext, sh, cnt, cur, bounce, guide_nd, guide_c, guide_jit, rec, rr, sh_cap, status
 template <bool ALT>
-__global__ void __launch_bounds__(256, 3) k_shade(BC_SHADE_ARGS) { shade_body<ALT, 256>(BC_SHADE_PASS); }
+__global__ void __launch_bounds__(256, 4) k_shade(BC_SHADE_ARGS) { shade_body<ALT, 256>(BC_SHADE_PASS); }
 template <bool ALT>
-__global__ void __launch_bounds__(128, 6) k_shade_128(BC_SHADE_ARGS) { shade_body<ALT, 128>(BC_SHADE_PASS); }
+__global__ void __launch_bounds__(128, 8) k_shade_128(BC_SHADE_ARGS) { shade_body<ALT, 128>(BC_SHADE_PASS); }
 #undef BC_SHADE_ARGS
 #undef BC_SHADE_PASS
 
@@ -1513,10 +1513,10 @@ static WaveShape wave_shape(int cap, int bounces, bool lights, const GradArgs* g
   w.gen_grid = (cap + 255) / 256;
   w.ext_grid = ext[var];
   w.con_grid = con;
-  // grid-stride kernels at their resident blocks per SM (three of 256 threads,
-  // six of 128: their register budget): one wave of blocks, no partial last wave
+  // grid-stride kernels at their resident blocks per SM (four of 256 threads,
+  // eight of 128: their register budget): one wave of blocks, no partial last wave
   w.shade_block = shade_block == 128 ? 128 : 256;
-  w.shade_grid = sm_count() * (w.shade_block == 128 ? 6 : 3);
+  w.shade_grid = sm_count() * (w.shade_block == 128 ? 8 : 4);
   w.acc_grid = sm_count() * 3;
   w.bounces = bounces;
   w.lights = lights;

@@ -461,7 +461,7 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *                        ray in registers, 48 registers (ten blocks); 2: ray
  *                        in shared memory, 40 registers (twelve blocks).
  *   "render_shade_block" 256 (default) or 128: threads per block of the wave
- *                        engine's shading kernel (three or six blocks per SM).
+ *                        engine's shading kernel (four or eight blocks per SM, 64 registers).
  *   "render_timing"      0 (default); 1: the renders record an event before every
  *                        kernel launch (no captured graph) for bc_last_timing's
  *                        per-kernel times; images are the same.

@@ -346,7 +346,9 @@ __device__ __forceinline__ void extend_body(SceneView sv, const ViewGPU* __restr
   for (;;) {
     const bool need = path < 0 && !exhausted;
     const unsigned m = __ballot_sync(0xffffffffu, need);
-    if (m) {
+    // refill once several lanes are idle (or none is busy): a refill costs the
+    // whole warp a ballot, an atomic and the new rays' loads
+    if (m && (__popc(m) >= 8 || !__any_sync(0xffffffffu, path >= 0))) {
       const int leader = __ffs(m) - 1;
       int base = 0;
       if ((int)lane == leader) base = atomicAdd(&cnt->work_ext, __popc(m));

@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(128, MINB) k_closest_exact_persistent(SceneVie
   for (;;) {
     const bool need = idx < 0 && !exhausted;
     const unsigned m = __ballot_sync(0xffffffffu, need);
-    if (m) {
+    if (m && (__popc(m) >= kRefillLanes || !__any_sync(0xffffffffu, idx >= 0))) {
       const int leader = __ffs(m) - 1;
       unsigned long long base = 0;
       if ((int)lane == leader) base = atomicAdd(work, (unsigned long long)__popc(m));
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(128, 12) k_exact_walk(SceneView sv, const floa
   for (;;) {
     const bool need = idx < 0 && !exhausted;
     const unsigned m = __ballot_sync(0xffffffffu, need);
-    if (m) {
+    if (m && (__popc(m) >= kRefillLanes || !__any_sync(0xffffffffu, idx >= 0))) {
       const int leader = __ffs(m) - 1;
       unsigned long long base = 0;
       if ((int)lane == leader) base = atomicAdd(work, (unsigned long long)__popc(m));
@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(128, 12) k_any_walk(SceneView sv, const float4
   for (;;) {
     const bool need = idx < 0 && !exhausted;
     const unsigned m = __ballot_sync(0xffffffffu, need);
-    if (m) {
+    if (m && (__popc(m) >= kRefillLanes || !__any_sync(0xffffffffu, idx >= 0))) {
       const int leader = __ffs(m) - 1;
       unsigned long long base = 0;
       if ((int)lane == leader) base = atomicAdd(work, (unsigned long long)__popc(m));
@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(128) k_closest_fast_persistent(SceneView sv, c
   for (;;) {
     const bool need = idx < 0 && !exhausted;
     const unsigned m = __ballot_sync(0xffffffffu, need);
-    if (m) {
+    if (m && (__popc(m) >= kRefillLanes || !__any_sync(0xffffffffu, idx >= 0))) {
       const int leader = __ffs(m) - 1;
       unsigned long long base = 0;
       if ((int)lane == leader) base = atomicAdd(work, (unsigned long long)__popc(m));

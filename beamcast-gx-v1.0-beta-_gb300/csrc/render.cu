@@ -346,9 +346,7 @@ __device__ __forceinline__ void extend_body(SceneView sv, const ViewGPU* __restr
   for (;;) {
     const bool need = path < 0 && !exhausted;
     const unsigned m = __ballot_sync(0xffffffffu, need);
-    // refill once several lanes are idle (or none is busy): a refill costs the
-    // whole warp a ballot, an atomic and the new rays' loads
-    if (m && (__popc(m) >= 8 || !__any_sync(0xffffffffu, path >= 0))) {
+    if (m && (__popc(m) >= kRefillLanes || !__any_sync(0xffffffffu, path >= 0))) {
       const int leader = __ffs(m) - 1;
       int base = 0;
       if ((int)lane == leader) base = atomicAdd(&cnt->work_ext, __popc(m));
@@ -884,7 +882,7 @@ __global__ void __launch_bounds__(128) k_connect(SceneView sv, PathSoA ps, Shado
   for (;;) {
     const bool need = i < 0 && !exhausted;
     const unsigned m = __ballot_sync(0xffffffffu, need);
-    if (m) {
+    if (m && (__popc(m) >= kRefillLanes || !__any_sync(0xffffffffu, i >= 0))) {
       const int leader = __ffs(m) - 1;
       int base = 0;
       if ((int)lane == leader) base = atomicAdd(&cnt->work_con, __popc(m));

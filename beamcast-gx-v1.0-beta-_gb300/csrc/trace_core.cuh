@@ -27,6 +27,15 @@ namespace bcgx {
 constexpr float kU = 5.9604645e-8f;  // 2^-24, fp32 unit roundoff
 constexpr float kFarSlack = 8.0e-7f;  // > 2*gamma_3 + rounding of the scaling itself
 
+// Refill policy of the persistent walks: a warp takes new queries once this many
+// of its lanes are idle, or when none is busy. A refill costs the whole warp a
+// ballot, a queue atomic and the new rays' loads, so taking one per finished
+// lane is slower than letting a few lanes wait.
+#ifndef BCGX_REFILL_LANES
+#define BCGX_REFILL_LANES 8
+#endif
+constexpr int kRefillLanes = BCGX_REFILL_LANES;
+
 struct Ray32 {
   float ox, oy, oz;
   float dx, dy, dz;

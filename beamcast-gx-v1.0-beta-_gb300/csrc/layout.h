@@ -77,8 +77,11 @@ struct alignas(16) LightGPU {
   float cx, cy, cz, r;
   float er, eg, eb, select_pdf;
   int32_t prim;
-  int32_t pad;
-  double cdf;  // fp64, so the CDF search takes the CPU's branch for every draw
+  // the largest fp32 value <= cdf: for a draw u that is an fp32 value,
+  // cdf >= u exactly when cdf_dn >= u, so the search takes the CPU's fp64
+  // branch for every draw without fp64 arithmetic on the device
+  float cdf_dn;
+  double cdf;  // the light CDF entry (fp64, as the CPU holds it)
 };
 static_assert(sizeof(LightGPU) == 48, "LightGPU must be 48 bytes");
 

@@ -293,7 +293,8 @@ void pack_lights(const bc_scene_desc& d, PackedScene* ps) {
     if (pdf <= 0) pdf = 1.0 / (double)d.n_lights;  // chooseLight fallback, renderer.go:1389-1391
     L.select_pdf = (float)pdf;
     L.cdf = d.light_cdf[i];
-    L.pad = 0;
+    L.cdf_dn = (float)L.cdf;
+    if ((double)L.cdf_dn > L.cdf) L.cdf_dn = std::nextafter(L.cdf_dn, -INFINITY);
     L.prim = p;
   }
 }

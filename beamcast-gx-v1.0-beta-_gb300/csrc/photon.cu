@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(128) k_photon_trace(PhotonTraceArgs a, unsigne
     int out = 0;
     if (run) {
       Pcg32 rng = make_path_rng(a.seed, (uint64_t)k, kPhotonStream);
-      const int li = min((int)((double)rng.uniform() * (double)a.n_lights), a.n_lights - 1);  // rng.Intn
+      const int li = draw_index(rng, a.n_lights);  // rng.Intn
       const LightGPU Lg = a.lights[a.light_off + li];
       const float3 surf = rand_unit_vector(rng);
       float3 o = f3(Lg.cx, Lg.cy, Lg.cz) + surf * (Lg.r + 2e-4f);

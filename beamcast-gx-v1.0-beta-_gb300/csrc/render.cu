@@ -100,10 +100,11 @@ struct WaveCounters {
 // One view of a batch (or the single view of a frame / row chunk).
 struct ViewGPU {
   double origin[3], lower[3], horiz[3], vert[3];
-  // primary-ray constants, from the basis on the host: the lower-left corner
-  // relative to the origin (no cancellation on the device), the reciprocals of
-  // max(W - 1, 1) and max(H - 1, 1), the origin rounded to fp32
-  double base[3], inv_w1, inv_h1;
+  // primary-ray constants as float-float pairs (hi, lo), from the fp64 basis on
+  // the host: the lower-left corner relative to the origin (no cancellation on
+  // the device), the two spans, the reciprocals of max(W - 1, 1) and
+  // max(H - 1, 1); and the origin rounded to fp32
+  float2 base[3], span_u[3], span_v[3], inv_w1, inv_h1;
   float o32[3];
   long long path_off;  // first global path index of the view
   long long pix_off;   // first pixel of the view's rows in the frame buffers
@@ -224,44 +225,87 @@ __device__ __forceinline__ int view_of(const ViewGPU* __restrict__ views, int n_
   return lo;
 }
 
+// ---- float-float arithmetic (primary rays) ------------------------------------
+// A value is hi + lo with |lo| <= ulp(hi) / 2. TwoSum (Knuth, TAOCP vol. 2,
+// 4.2.2) and the FMA form of Dekker's TwoProduct give exact rounding errors;
+// sums use Dekker's add2 ("A floating-point technique for extending the
+// available precision", Numer. Math. 18, 1971), whose error stays below 2^-44 of
+// the larger operand. The _rn intrinsics keep the compiler from contracting or
+// reassociating the error terms.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_of(float2 v) { return FF{v.x, v.y}; }
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return FF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return FF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const FF s = ff_two_sum(a.hi, b.hi);
+  return ff_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return ff_fast_two_sum(p, e);
+}
+
 // ---- generate --------------------------------------------------------------
 // Primary ray of sample s of pixel (x, y) and the path's stream (adaptivePixel's
 // sample loop, renderer.go:1940-1950): Halton / R2 jitter rotated per pixel, or
-// random jitter; fp64 camera arithmetic, rounded to fp32 once. GB300's fp64
-// rate is a small fraction of its fp32 rate, so the per-sample fp64 work is
-// kept short: the pixel coordinate is scaled by a reciprocal instead of being
-// divided, and the direction is (lower - origin) + u horiz + v vert with the
-// first term from the host. Against the reference's operation order this moves
-// the fp64 direction by a few units in its last place, far below the fp32
-// rounding that follows.
-__device__ __forceinline__ void primary_ray(const ViewGPU& V, int x, int y, int s, const double2* __restrict__ seq,
-                                            float3* o, float3* d, Pcg32* rng, double* jx, double* jy) {
+// random jitter; the camera arithmetic in float-float (about 48 significant
+// bits, from the host's fp64 basis), rounded to fp32 once. GB300's fp64 pipe
+// runs at a small fraction of its fp32 rate, and the fp64 form of this
+// arithmetic (some 25 fp64 operations a sample) bounded k_generate. The pixel
+// coordinate is scaled by a reciprocal, and the direction is
+// (lower - origin) + u horiz + v vert with the first term from the host; against
+// the reference's fp64 operation order the direction moves by ~2^-44 of the
+// camera vectors' size before the fp32 rounding, which it changes only when the
+// fp64 value lies that close to a rounding boundary.
+// seq: per sample (x hi, x lo, y hi, y lo) of the view's sample table.
+__device__ __forceinline__ void primary_ray(const ViewGPU& V, int x, int y, int s, const float4* __restrict__ seq,
+                                            float3* o, float3* d, Pcg32* rng, float* jx_out, float* jy_out) {
   *rng = make_path_rng(V.seed, (uint64_t)y * (uint64_t)V.W + (uint64_t)x, (uint64_t)s);
+  FF jx, jy;
   if (V.sampler != BC_SAMPLER_RANDOM && s < V.nseq) {
-    double rx, ry;
-    pixel_rotation(x, y, &rx, &ry);
-    const double2 q = seq[V.seq_off + s];
-    // fract(q + r) with q, r in [0, 1): the sum lies in [0, 2), so floor is 0
-    // or 1 and a - 1 is exact (Sterbenz); the same bits as a - floor(a)
-    const double a = q.x + rx, b = q.y + ry;
-    *jx = a >= 1.0 ? a - 1.0 : a;
-    *jy = b >= 1.0 ? b - 1.0 : b;
+    // the per-pixel rotation h * 2^-32 split exactly into 24 + 8 bits
+    uint32_t h1, h2;
+    pixel_rotation_bits(x, y, &h1, &h2);
+    const float k24 = 1.0f / 16777216.0f, k32 = 1.0f / 4294967296.0f;
+    const FF rx{(float)(h1 >> 8) * k24, (float)(h1 & 255u) * k32};
+    const FF ry{(float)(h2 >> 8) * k24, (float)(h2 & 255u) * k32};
+    const float4 q = __ldg(seq + V.seq_off + s);
+    // fract(q + r) with q, r in [0, 1): the sum lies in [0, 2); hi - 1 is exact
+    // (Sterbenz) when the sum is at least 1
+    const FF a = ff_add(FF{q.x, q.y}, rx), b = ff_add(FF{q.z, q.w}, ry);
+    jx = (a.hi > 1.0f || (a.hi == 1.0f && a.lo >= 0.0f)) ? ff_fast_two_sum(a.hi - 1.0f, a.lo) : a;
+    jy = (b.hi > 1.0f || (b.hi == 1.0f && b.lo >= 0.0f)) ? ff_fast_two_sum(b.hi - 1.0f, b.lo) : b;
   } else {
-    *jx = (double)rng->uniform();
-    *jy = (double)rng->uniform();
+    jx = FF{rng->uniform(), 0.0f};
+    jy = FF{rng->uniform(), 0.0f};
   }
-  const double u = ((double)x + *jx) * V.inv_w1;
-  const double vv = ((double)(V.H - 1 - y) + *jy) * V.inv_h1;
+  const FF u = ff_mul(ff_add(FF{(float)x, 0.0f}, jx), ff_of(V.inv_w1));
+  const FF vv = ff_mul(ff_add(FF{(float)(V.H - 1 - y), 0.0f}, jy), ff_of(V.inv_h1));
   float dd[3];
 #pragma unroll
-  for (int k = 0; k < 3; k++) dd[k] = __double2float_rn(fma(V.vert[k], vv, fma(V.horiz[k], u, V.base[k])));
+  for (int k = 0; k < 3; k++)
+    dd[k] = ff_add(ff_add(ff_of(V.base[k]), ff_mul(ff_of(V.span_u[k]), u)), ff_mul(ff_of(V.span_v[k]), vv)).hi;
   *o = f3(V.o32[0], V.o32[1], V.o32[2]);
   *d = f3(dd[0], dd[1], dd[2]);
+  *jx_out = jx.hi;
+  *jy_out = jy.hi;
 }
 
-__device__ __forceinline__ uint32_t jitter_word(double jx, double jy) {
-  uint32_t a = (uint32_t)rintf(fminf(fmaxf((float)jx, 0.0f), 1.0f) * 65535.0f);
-  uint32_t b = (uint32_t)rintf(fminf(fmaxf((float)jy, 0.0f), 1.0f) * 65535.0f);
+__device__ __forceinline__ uint32_t jitter_word(float jx, float jy) {
+  uint32_t a = (uint32_t)rintf(fminf(fmaxf(jx, 0.0f), 1.0f) * 65535.0f);
+  uint32_t b = (uint32_t)rintf(fminf(fmaxf(jy, 0.0f), 1.0f) * 65535.0f);
   return (b << 16) | a;
 }
 
@@ -269,7 +313,7 @@ __device__ __forceinline__ uint32_t jitter_word(double jx, double jy) {
 // The wave's paths of pixels that have not stopped (adaptive sampling) enter
 // the first queue (warp-aggregated append; cnt->q[0] is zero on entry).
 __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __restrict__ views, PathSoA ps,
-                           int* __restrict__ queue, const double2* __restrict__ seq,
+                           int* __restrict__ queue, const float4* __restrict__ seq,
                            uint32_t* __restrict__ guide_jit, WaveCounters* cnt, AdaptState ad) {
   const long long w0 = bs->w0;
   const int n = (int)min((long long)bs->cap, bs->total - w0);
@@ -291,7 +335,7 @@ __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __r
   const int x = p % V.W, y = V.y0 + p / V.W;
   float3 o, d;
   Pcg32 rng;
-  double jx, jy;
+  float jx, jy;
   primary_ray(V, x, y, s, seq, &o, &d, &rng, &jx, &jy);
   sst(ps.ox + i, o.x); sst(ps.oy + i, o.y); sst(ps.oz + i, o.z);
   sst(ps.dx + i, d.x); sst(ps.dy + i, d.y); sst(ps.dz + i, d.z);
@@ -519,15 +563,15 @@ __device__ __forceinline__ int sample_direct(const ViewGPU& wp, const ShadeScene
   if (wp.n_lights <= 0) return 0;
   int li;
   float sel;
-  if (!wp.power) {  // rng.Intn (in fp64 so the index matches the CPU draw)
-    li = min((int)((double)rng.uniform() * (double)wp.n_lights), wp.n_lights - 1);
+  if (!wp.power) {  // rng.Intn
+    li = draw_index(rng, wp.n_lights);
     sel = 1.0f / (float)wp.n_lights;
   } else {  // sort.Search over LightCDF
-    const double r = (double)rng.uniform();
+    const float r = rng.uniform();
     int lo = 0, hi = wp.n_lights;
     while (lo < hi) {
       int mid = (lo + hi) >> 1;
-      if (!(__ldg(&sc.lights[wp.light_off + mid].cdf) >= r)) lo = mid + 1; else hi = mid;
+      if (!(__ldg(&sc.lights[wp.light_off + mid].cdf_dn) >= r)) lo = mid + 1; else hi = mid;
     }
     li = min(lo, wp.n_lights - 1);
     sel = __ldg(&sc.lights[wp.light_off + li].select_pdf);
@@ -1092,7 +1136,7 @@ __global__ void k_finish_views(const ViewGPU* __restrict__ views, int n_views, c
 // path of that sample is done.
 template <int STACK, bool SPH, bool ALT>
 __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict__ views, int v, int n_mats,
-                                                      ShadeScene sc, const double2* __restrict__ seq,
+                                                      ShadeScene sc, const float4* __restrict__ seq,
                                                       float* __restrict__ sum, float* __restrict__ sumsq,
                                                       float4* __restrict__ guide_nd, uint32_t* __restrict__ guide_c,
                                                       uint32_t* __restrict__ guide_jit, WaveCounters* cnt,
@@ -1111,7 +1155,7 @@ __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict_
     float sl = 0.0f, ssl = 0.0f;
     for (int s = 0; s < V.spp; s++) {
       RegPath st;
-      double jx, jy;
+      float jx, jy;
       primary_ray(V, x, y, s, seq, &st.o, &st.d, &st.rng, &jx, &jy);
       st.tp = f3(1.0f, 1.0f, 1.0f);
       st.L = f3(0.0f, 0.0f, 0.0f);
@@ -1199,7 +1243,7 @@ struct RenderBuffers {
   bcgx::WaveCounters* cnt = nullptr;
   bcgx::BatchState* bs = nullptr;
   bcgx::ViewGPU* views = nullptr;
-  double2* seq_xy = nullptr;
+  float4* seq_xy = nullptr;  // per sample: (x hi, x lo, y hi, y lo)
   float* sum = nullptr;        // 3 per pixel
   float* sumsq = nullptr;      // 3 per pixel (sample second moments, on request)
   bool want_sumsq = false;
@@ -1402,6 +1446,12 @@ int effective_spp(const bc_settings& s) {  // renderer.go:2395-2417
 
 // Halton table (buildSampleSequence, renderer.go:1883-1904), computed on the
 // host in fp64 exactly as the reference does; appended to X, Y.
+// fp64 value as a float-float pair (hi, lo): hi = fp32(v), lo = fp32(v - hi)
+static float2 ff_split(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+
 static void sample_sequence(const bc_settings& s, std::vector<double>* X, std::vector<double>* Y) {
   if (s.sampler == BC_SAMPLER_RANDOM) return;
   const int n = effective_spp(s);
@@ -1758,11 +1808,13 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
     }
     camera_basis(r.cam, (double)V.W / (double)V.H, V.origin, V.lower, V.horiz, V.vert);
     for (int k = 0; k < 3; k++) {
-      V.base[k] = V.lower[k] - V.origin[k];
+      V.base[k] = ff_split(V.lower[k] - V.origin[k]);
+      V.span_u[k] = ff_split(V.horiz[k]);
+      V.span_v[k] = ff_split(V.vert[k]);
       V.o32[k] = (float)V.origin[k];
     }
-    V.inv_w1 = 1.0 / (double)std::max(V.W - 1, 1);
-    V.inv_h1 = 1.0 / (double)std::max(V.H - 1, 1);
+    V.inv_w1 = ff_split(1.0 / (double)std::max(V.W - 1, 1));
+    V.inv_h1 = ff_split(1.0 / (double)std::max(V.H - 1, 1));
     V.path_off = total;
     total += (long long)V.npix * V.spp;
     max_bounces = std::max(max_bounces, V.bounces);
@@ -1821,7 +1873,7 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
   // device tables at fixed offsets (a captured wave keeps these addresses):
   // [BatchState | WaveCounters | views], and the (x, y) sample pairs
   const size_t tbytes = 512 + n * sizeof(ViewGPU);
-  const size_t sbytes = std::max<size_t>(16, X.size() * sizeof(double2));
+  const size_t sbytes = std::max<size_t>(16, X.size() * sizeof(float4));
   cudaError_t e = cudaStreamSynchronize(ctx->stream);  // the staging buffer may still be in flight
   if (!e) e = rb->table.ensure(tbytes);
   if (!e) e = rb->seq.ensure(sbytes);
@@ -1830,20 +1882,20 @@ bc_status render_views(bc_context* ctx, const std::vector<ViewRequest>& req, siz
   rb->bs = rb->table.as<BatchState>();
   rb->cnt = reinterpret_cast<WaveCounters*>((char*)rb->table.p + 256);
   rb->views = reinterpret_cast<ViewGPU*>((char*)rb->table.p + 512);
-  rb->seq_xy = rb->seq.as<double2>();
+  rb->seq_xy = rb->seq.as<float4>();
   char* hs = (char*)rb->staging.p;
   std::memset(hs, 0, 512);
   std::memcpy(hs, &bsh, sizeof(bsh));
   std::memcpy(hs + 512, views.data(), n * sizeof(ViewGPU));
-  double* hq = reinterpret_cast<double*>(hs + tbytes + ((16 - (tbytes & 15)) & 15));
+  float4* hq = reinterpret_cast<float4*>(hs + tbytes + ((16 - (tbytes & 15)) & 15));
   for (size_t i = 0; i < X.size(); i++) {
-    hq[2 * i] = X[i];
-    hq[2 * i + 1] = Y[i];
+    const float2 a = ff_split(X[i]), b = ff_split(Y[i]);
+    hq[i] = make_float4(a.x, a.y, b.x, b.y);
   }
   timing_begin(ctx);
   e = cudaMemcpyAsync(rb->table.p, hs, tbytes, cudaMemcpyHostToDevice, ctx->stream);
   if (!e && !X.empty())
-    e = cudaMemcpyAsync(rb->seq.p, hq, X.size() * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream);
+    e = cudaMemcpyAsync(rb->seq.p, hq, X.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream);
   for (int v = 0; v < n && !e; v++) {
     const ViewGPU& V = views[v];
     e = cudaMemsetAsync(rb->sum + 3 * (size_t)V.pix_off, 0, 3 * sizeof(float) * (size_t)V.npix, ctx->stream);

@@ -44,6 +44,15 @@ __host__ __device__ __forceinline__ Pcg32 make_path_rng(uint64_t seed, uint64_t 
 
 constexpr int kMaxRejection = 64;
 
+// rng.Intn(n) as the CPU draws it: floor(u n) of the fp64 product of the 24-bit
+// uniform u = k 2^-24 and n, capped at n - 1. Below n = 2^29 the product is
+// exact, so integer arithmetic gives the same index without fp64 work.
+__device__ __forceinline__ int draw_index(Pcg32& r, int n) {
+  const uint32_t k = r.next() >> 8;  // the draw of uniform()
+  if (n < (1 << 29)) return min((int)(((uint64_t)k * (uint64_t)n) >> 24), n - 1);
+  return min((int)((double)k * (1.0 / 16777216.0) * (double)n), n - 1);
+}
+
 __device__ __forceinline__ float3 rand_in_unit_sphere(Pcg32& r) {  // renderer.go:1262-1269
   float x = 0, y = 0, z = 0;
   for (int i = 0; i < kMaxRejection; i++) {
@@ -87,16 +96,17 @@ __device__ __forceinline__ float3 rand_cos_hemisphere(float3 n, Pcg32& r) {
   return make_float3(t.x * x + bt.x * y + n.x * z, t.y * x + bt.y * y + n.y * z, t.z * x + bt.z * y + n.z * z);
 }
 
-__host__ __device__ __forceinline__ void pixel_rotation(int x, int y, double* rx, double* ry) {
+// Per-pixel rotation of the sample table (renderer.go:1906-1915): the two 32-bit
+// hashes whose values times 2^-32 are the rotation offsets (rx, ry) in [0, 1).
+__host__ __device__ __forceinline__ void pixel_rotation_bits(int x, int y, uint32_t* h1_out, uint32_t* h2_out) {
   uint32_t h1 = ((uint32_t)x * 0x9e3779b1u) ^ ((uint32_t)y * 0x85ebca77u);
   h1 ^= h1 >> 16;
   h1 *= 0x7feb352du;
   h1 ^= h1 >> 15;
   uint32_t h2 = h1 ^ 0x68bc21ebu;
   h2 ^= h2 >> 13;
-  const double inv = 1.0 / 4294967296.0;
-  *rx = (double)h1 * inv;
-  *ry = (double)h2 * inv;
+  *h1_out = h1;
+  *h2_out = h2;
 }
 
 // ---- small fp32 vector helpers ---------------------------------------------

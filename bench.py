@@ -538,7 +538,7 @@ def measure_render(args):
     value = rays / sum(times) / 1e6
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 (fp64 primary rays)", "data": "synthetic, seeded",
+            "vs_baseline": None, "dtype": "f32 (float-float primary rays)", "data": "synthetic, seeded",
             "config": {"workload": workload, "spp": st.spp, "segments_per_frame": rays // max(1, args.steps),
                        "extend_variant": ctx.get_option("render_extend"),
                        "shade_block": ctx.get_option("render_shade_block")},
@@ -814,7 +814,7 @@ def measure_ultra(args):
     value = all_rays / (total_ms / 1e3) / 1e6
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 primary rays)", "data": ULTRA_DATA,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float-float primary rays)", "data": ULTRA_DATA,
             "config": {"workload": ULTRA_WORKLOAD, "spp": st.spp, "segments_per_step": rays // args.steps,
                        "triangles": spec.n_triangles(), "bvh8_nodes": stats["nodes8"],
                        "scene_bytes": stats["device_bytes"], "host_bvh_build_s": round(build_s, 2),
@@ -984,7 +984,7 @@ def measure_batch(args):
     plain_v = pr / sum(pt) / 1e6
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sum(bt) / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 primary rays)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float-float primary rays)",
             "data": "synthetic, seeded (seed 0xBEAC0004)",
             "config": {"workload": f"batch: {n_views} views over 4 resident scenes (10k/50k/200k/500k tris), "
                                    "128x128..1920x1080, spp U{4..64}, 8 bounces",
@@ -1284,7 +1284,7 @@ def run_integrators(args):
         value = rays / sum(times) / 1e6
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 primary rays)",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float-float primary rays)",
                 "data": "synthetic, seeded",
                 "config": {"workload": f"integrator comparison: Cornell-like room, 384x216, 2 spp, 5 bounces, "
                                        f"{integ}" + (", PhotonMapping 1" if st.photon_mapping else ""),

@@ -282,12 +282,13 @@ extern "C" {
 bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t scene_id, uint64_t topology_rev,
                           uint64_t geometry_rev) {
   if (!ctx || !scene) return set_error(ctx, BC_ERR_INVALID_ARG, "NULL context or scene");
+  const bool same_pack = ctx->packed_merge == ctx->scene_leaf_merge;
   if (ctx->has_scene && !ctx->is_set && ctx->scene_id == scene_id && ctx->topo_rev == topology_rev &&
-      ctx->geom_rev == geometry_rev)
+      ctx->geom_rev == geometry_rev && same_pack)
     return BC_OK;
   cudaSetDevice(ctx->device);
   bc_status st;
-  if (ctx->has_scene && !ctx->is_set && ctx->scene_id == scene_id && ctx->topo_rev == topology_rev) {
+  if (ctx->has_scene && !ctx->is_set && ctx->scene_id == scene_id && ctx->topo_rev == topology_rev && same_pack) {
     // only the geometry moved: rewrite primitives and node boxes on the device
     st = update_geometry(ctx, *scene);
     if (st == BC_OK) {
@@ -301,7 +302,9 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
   }
   PackedScene ps;
   std::string err;
-  st = pack_scene(*scene, &ps, &err);
+  CollapseParams cp;
+  cp.merge = ctx->scene_leaf_merge;
+  st = pack_scene(*scene, &ps, &err, cp);
   if (st != BC_OK) return set_error(ctx, st, err);
   SceneRange r;
   r.n_lights = (int32_t)ps.lights.size();
@@ -309,6 +312,7 @@ bc_status bc_scene_upload(bc_context* ctx, const bc_scene_desc* scene, uint64_t 
   scene_extent(*scene, &r);
   if ((st = install_scene(ctx, ps, std::vector<SceneRange>{r}))) return st;
   if ((st = keep_geometry_map(ctx, *scene, ps))) return st;
+  ctx->packed_merge = cp.merge;
   ctx->is_set = false;
   ctx->scene_id = scene_id;
   ctx->topo_rev = topology_rev;
@@ -320,15 +324,18 @@ bc_status bc_scene_set_upload(bc_context* ctx, const bc_scene_desc* scenes, int3
                               uint64_t revision) {
   if (!ctx || !scenes || n_scenes < 1) return set_error(ctx, BC_ERR_INVALID_ARG, "NULL argument or empty set");
   if (ctx->has_scene && ctx->is_set && ctx->scene_id == set_id && ctx->geom_rev == revision &&
-      (int32_t)ctx->ranges.size() == n_scenes)
+      (int32_t)ctx->ranges.size() == n_scenes && ctx->packed_merge == ctx->scene_leaf_merge)
     return BC_OK;
   cudaSetDevice(ctx->device);
   PackedScene ps;
   std::vector<SceneRange> ranges;
   std::string err;
-  bc_status st = pack_scene_set(scenes, n_scenes, &ps, &ranges, &err);
+  CollapseParams cp;
+  cp.merge = ctx->scene_leaf_merge;
+  bc_status st = pack_scene_set(scenes, n_scenes, &ps, &ranges, &err, cp);
   if (st != BC_OK) return set_error(ctx, st, err);
   if ((st = install_scene(ctx, ps, ranges))) return st;
+  ctx->packed_merge = cp.merge;
   ctx->is_set = true;
   ctx->scene_id = set_id;
   ctx->topo_rev = 0;
@@ -554,6 +561,11 @@ bc_status bc_set_option(bc_context* ctx, const char* name, int64_t value) {
     ctx->render_timing = (int)value;
     return BC_OK;
   }
+  if (n == "scene_leaf_merge") {
+    if (value < -1 || value > 1) return set_error(ctx, BC_ERR_INVALID_ARG, "scene_leaf_merge must be -1, 0 or 1");
+    ctx->scene_leaf_merge = (int)value;
+    return BC_OK;
+  }
   return set_error(ctx, BC_ERR_INVALID_ARG, "unknown option " + n);
 }
 
@@ -572,6 +584,7 @@ bc_status bc_get_option(const bc_context* ctx, const char* name, int64_t* value)
   if (n == "render_extend") { *value = ctx->render_extend; return BC_OK; }
   if (n == "render_shade_block") { *value = ctx->render_shade_block; return BC_OK; }
   if (n == "render_timing") { *value = ctx->render_timing; return BC_OK; }
+  if (n == "scene_leaf_merge") { *value = ctx->scene_leaf_merge; return BC_OK; }
   return BC_ERR_INVALID_ARG;
 }
 

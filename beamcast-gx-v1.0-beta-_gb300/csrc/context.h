@@ -104,6 +104,8 @@ struct bc_context {
   // bc_raycast, [2] bc_raycast_device
   unsigned long long* d_work = nullptr;
   long long render_wave_cap = 1 << 27;  // paths per wave (bc_set_option "render_wave_cap")
+  int scene_leaf_merge = -1;            // BVH8 leaf merging of the next upload (bc_set_option "scene_leaf_merge")
+  int packed_merge = -1;                // the leaf merging the resident scene was packed with
   int render_graph = 1;                 // replay a captured wave graph (bc_set_option "render_graph")
   int render_engine = 0;                // 0: wave engine, 1: one kernel per view (bc_set_option "render_engine")
   int render_extend = 1;                // k_extend variant 0..2 (bc_set_option "render_extend")

@@ -138,31 +138,48 @@ uint32_t leaf_ref(const bc_scene_desc& d, int32_t i) {
   return kLeafBit | ((uint32_t)(d.node_count[i] - 1) & 0xfu) << 27 | ((uint32_t)d.node_start[i] & kSlotMask);
 }
 
-// Wide collapse: repeatedly open the inner child of largest surface area
-// until a node has 8 children or only leaves. Leaves (and their primitive
-// ranges) are carried over unchanged, so the leaf sets match the binary tree.
-// Which binary subtrees become the children of each BVH8 node. The binary
-// leaves stay leaves (the leaf sets must be the reference's), so the traversal
-// cost that the choice changes is that of the node visits: the surface-area
-// heuristic charges each BVH8 node its box's area. A dynamic program over the
-// binary tree (after Ylitie, Karras and Laine, "Efficient Incoherent Ray
-// Traversal on GPUs Through Compressed Wide BVHs", HPG 2017, with the leaves
-// fixed) minimises the total: cost(i, k) is the least area sum of the BVH8
-// nodes that binary node i's subtree adds when it takes at most k child slots
-// of its parent; one slot makes i itself a child (its own BVH8 node if it is
-// inner, at cost A(i) + the best split of 8 slots between its children), more
-// slots may open it into its children's slots. It gives 10% less node area
-// than opening the largest child greedily on the Ultra-shaped scene, 8% on
-// the ray-cast scene; the hits are the same.
+// Which binary subtrees become the children of each BVH8 node, and which
+// become leaves. The surface-area heuristic charges each BVH8 node its box's
+// area A and each leaf tri_cost * A * (its primitives). A dynamic program over
+// the binary tree (after Ylitie, Karras and Laine, "Efficient Incoherent Ray
+// Traversal on GPUs Through Compressed Wide BVHs", HPG 2017) minimises the
+// total: cost(i, k) is the least cost that binary node i's subtree adds when
+// it takes at most k child slots of its parent. One slot makes i itself a
+// child: a leaf if it is one; if it is inner, its own BVH8 node (A(i) + the
+// best split of 8 slots between its children) or, when its subtree holds at
+// most max_leaf primitives in one contiguous slot range, a leaf of all of them.
+// More slots may open it into its children's slots. Every binary leaf's slots
+// stay in one BVH8 leaf, and the hits are the same whatever the choice.
+// Without merging the binary leaves stay exactly as they are; the node area is
+// then 10% below that of opening the largest child greedily on the
+// Ultra-shaped scene.
 class WideCollapse {
  public:
-  explicit WideCollapse(const bc_scene_desc& d) : d_(d), n_(d.n_nodes) {
+  WideCollapse(const bc_scene_desc& d, const CollapseParams& cp) : d_(d), n_(d.n_nodes) {
     cost_.assign((size_t)n_ * 9, 0.0);
     split_.assign((size_t)n_ * 9, 0);
     open_.assign((size_t)n_ * 9, 0);
+    merged_.assign(n_, 0);
+    start_.assign(n_, 0);
+    count_.assign(n_, 0);
+    const int max_leaf = cp.merges(d.n_prims) && cp.max_leaf > 0 && leaves_partition(d) ? std::min(cp.max_leaf, 16) : 0;
+    const double tri_cost = max_leaf > 0 ? cp.tri_cost : 0.0;  // 0: the node-area-only collapse
     for (int32_t i = n_ - 1; i >= 0; i--) {  // children follow their parent: reverse order is bottom-up
-      if (d.node_count[i] > 0) continue;     // a leaf adds no BVH8 node, whatever its slots
+      if (d.node_count[i] > 0) {
+        start_[i] = d.node_start[i];
+        count_[i] = d.node_count[i];
+        const double c = tri_cost * box_area(d.node_box + 6 * (size_t)i) * d.node_count[i];
+        for (int k = 1; k <= 8; k++) cost_[(size_t)i * 9 + k] = c;
+        continue;
+      }
       const int32_t l = d.node_left[i], r = d.node_right[i];
+      // the subtree's slots: one range when the children's ranges abut
+      const int32_t lo = std::min(start_[l], start_[r]);
+      const int64_t n = (int64_t)count_[l] + count_[r];
+      const bool run = count_[l] > 0 && count_[r] > 0 && n <= 16 &&
+                       (start_[l] + count_[l] == start_[r] || start_[r] + count_[r] == start_[l]);
+      start_[i] = run ? lo : 0;
+      count_[i] = run ? (int32_t)n : 0;  // 0: not one range of at most 16 slots
       double dist[9];  // dist[k]: the best split of k slots between the two children
       for (int k = 2; k <= 8; k++) {
         dist[k] = 0.0;
@@ -176,7 +193,15 @@ class WideCollapse {
         }
         split_[(size_t)i * 9 + k] = (uint8_t)at;
       }
-      cost_[(size_t)i * 9 + 1] = box_area(d.node_box + 6 * (size_t)i) + dist[8];
+      const double area = box_area(d.node_box + 6 * (size_t)i);
+      cost_[(size_t)i * 9 + 1] = area + dist[8];
+      if (count_[i] > 0 && count_[i] <= max_leaf) {
+        const double as_leaf = tri_cost * area * count_[i];
+        if (as_leaf < cost_[(size_t)i * 9 + 1]) {
+          cost_[(size_t)i * 9 + 1] = as_leaf;
+          merged_[i] = 1;
+        }
+      }
       for (int k = 2; k <= 8; k++) {
         const double fewer = cost_[(size_t)i * 9 + k - 1];
         const bool open = dist[k] < fewer;
@@ -193,9 +218,27 @@ class WideCollapse {
     expand(d_.node_right[w], 8 - a, kids, &nk);
     return nk;
   }
+  // A child that is a BVH8 leaf: a binary leaf, or an inner node merged into one.
+  bool is_leaf(int32_t i) const { return d_.node_count[i] > 0 || merged_[i]; }
+  uint32_t leaf_ref(int32_t i) const {
+    return kLeafBit | ((uint32_t)(count_[i] - 1) & 0xfu) << 27 | ((uint32_t)start_[i] & kSlotMask);
+  }
 
  private:
-  double cost(int32_t i, int k) const { return d_.node_count[i] > 0 ? 0.0 : cost_[(size_t)i * 9 + k]; }
+  // Every slot lies in exactly one binary leaf (a builder's tree always; a
+  // caller's tree is only checked for bounds), so merged ranges are exact.
+  static bool leaves_partition(const bc_scene_desc& d) {
+    std::vector<uint8_t> seen(d.n_prims, 0);
+    for (int32_t i = 0; i < d.n_nodes; i++)
+      for (int32_t s = d.node_start[i]; d.node_count[i] > 0 && s < d.node_start[i] + d.node_count[i]; s++) {
+        if (seen[s]) return false;
+        seen[s] = 1;
+      }
+    for (int32_t s = 0; s < d.n_prims; s++)
+      if (!seen[s]) return false;
+    return true;
+  }
+  double cost(int32_t i, int k) const { return cost_[(size_t)i * 9 + k]; }
   void expand(int32_t i, int k, int32_t kids[8], int* nk) const {
     while (k > 1 && d_.node_count[i] == 0 && !open_[(size_t)i * 9 + k]) k--;  // fewer slots were as good
     if (k == 1 || d_.node_count[i] > 0) {
@@ -211,11 +254,13 @@ class WideCollapse {
   std::vector<double> cost_;   // [node][k], k = 1..8
   std::vector<uint8_t> split_; // [node][k]: slots of the left child in the best split of k
   std::vector<uint8_t> open_;  // [node][k]: k slots open the node (else k - 1 were as good)
+  std::vector<uint8_t> merged_; // inner node that is a leaf when it takes one slot
+  std::vector<int32_t> start_, count_;  // the subtree's slot range (count 0: not one range)
 };
 
-void collapse(const bc_scene_desc& d, PackedScene* ps) {
+void collapse(const bc_scene_desc& d, const CollapseParams& cp, PackedScene* ps) {
   ps->nodes.clear();
-  const WideCollapse wide(d);
+  const WideCollapse wide(d, cp);
   struct Job { int32_t bin, parent, slot, depth, acc; };
   std::vector<Job> jobs{Job{0, -1, 0, 1, 0}};
   ps->depth = 0;
@@ -245,6 +290,8 @@ void collapse(const bc_scene_desc& d, PackedScene* ps) {
     for (int k = nk - 1; k >= 0; k--) {
       if (d.node_count[kids[k]] > 0) {
         ps->nodes[idx].child[k] = leaf_ref(d, kids[k]);
+      } else if (wide.is_leaf(kids[k])) {
+        ps->nodes[idx].child[k] = wide.leaf_ref(kids[k]);
       } else {
         jobs.push_back(Job{kids[k], idx, k, j.depth + 1, j.acc + nk - 1});
       }
@@ -317,14 +364,14 @@ void pack_binary(const bc_scene_desc& d, std::vector<BinNode>* out) {
   }
 }
 
-bc_status pack_scene(const bc_scene_desc& d, PackedScene* out, std::string* err) {
+bc_status pack_scene(const bc_scene_desc& d, PackedScene* out, std::string* err, const CollapseParams& cp) {
   bc_status st = validate(d, err);
   if (st != BC_OK) return st;
   try {
     out->n_prims = d.n_prims;
     out->n_binary = d.n_nodes;
     pack_slots(d, out);
-    collapse(d, out);
+    collapse(d, cp, out);
     pack_binary(d, &out->bin);
     pack_materials(d, out);
     pack_lights(d, out);
@@ -340,7 +387,7 @@ bc_status pack_scene(const bc_scene_desc& d, PackedScene* out, std::string* err)
 }
 
 bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::vector<SceneRange>* ranges,
-                         std::string* err) {
+                         std::string* err, const CollapseParams& cp) {
   if (n < 1 || !d) {
     if (err) *err = "a scene set needs at least one scene";
     return BC_ERR_INVALID_ARG;
@@ -349,7 +396,7 @@ bc_status pack_scene_set(const bc_scene_desc* d, int n, PackedScene* out, std::v
   ranges->assign(n, SceneRange());
   for (int k = 0; k < n; k++) {
     PackedScene ps;
-    bc_status st = pack_scene(d[k], &ps, err);
+    bc_status st = pack_scene(d[k], &ps, err, cp);
     if (st != BC_OK) {
       if (err) *err = "scene " + std::to_string(k) + ": " + *err;
       return st;

@@ -465,6 +465,13 @@ bc_status bc_post_process_noalloc(int32_t width, int32_t height, const float* d_
  *   "render_timing"      0 (default); 1: the renders record an event before every
  *                        kernel launch (no captured graph) for bc_last_timing's
  *                        per-kernel times; images are the same.
+ *   "scene_leaf_merge"   -1 (default): scenes of at most 1,024 primitives are
+ *                        packed with merged BVH8 leaves (inner binary subtrees of
+ *                        up to 8 primitives in one contiguous slot range become
+ *                        one leaf where a surface-area cost with a triangle test
+ *                        at 0.2 node visits favours it); 1: every scene; 0: the
+ *                        BVH8 leaves are the binary tree's leaves. Applies to the
+ *                        next scene upload; hits are the same either way.
  *   "render_engine"      0 (default): the wave engine; 1: one kernel launch per
  *                        view, one thread per pixel looping over samples and
  *                        bounces (the reference OpenCL kernel's shape, kept as the

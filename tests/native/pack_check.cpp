@@ -1,8 +1,10 @@
 // Host check of the BVH8 packer (compiled and run by tests/test_pack_native.py):
 // every quantized child box, decoded the way the device decodes it (round-down
 // lower bound, round-up upper bound of p + q * 2^e), must strictly contain the
-// fp64 box of the binary node it stands for, and the BVH8 leaves must be exactly
-// the binary tree's leaves.
+// fp64 box of the binary node it stands for; without leaf merging the BVH8
+// leaves must be exactly the binary tree's leaves, and with it every leaf must
+// hold the slots of one binary subtree and every slot lie in exactly one leaf.
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -19,9 +21,65 @@ using namespace bcgx;
 static float rd(double x) { return round_down_f32(x); }
 static float ru(double x) { return round_up_f32(x); }
 
+// slot range [lo, hi) and primitive count of binary node i's subtree
+static void subtree_range(const bc_scene_desc& d, int i, int64_t* lo, int64_t* hi, int64_t* n) {
+  if (d.node_count[i] > 0) {
+    *lo = d.node_start[i];
+    *hi = (int64_t)d.node_start[i] + d.node_count[i];
+    *n = d.node_count[i];
+    return;
+  }
+  int64_t l0, h0, n0, l1, h1, n1;
+  subtree_range(d, d.node_left[i], &l0, &h0, &n0);
+  subtree_range(d, d.node_right[i], &l1, &h1, &n1);
+  *lo = std::min(l0, l1);
+  *hi = std::max(h0, h1);
+  *n = n0 + n1;
+}
+
+static int check_merged(const bc_scene_desc& d) {
+  PackedScene ps;
+  std::string err;
+  CollapseParams cp;
+  cp.merge = 1;
+  if (pack_scene(d, &ps, &err, cp) != BC_OK) { std::printf("pack failed: %s\n", err.c_str()); return 1; }
+  std::vector<int> cover(d.n_prims, 0);
+  int merged = 0, bad = 0;
+  for (size_t i = 0; i < ps.nodes.size(); i++) {
+    const Node8& n = ps.nodes[i];
+    for (int k = 0; k < n.nchild; k++) {
+      const int b = ps.kids8[8 * i + k];
+      const double* box = d.node_box + 6 * (size_t)b;
+      const float p[3] = {n.px, n.py, n.pz};
+      const uint8_t e[3] = {n.ex, n.ey, n.ez};
+      const uint8_t ql[3] = {n.qlox[k], n.qloy[k], n.qloz[k]};
+      const uint8_t qh[3] = {n.qhix[k], n.qhiy[k], n.qhiz[k]};
+      for (int a = 0; a < 3; a++) {
+        const double sc = std::ldexp(1.0, (int)e[a] - 127);
+        const float lo = rd((double)p[a] + ql[a] * sc), hi = ru((double)p[a] + qh[a] * sc);
+        if (!((double)lo < box[a]) || !((double)hi > box[3 + a])) bad++;
+      }
+      if (!(n.child[k] & kLeafBit)) continue;
+      const int64_t start = n.child[k] & kSlotMask, cnt = ((n.child[k] >> 27) & 15u) + 1;
+      int64_t lo, hi, np;
+      subtree_range(d, b, &lo, &hi, &np);
+      if (lo != start || hi != start + cnt || np != cnt) { std::printf("leaf range differs from its subtree\n"); return 1; }
+      if (d.node_count[b] == 0) merged++;
+      for (int64_t s = start; s < start + cnt; s++) cover[s]++;
+    }
+  }
+  for (int32_t s = 0; s < d.n_prims; s++)
+    if (cover[s] != 1) { std::printf("slot %d in %d leaves\n", s, cover[s]); return 1; }
+  if (bad) { std::printf("%d non-conservative child bounds (merged)\n", bad); return 1; }
+  if (merged == 0) { std::printf("no merged leaf\n"); return 1; }
+  std::printf("ok merged nodes=%zu merged_leaves=%d\n", ps.nodes.size(), merged);
+  return 0;
+}
+
 static int check_scene(bc_hscene* s) {
   bc_scene_desc d;
   if (bc_hscene_describe(s, &d) != BC_OK) return 1;
+  if (check_merged(d)) return 1;
   PackedScene ps;
   std::string err;
   if (pack_scene(d, &ps, &err) != BC_OK) { std::printf("pack failed: %s\n", err.c_str()); return 1; }

@@ -1,5 +1,7 @@
 """Host checks of the device scene packer (no GPU): quantized BVH8 child boxes
-are strictly conservative and the BVH8 leaves are the binary tree's leaves."""
+are strictly conservative; the BVH8 leaves are the binary tree's leaves, or,
+with leaf merging on, each leaf holds one binary subtree's slots and every slot
+lies in exactly one leaf."""
 import os
 import shutil
 import subprocess
@@ -22,3 +24,4 @@ def test_quantized_nodes_conservative(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.count("ok nodes=") == 6
+    assert out.stdout.count("ok merged nodes=") == 6

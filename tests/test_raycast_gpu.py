@@ -293,3 +293,32 @@ def test_device_call_status_reaches_its_own_sync(gpu_ctx, native_lib):
         torch.cuda.synchronize()
         if call == "closest":  # the results themselves are unaffected by the hook
             assert np.array_equal(d_p.cpu().numpy(), p_h)
+
+
+@pytest.mark.parametrize("which", ["random", "stacked"])
+def test_merged_leaves_parity(gpu_ctx, orc, which):
+    """With BVH8 leaf merging forced on (option scene_leaf_merge 1: binary
+    subtrees of up to 8 primitives packed as one leaf), closest hits, exact ties
+    included, and any hits still match the oracle and the unmerged packing."""
+    if which == "random":
+        spec = scenes.random_triangles(100_000, seed=scenes.SEED_TRIS + 9)
+        rays = scenes.random_rays(262_144, seed=19)
+    else:
+        spec = _stacked_triangles(seed=43)
+        rays = scenes.random_rays(131_072, seed=20)
+    ref = orc.OracleScene.from_spec(spec)
+    s = scenes.to_scene(spec)
+    assert gpu_ctx.get_option("scene_leaf_merge") == -1
+    gpu_ctx.upload(s)
+    plain = gpu_ctx.raycast(rays)
+    try:
+        gpu_ctx.set_option("scene_leaf_merge", 1)
+        gpu_ctx.upload(s)  # same scene: the changed option repacks it
+        _check(gpu_ctx, ref, rays)
+        merged = gpu_ctx.raycast(rays)
+        occ = gpu_ctx.occluded(rays)
+    finally:
+        gpu_ctx.set_option("scene_leaf_merge", -1)
+    assert np.array_equal(merged[1], plain[1]) and np.array_equal(merged[0], plain[0])
+    occ_ref, _ = ref.occluded_f32(rays)
+    assert np.array_equal(occ, occ_ref)

@@ -41,9 +41,8 @@ struct PathSoA {
   float *tx, *ty, *tz;     // throughput
   float *lx, *ly, *lz;     // radiance of the path so far
   float *px, *py, *pz;     // prevPoint
-  float *ppdf;             // prevBSDFPDF
+  uint32_t* prev;          // prevBSDFPDF (fp32, >= 0) in bits 0-30, prevWasDiffuse in bit 31
   uint64_t *rs, *ri;       // PCG32 state and increment
-  uint32_t* flags;         // bit 0: prevWasDiffuse
   float* hit_t;
   int32_t* hit_slot;
   int32_t* view;           // view of the path
@@ -341,8 +340,7 @@ __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __r
   sst(ps.dx + i, d.x); sst(ps.dy + i, d.y); sst(ps.dz + i, d.z);
   sst(ps.tx + i, 1.0f); sst(ps.ty + i, 1.0f); sst(ps.tz + i, 1.0f);
   sst(ps.lx + i, 0.0f); sst(ps.ly + i, 0.0f); sst(ps.lz + i, 0.0f);
-  sst(ps.ppdf + i, 0.0f);
-  sst(ps.flags + i, 0u);
+  sst(ps.prev + i, 0u);
   sst(ps.rs + i, rng.state);
   sst(ps.ri + i, rng.inc);
   sst(ps.view + i, (int32_t)v);
@@ -464,24 +462,48 @@ __device__ __forceinline__ float light_dir_pdf(const ShadeScene& sc, int n_light
 // Path state between bounces as the shading step sees it. The wavefront
 // kernels keep it in the SoA arrays (SoAPath loads what a vertex needs and
 // stores what changes); the one-kernel renderer keeps it in registers (RegPath).
+// LAZY: the path's radiance L is read on its first addition at a vertex and
+// written back only if something was added; most vertices (a diffuse or metal
+// bounce without a light sample) leave it as it was, and the additions keep
+// their order. The kernel with the other integrators' code keeps L in
+// registers from the start: at its register budget the lazy form spills.
+template <bool LAZY>
 struct SoAPath {
   const PathSoA& ps;
   int path;
   float3 o, d, tp, L;
+  bool l_read, l_added;
   Pcg32 rng;
   uint32_t flags;
   float ppdf;
-  __device__ SoAPath(const PathSoA& p, int i) : ps(p), path(i) {
+  __device__ SoAPath(const PathSoA& p, int i) : ps(p), path(i), l_read(false), l_added(false) {
     o = f3(sld(ps.ox + i), sld(ps.oy + i), sld(ps.oz + i));
     d = f3(sld(ps.dx + i), sld(ps.dy + i), sld(ps.dz + i));
     tp = f3(sld(ps.tx + i), sld(ps.ty + i), sld(ps.tz + i));
-    L = f3(sld(ps.lx + i), sld(ps.ly + i), sld(ps.lz + i));
+    if (!LAZY) get_L();
+  }
+  __device__ __forceinline__ float3 get_L() {
+    if (!l_read) {
+      L = f3(sld(ps.lx + path), sld(ps.ly + path), sld(ps.lz + path));
+      l_read = true;
+    }
+    return L;
+  }
+  __device__ __forceinline__ void add_L(float3 v) {
+    L = get_L() + v;
+    l_added = true;
+  }
+  __device__ __forceinline__ void flush_L() {
+    if (!LAZY || l_added) {
+      sst(ps.lx + path, L.x); sst(ps.ly + path, L.y); sst(ps.lz + path, L.z);
+    }
   }
   __device__ __forceinline__ void load_vertex() {  // only a path that hit a valid material needs these
     rng.state = sld(ps.rs + path);
     rng.inc = sld(ps.ri + path);
-    flags = sld(ps.flags + path);
-    ppdf = sld(ps.ppdf + path);
+    const uint32_t w = sld(ps.prev + path);
+    flags = w >> 31;
+    ppdf = __uint_as_float(w & 0x7fffffffu);
   }
   __device__ __forceinline__ float3 prev() const {
     return f3(sld(ps.px + path), sld(ps.py + path), sld(ps.pz + path));
@@ -493,8 +515,7 @@ struct SoAPath {
     sst(ps.ox + path, no.x); sst(ps.oy + path, no.y); sst(ps.oz + path, no.z);
     sst(ps.dx + path, nd.x); sst(ps.dy + path, nd.y); sst(ps.dz + path, nd.z);
     sst(ps.tx + path, tp.x); sst(ps.ty + path, tp.y); sst(ps.tz + path, tp.z);
-    sst(ps.flags + path, flags);
-    sst(ps.ppdf + path, ppdf);
+    sst(ps.prev + path, (__float_as_uint(ppdf) & 0x7fffffffu) | (flags & 1u) << 31);  // ppdf >= 0 (or -0)
     sst(ps.rs + path, rng.state);
   }
 };
@@ -504,6 +525,8 @@ struct RegPath {
   Pcg32 rng;
   uint32_t flags;
   float ppdf;
+  __device__ __forceinline__ float3 get_L() const { return L; }
+  __device__ __forceinline__ void add_L(float3 v) { L = L + v; }
   __device__ __forceinline__ void load_vertex() {}
   __device__ __forceinline__ float3 prev() const { return pv; }
   __device__ __forceinline__ void set_prev(float3 p) { pv = p; }
@@ -612,7 +635,8 @@ __device__ __forceinline__ int sample_direct(const ViewGPU& wp, const ShadeScene
 // (the path-only kernels compile without their code).
 template <bool ALT, class P>
 __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, const ShadeScene& sc, P& s, float t,
-                                             int slot, int bounce, const GuideOut& gd, VertexOut& out) {
+                                             int slot, int bounce, const GuideOut& gd, VertexOut& out,
+                                             bool want_rec) {
   out.alive = false;
   out.shadow = false;
   out.rec_m = -1;
@@ -620,9 +644,8 @@ __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, cons
   const int rr_depth = wp.rr_depth < 1 ? 4 : wp.rr_depth;
   const float3 o = s.o, d = s.d;
   float3 tp = s.tp;
-  float3 L = s.L;
   if (slot < 0) {
-    L = L + had(tp, background(d));
+    s.add_L(had(tp, background(d)));
   } else {
     const float4 nrm = __ldg(sc.sv.snorm + slot);
     const int m = __float_as_int(nrm.w);
@@ -646,7 +669,7 @@ __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, cons
           }
           w = power_heuristic(ppdf, lpdf);
         }
-        L = L + had(tp, f3(M.er, M.eg, M.eb)) * w;
+        s.add_L(had(tp, f3(M.er, M.eg, M.eb)) * w);
         out.rec_m = m | kEmitTag;
         out.rec_v = tp * w;
       } else {
@@ -654,12 +677,12 @@ __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, cons
         float3 nd_dir = d, no = o;
         if (kind == BC_MAT_DIFFUSE) {
           out.rec_m = m;
-          out.rec_v = L;  // everything added from here on carries this albedo once more
-          if (ALT && wp.integrator == BC_INTEGRATOR_PHOTON) L = L + had(tp, photon_gather(wp.pm, p, N));
+          if (want_rec) out.rec_v = s.get_L();  // everything added from here on carries this albedo once more
+          if (ALT && wp.integrator == BC_INTEGRATOR_PHOTON) s.add_L(had(tp, photon_gather(wp.pm, p, N)));
           float3 contrib;
           const int k = sample_direct(wp, sc, rng, p, N, M, tp, &out.so, &out.sd, &contrib);
           if (k == 1) {
-            L = L + contrib;
+            s.add_L(contrib);
           } else if (k == 2) {
             out.shadow = true;
             out.scon = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
@@ -713,7 +736,6 @@ __device__ __forceinline__ void shade_vertex(const ViewGPU& wp, int n_mats, cons
       }
     }
   }
-  s.L = L;
 }
 
 // One vertex of traceRecursiveInner (renderer.go:1569-1621). s.tp is the weight
@@ -730,13 +752,12 @@ __device__ __forceinline__ bool shade_recursive(const ViewGPU& wp, int n_mats, c
   Pcg32 rng = s.rng;
   const float3 o = s.o, d = s.d;
   float3 W = s.tp;
-  float3 L = s.L;
   bool cont = false;
   float3 nd_dir = d, no = o;
   float4 rec = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
   const size_t r = (size_t)bounce * rr.cap + path;
   if (slot < 0) {
-    L = L + had(W, background(d));
+    s.add_L(had(W, background(d)));
   } else {
     const float4 nrm = __ldg(sc.sv.snorm + slot);
     const int m = __float_as_int(nrm.w);
@@ -748,7 +769,7 @@ __device__ __forceinline__ bool shade_recursive(const ViewGPU& wp, int n_mats, c
       const float3 col = f3(M.cr, M.cg, M.cb);
       if (gd.px >= 0) write_guides(gd, N, t, d, m);
       if (kind == BC_MAT_EMISSIVE) {
-        L = L + had(W, f3(M.er, M.eg, M.eb));
+        s.add_L(had(W, f3(M.er, M.eg, M.eb)));
       } else if (kind == BC_MAT_DIFFUSE) {
         const float scale = (wp.bounces - bounce < 8) ? 1.0f / fminf(fmaxf(maxcomp(col), 0.1f), 0.95f) : 1.0f;
         const float3 Wv = W * scale;
@@ -785,7 +806,6 @@ __device__ __forceinline__ bool shade_recursive(const ViewGPU& wp, int n_mats, c
     }
   }
   rr.a[r] = rec;
-  s.L = L;
   s.rng = rng;
   if (cont && bounce + 1 < wp.bounces) {  // depth - 1 > 0: the subtree is traced
     s.tp = W;
@@ -855,7 +875,7 @@ __device__ __forceinline__ void shade_body(const ViewGPU* __restrict__ views, in
     out.shadow = false;
     if (path >= 0) {
       const ViewGPU& wp = views[sld(ps.view + path)];
-      SoAPath s(ps, path);
+      SoAPath<!ALT> s(ps, path);
       GuideOut gd{guide_nd, guide_c, guide_jit, -1};
       if (bounce == 0 && wp.want_guides && ps.samp[path] == 0) gd.px = wp.pix_off + ps.pix[path];
       const float hit_t = sld(ps.hit_t + path);
@@ -865,9 +885,9 @@ __device__ __forceinline__ void shade_body(const ViewGPU* __restrict__ views, in
         out.alive = !ended;
         if (ended) unwind_recursive(wp, sc, s.rng, rr, path, bounce, sh, cnt, sh_cap, status);
       } else {
-        shade_vertex<ALT>(wp, n_mats, sc, s, hit_t, hit_slot, bounce, gd, out);
+        shade_vertex<ALT>(wp, n_mats, sc, s, hit_t, hit_slot, bounce, gd, out, rec.m != nullptr);
       }
-      sst(ps.lx + path, s.L.x); sst(ps.ly + path, s.L.y); sst(ps.lz + path, s.L.z);
+      s.flush_L();
       if (rec.m) {
         const size_t r = (size_t)bounce * rec.cap + path;
         rec.m[r] = out.rec_m;
@@ -1173,7 +1193,7 @@ __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict_
         segs++;
         const GuideOut gd{guide_nd, guide_c, guide_jit, (b == 0 && guide) ? V.pix_off + p : -1};
         VertexOut out;
-        shade_vertex<ALT>(V, n_mats, sc, st, leaf.best_t, leaf.best_slot, b, gd, out);
+        shade_vertex<ALT>(V, n_mats, sc, st, leaf.best_t, leaf.best_slot, b, gd, out, false);
         if (out.shadow) {
           shadows++;
           const Ray32 sr = make_ray(out.so.x, out.so.y, out.so.z, out.sd.x, out.sd.y, out.sd.z, 1e-4f);
@@ -1371,7 +1391,7 @@ static void timing_collect(bc_context* ctx) {
 static bc_status ensure_paths(bc_context* ctx, int cap, long long sh_cap) {
   RenderBuffers* rb = ctx->rb;
   if (rb->cap < cap) {
-    size_t per = 16 * sizeof(float) + 2 * sizeof(uint64_t) + sizeof(uint32_t) + sizeof(float) + 4 * sizeof(int32_t);
+    size_t per = 15 * sizeof(float) + sizeof(uint32_t) + 2 * sizeof(uint64_t) + sizeof(float) + 4 * sizeof(int32_t);
     cudaError_t e = rb->paths.ensure((size_t)cap * per + 64 * 256);
     if (e == cudaSuccess) e = rb->queues.ensure((size_t)cap * 2 * sizeof(int) + 4 * 256);
     if (e != cudaSuccess) {
@@ -1380,11 +1400,11 @@ static bc_status ensure_paths(bc_context* ctx, int cap, long long sh_cap) {
     }
     char* p = (char*)rb->paths.p;
     PathSoA& s = rb->ps;
-    float** fl[] = {&s.ox, &s.oy, &s.oz, &s.dx, &s.dy, &s.dz, &s.tx, &s.ty, &s.tz, &s.lx, &s.ly, &s.lz, &s.px, &s.py, &s.pz, &s.ppdf};
+    float** fl[] = {&s.ox, &s.oy, &s.oz, &s.dx, &s.dy, &s.dz, &s.tx, &s.ty, &s.tz, &s.lx, &s.ly, &s.lz, &s.px, &s.py, &s.pz};
     for (float** f : fl) *f = carve<float>(p, cap);
+    s.prev = carve<uint32_t>(p, cap);
     s.rs = carve<uint64_t>(p, cap);
     s.ri = carve<uint64_t>(p, cap);
-    s.flags = carve<uint32_t>(p, cap);
     s.hit_t = carve<float>(p, cap);
     s.hit_slot = carve<int32_t>(p, cap);
     s.view = carve<int32_t>(p, cap);

@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(128) k_photon_trace(PhotonTraceArgs a, unsigne
       float3 o = f3(Lg.cx, Lg.cy, Lg.cz) + surf * (Lg.r + 2e-4f);
       float3 d = rand_cos_hemisphere(surf, rng);
       float3 tp = f3(Lg.er, Lg.eg, Lg.eb) * ((4.0f * kPhotonPi * Lg.r * Lg.r) / (float)a.budget);
-      FastWalker<STACK> w;
+      FastWalker<STACK, kLeafVote> w;
       for (int b = 0; b < a.max_bounces; b++) {
         rays++;
         const Ray32 r = make_ray(o.x, o.y, o.z, d.x, d.y, d.z, 1e-4f);

@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(128, MINB) k_closest_exact_persistent(SceneVie
   bool exhausted = false;
   Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
   ExactClosestLeaf<false> leaf(sv, r, 0.0f, status);
-  Walker<STACK> w;
+  Walker<STACK, kExactLeafVote> w;
   w.reset(r);
   int parked = 0;  // warp-uniform
   for (;;) {
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(128, 12) k_exact_walk(SceneView sv, const floa
   bool exhausted = false;
   Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
   FilterLeaf leaf(sv, r);
-  Walker<STACK> w;
+  Walker<STACK, kExactLeafVote> w;
   w.reset(r);
   for (;;) {
     const bool need = idx < 0 && !exhausted;
@@ -594,7 +594,7 @@ __global__ void __launch_bounds__(128) k_closest_fast_persistent(SceneView sv, c
   bool exhausted = false;
   Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
   FastClosestLeaf<false> leaf(sv, r, 0.0f);
-  FastWalker<STACK> w;
+  FastWalker<STACK, kLeafVote> w;
   w.reset(r);
   for (;;) {
     const bool need = idx < 0 && !exhausted;

@@ -383,7 +383,7 @@ __device__ __forceinline__ void extend_body(SceneView sv, const ViewGPU* __restr
   Ray32& r = VAR == 2 ? ray_sh[threadIdx.x] : ray_reg;
   r = make_ray(0, 0, 0, 0, 0, 0, 0);
   FastClosestLeaf<SPH> leaf(sv, r, 1e30f);
-  FastWalker<STACK> w;
+  FastWalker<STACK, kLeafVote> w;
   w.reset(r);
   for (;;) {
     const bool need = path < 0 && !exhausted;
@@ -1170,7 +1170,7 @@ __global__ void __launch_bounds__(128) k_render_plain(const ViewGPU* __restrict_
     float* qp = sumsq ? sumsq + 3 * (size_t)(V.pix_off + p) : nullptr;
     float3 acc = f3(sp[0], sp[1], sp[2]);
     float3 acc2 = qp ? f3(qp[0], qp[1], qp[2]) : f3(0, 0, 0);
-    FastWalker<STACK> w;
+    FastWalker<STACK, kLeafVote> w;
     int an = 0;
     float sl = 0.0f, ssl = 0.0f;
     for (int s = 0; s < V.spp; s++) {

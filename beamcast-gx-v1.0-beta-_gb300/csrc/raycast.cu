@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(128, 12) k_any_walk(SceneView sv, const float4
   bool exhausted = false;
   Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
   FilterAnyLeaf leaf(sv, r);
-  Walker<STACK> w;
+  Walker<STACK, kAnyLeafVote> w;
   w.reset(r);
   for (;;) {
     const bool need = idx < 0 && !exhausted;

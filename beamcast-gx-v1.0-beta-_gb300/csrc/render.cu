@@ -941,7 +941,7 @@ __global__ void __launch_bounds__(128) k_connect(SceneView sv, PathSoA ps, Shado
   bool exhausted = false;
   Ray32 r = make_ray(0, 0, 0, 0, 0, 0, 0);
   FastAnyLeaf<SPH> leaf(sv, r, 0.0f);
-  FastWalker<STACK> w;
+  FastWalker<STACK, kAnyLeafVote> w;
   w.reset(r);
   for (;;) {
     const bool need = i < 0 && !exhausted;

@@ -31,10 +31,7 @@ constexpr float kFarSlack = 8.0e-7f;  // > 2*gamma_3 + rounding of the scaling i
 // of its lanes are idle, or when none is busy. A refill costs the whole warp a
 // ballot, a queue atomic and the new rays' loads, so taking one per finished
 // lane is slower than letting a few lanes wait.
-#ifndef BCGX_REFILL_LANES
-#define BCGX_REFILL_LANES 8
-#endif
-constexpr int kRefillLanes = BCGX_REFILL_LANES;
+constexpr int kRefillLanes = 8;
 
 struct Ray32 {
   float ox, oy, oz;
@@ -533,11 +530,12 @@ __device__ __forceinline__ uint32_t order_children(float nr[8], uint32_t ch[8], 
 // and leaf tests does not depend on it, so neither do the hits. Measured on
 // one box against 8 (A/B in one call): the render walk on the Ultra-shaped
 // frame 2,233 -> 2,264 / 2,373 / 2,379 / 2,292 / 2,092 Mseg/s at 6 / 4 / 3 / 2 / 1;
-// the exact closest-hit ray cast 557 -> 635 / 630 Mrays/s at 4 / 3; the
-// exact any hit 742 -> 626 / 723 at 4 / 3 (a lane stops at its first hit, and
-// any-hit walks keep 8).
+// the exact closest-hit ray cast 557 -> 551 / 603 / 635 / 630 Mrays/s at
+// 6 / 5 / 4 / 3; the exact any hit 742 -> 496 / 523 / 626 / 723 at 7 / 6 / 4 / 3
+// (a lane stops at its first hit, and any-hit walks keep 8).
 constexpr int kLeafVote = 3;       // closest-hit walks of the renderer
 constexpr int kExactLeafVote = 4;  // the exact closest-hit ray cast
+constexpr int kAnyLeafVote = 8;    // any-hit walks
 template <int VOTE>
 __device__ __forceinline__ bool leaf_phase_now(uint32_t pending) {
   const unsigned am = __activemask();

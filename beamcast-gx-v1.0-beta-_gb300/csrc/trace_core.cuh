@@ -31,7 +31,7 @@ constexpr float kFarSlack = 8.0e-7f;  // > 2*gamma_3 + rounding of the scaling i
 // of its lanes are idle, or when none is busy. A refill costs the whole warp a
 // ballot, a queue atomic and the new rays' loads, so taking one per finished
 // lane is slower than letting a few lanes wait.
-constexpr int kRefillLanes = 8;
+constexpr int kRefillLanes = 6;
 
 struct Ray32 {
   float ox, oy, oz;

@@ -351,8 +351,8 @@ __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __r
 }
 
 // ---- extend ----------------------------------------------------------------
-// Persistent: a lane whose ray is done takes the next queue entry at once (one
-// atomic per warp for all lanes that need work). The walk is latency-bound, so
+// Persistent: idle lanes take the next queue entries once kRefillLanes of the
+// warp's lanes are idle (one atomic per warp for all of them). The walk is latency-bound, so
 // resident warps matter; three variants trade registers against them
 // (bc_set_option "render_extend", chosen per workload by bc_autotune_render):
 //   0: the ray in registers, no register budget (51 registers, nine 128-thread

@@ -892,21 +892,34 @@ struct FastClosestLeaf {
     tlim = widen(tmax);
     done = false;
   }
+  __device__ __forceinline__ void test(int s, float4 A, float4 E1, float4 E2) {
+    float t;
+    const bool hit = (SPHERES && E2.w < 0.0f) ? sphere_hit32(A, E1, r, best_t, &t) : tri_hit32(A, E1, E2, r, best_t, &t);
+    if (hit) {
+      best_t = t;
+      best_slot = s;
+      tlim = widen(t);
+    }
+  }
+  // Triangles are loaded two at a time, so the second one's loads are in
+  // flight while the first is tested; they are tested in slot order.
   __device__ __forceinline__ void operator()(uint32_t ref) {
     const int cnt = (int)((ref >> 27) & 15u) + 1;
     const int s0 = (int)(ref & kSlotMask);
-    for (int k = 0; k < cnt; k++) {
+    for (int k = 0; k < cnt; k += 2) {
       const int s = s0 + k;
+      const bool two = k + 1 < cnt;
       const float4 A = __ldg(sv.tri + 3 * s);
       const float4 E1 = __ldg(sv.tri + 3 * s + 1);
       const float4 E2 = __ldg(sv.tri + 3 * s + 2);
-      float t;
-      const bool hit = (SPHERES && E2.w < 0.0f) ? sphere_hit32(A, E1, r, best_t, &t) : tri_hit32(A, E1, E2, r, best_t, &t);
-      if (hit) {
-        best_t = t;
-        best_slot = s;
-        tlim = widen(t);
+      float4 B = A, F1 = E1, F2 = E2;
+      if (two) {
+        B = __ldg(sv.tri + 3 * s + 3);
+        F1 = __ldg(sv.tri + 3 * s + 4);
+        F2 = __ldg(sv.tri + 3 * s + 5);
       }
+      test(s, A, E1, E2);
+      if (two) test(s + 1, B, F1, F2);
     }
   }
 };

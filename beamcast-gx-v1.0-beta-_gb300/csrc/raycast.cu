@@ -69,9 +69,9 @@ __global__ void __launch_bounds__(128) k_closest_fast(SceneView sv, const float4
 }
 
 // ---- persistent kernels with per-lane refill -------------------------------
-// A lane whose ray is done fetches the next ray index at once (one atomic per
-// warp for all lanes that need work), so the warp does not idle until its
-// slowest ray ends. The exact kernel parks each finished ray's contenders in a
+// Lanes whose rays are done fetch the next ray indices once kRefillLanes of the
+// warp's lanes are idle (one atomic per warp for all of them), so the warp does
+// not idle until its slowest ray ends. The exact kernel parks each finished ray's contenders in a
 // per-warp queue in shared memory; when 32 are parked, the warp settles them
 // in fp64 with every lane active. Triangle-only scenes (spheres settle at
 // once and use the kernels above).

@@ -4,13 +4,15 @@
 // views over a resident scene set:
 //
 //   generate  -> the wave's paths: global path index -> (view, sample, pixel);
-//                Halton jitter with the per-pixel rotation, fp64 primary ray
-//                (rounded to fp32), one PCG32 stream per (pixel, sample)
+//                Halton jitter with the per-pixel rotation, float-float primary
+//                ray (rounded to fp32), one PCG32 stream per (pixel, sample)
 //   extend    -> closest hit of every queued path from its view's scene root
-//                (persistent: a lane takes the next path as soon as its walk ends)
+//                (persistent: idle lanes take the next paths once a few of the
+//                warp's lanes are idle)
 //   shade     -> miss / emissive (MIS weight) / diffuse (NEE shadow ray + cosine
-//                bounce) / metal / glass, Russian roulette; survivors and shadow
-//                rays are pushed with warp-ballot compaction (one atomic per warp)
+//                bounce) / metal / glass, Russian roulette; survivors are pushed
+//                with block-level compaction (one atomic per block), shadow rays
+//                with warp-ballot compaction (one atomic per warp)
 //   connect   -> any hit for the shadow queue; unoccluded contributions are added
 //   accumulate-> per pixel, the firefly-clamped sample radiance of the wave,
 //                summed in sample order (no atomics: one thread per pixel)

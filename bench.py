@@ -15,7 +15,7 @@ the unit the reference counts as Rays (renderer.go:1491).
   value   : Mpath-segments/s of the wave engine: extension rays / device time
             of the frame (CUDA events the library records on its launching
             stream before the frame's first and after its last device work,
-            read with bc_last_timing). The path state (128 Mi paths x 104 B)
+            read with bc_last_timing). The path state (128 Mi paths x 100 B)
             and the scene (~300 MB) exceed L2, so no flush is needed.
   plain   : the same frames (same seeds, same samples, so equal RMSE) by the
             one-kernel form: one launch per view, a thread per pixel looping
@@ -818,7 +818,7 @@ def measure_ultra(args):
             "config": {"workload": ULTRA_WORKLOAD, "spp": st.spp, "segments_per_step": rays // args.steps,
                        "triangles": spec.n_triangles(), "bvh8_nodes": stats["nodes8"],
                        "scene_bytes": stats["device_bytes"], "host_bvh_build_s": round(build_s, 2),
-                       "l2": "not flushed: path state (128 Mi paths x 104 B) and scene exceed the 126 MB L2",
+                       "l2": "not flushed: path state (128 Mi paths x 100 B) and scene exceed the 126 MB L2",
                        "wave_cap": ctx.get_option("render_wave_cap"),
                        "extend_variant": ctx.get_option("render_extend"),
                        "shade_block": ctx.get_option("render_shade_block"),

@@ -131,9 +131,50 @@ static int check_scene(bc_hscene* s) {
   return 0;
 }
 
+// The light records' fp32 CDF copy is the largest fp32 value <= the fp64 CDF
+// entry, so the device's fp32 comparison with an fp32 draw takes the fp64
+// comparison's branch for every draw.
+static int check_light_cdf() {
+  std::mt19937_64 rng(777);
+  std::uniform_real_distribution<double> U(0, 1);
+  bc_hscene* s = bc_hscene_create();
+  const double c0[3] = {0.5, 0.5, 0.5}, e0[3] = {0, 0, 0};
+  const int diffuse = bc_hscene_add_material(s, BC_MAT_DIFFUSE, c0, 0, 0, e0);
+  for (int k = 0; k < 300; k++) {
+    const double em[3] = {0.1 + 10 * U(rng), 0.1 + U(rng), 0.1 + 3 * U(rng)};
+    const int m = bc_hscene_add_material(s, BC_MAT_EMISSIVE, c0, 0, 0, em);
+    const double c[3] = {U(rng), U(rng), U(rng)};
+    bc_hscene_add_sphere(s, c, 0.001 + 0.05 * U(rng), k % 7 ? m : diffuse);
+  }
+  bc_hscene_set_bvh(s, "SAH", 32, 4);
+  bc_hscene_build(s);
+  bc_scene_desc d;
+  int rc = bc_hscene_describe(s, &d) != BC_OK;
+  PackedScene ps;
+  std::string err;
+  if (!rc && pack_scene(d, &ps, &err) != BC_OK) rc = 1;
+  int exact = 0;
+  for (size_t i = 0; !rc && i < ps.lights.size(); i++) {
+    const double cdf = ps.lights[i].cdf;
+    const float dn = ps.lights[i].cdf_dn;
+    if (!((double)dn <= cdf) || !((double)std::nextafter(dn, INFINITY) > cdf)) {
+      std::printf("light %zu: cdf_dn %.9g not the largest fp32 <= %.17g\n", i, dn, cdf);
+      rc = 1;
+    }
+    exact += (double)dn == cdf;
+  }
+  if (!rc && ps.lights.size() < 200) {
+    std::printf("only %zu lights\n", ps.lights.size());
+    rc = 1;
+  }
+  if (!rc) std::printf("ok light cdf lights=%zu exact=%d\n", ps.lights.size(), exact);
+  bc_hscene_destroy(s);
+  return rc;
+}
+
 int main() {
   std::mt19937_64 rng(12345);
-  int rc = 0;
+  int rc = check_light_cdf();
   for (int trial = 0; trial < 6; trial++) {
     bc_hscene* s = bc_hscene_create();
     double c0[3] = {0.5, 0.5, 0.5}, e0[3] = {0, 0, 0};

@@ -1,7 +1,8 @@
 """Host checks of the device scene packer (no GPU): quantized BVH8 child boxes
 are strictly conservative; the BVH8 leaves are the binary tree's leaves, or,
 with leaf merging on, each leaf holds one binary subtree's slots and every slot
-lies in exactly one leaf."""
+lies in exactly one leaf; the sphere lights' fp32 CDF copies are the largest
+fp32 values not above their fp64 entries."""
 import os
 import shutil
 import subprocess
@@ -25,3 +26,4 @@ def test_quantized_nodes_conservative(tmp_path):
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.count("ok nodes=") == 6
     assert out.stdout.count("ok merged nodes=") == 6
+    assert "ok light cdf" in out.stdout

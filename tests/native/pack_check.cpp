@@ -76,10 +76,43 @@ static int check_merged(const bc_scene_desc& d) {
   return 0;
 }
 
+// A caller's tree whose leaf ranges overlap passes the bounds checks but is no
+// partition of the slots: leaf merging then stays off, and every BVH8 leaf is
+// one of the caller's leaves.
+static int check_overlapping_leaves(const bc_scene_desc& d0) {
+  std::vector<int32_t> start(d0.node_start, d0.node_start + d0.n_nodes);
+  int first = -1, second = -1;
+  for (int i = 0; i < d0.n_nodes; i++)
+    if (d0.node_count[i] > 0) {
+      if (first < 0) first = i;
+      else if (second < 0 && start[i] != start[first]) second = i;
+    }
+  if (first < 0 || second < 0) { std::printf("fewer than two leaves\n"); return 1; }
+  start[second] = start[first];  // the two leaves now share slots
+  bc_scene_desc d = d0;
+  d.node_start = start.data();
+  PackedScene ps;
+  std::string err;
+  CollapseParams cp;
+  cp.merge = 1;
+  if (pack_scene(d, &ps, &err, cp) != BC_OK) { std::printf("pack failed: %s\n", err.c_str()); return 1; }
+  for (size_t i = 0; i < ps.nodes.size(); i++)
+    for (int k = 0; k < ps.nodes[i].nchild; k++) {
+      const int b = ps.kids8[8 * i + k];
+      if ((ps.nodes[i].child[k] & kLeafBit) && d.node_count[b] == 0) {
+        std::printf("merged leaf over overlapping ranges\n");
+        return 1;
+      }
+    }
+  std::printf("ok overlapping leaves unmerged\n");
+  return 0;
+}
+
 static int check_scene(bc_hscene* s) {
   bc_scene_desc d;
   if (bc_hscene_describe(s, &d) != BC_OK) return 1;
   if (check_merged(d)) return 1;
+  if (check_overlapping_leaves(d)) return 1;
   PackedScene ps;
   std::string err;
   if (pack_scene(d, &ps, &err) != BC_OK) { std::printf("pack failed: %s\n", err.c_str()); return 1; }

@@ -27,3 +27,4 @@ def test_quantized_nodes_conservative(tmp_path):
     assert out.stdout.count("ok nodes=") == 6
     assert out.stdout.count("ok merged nodes=") == 6
     assert "ok light cdf" in out.stdout
+    assert out.stdout.count("ok overlapping leaves unmerged") == 6

@@ -357,12 +357,12 @@ __global__ void k_generate(const BatchState* __restrict__ bs, const ViewGPU* __r
 // warp's lanes are idle (one atomic per warp for all of them). The walk is latency-bound, so
 // resident warps matter; three variants trade registers against them
 // (bc_set_option "render_extend", chosen per workload by bc_autotune_render):
-//   0: the ray in registers, no register budget (51 registers, nine 128-thread
+//   0: the ray in registers, no register budget (56 registers, nine 128-thread
 //      blocks per SM);
-//   1: the ray in registers, 48 registers (ten blocks; ptxas spills 10 bytes);
+//   1: the ray in registers, 48 registers (ten blocks; ptxas spills 26 bytes);
 //   2: each thread's ray in shared memory, which the triangle tests read (the
 //      node test keeps its per-ray constants in registers): 40 registers
-//      without spills, twelve blocks.
+//      (82 bytes spilled), twelve blocks.
 // All three compute the same hits.
 constexpr int kExtendVariants = 3;
 

@@ -7,6 +7,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <system_error>
+#include <thread>
 
 #include "quantize.h"
 
@@ -28,6 +30,29 @@ float round_down_f32(double x) { return rd_f32(x); }
 float round_up_f32(double x) { return ru_f32(x); }
 
 namespace {
+
+// f(lo, hi) over [0, n) in contiguous chunks of at least min_chunk items, on up
+// to 16 host threads; the chunks write disjoint outputs. Where no thread can be
+// started, the rest runs on the calling thread.
+template <class F>
+void parallel_chunks(int64_t n, int64_t min_chunk, const F& f) {
+  const int64_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const int64_t chunks = std::min<int64_t>(hw, (n + min_chunk - 1) / std::max<int64_t>(1, min_chunk));
+  if (chunks <= 1) {
+    if (n > 0) f((int64_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve((size_t)chunks - 1);
+  int64_t c = 1;
+  try {
+    for (; c < chunks; c++) th.emplace_back(f, n * c / chunks, n * (c + 1) / chunks);
+  } catch (const std::system_error&) {
+    for (int64_t k = c; k < chunks; k++) f(n * k / chunks, n * (k + 1) / chunks);
+  }
+  f((int64_t)0, n / chunks);
+  for (std::thread& t : th) t.join();
+}
 
 double box_area(const double* b) {
   double ex = b[3] - b[0], ey = b[4] - b[1], ez = b[5] - b[2];
@@ -111,22 +136,24 @@ void pack_slots(const bc_scene_desc& d, PackedScene* ps) {
   ps->snorm.resize(n);
   ps->slot_prim.resize(n);
   ps->has_spheres = false;
-  for (int32_t s = 0; s < n; s++) {
-    const int32_t p = d.order[s];
-    ps->slot_prim[s] = p;
-    int32_t mat = d.prim_material[p];
-    float matbits;
-    std::memcpy(&matbits, &mat, 4);
-    const bool sphere = d.prim_kind[p] == BC_PRIM_SPHERE;
-    ps->has_spheres = ps->has_spheres || sphere;
-    const double zero[3] = {0.0, 0.0, 0.0};
-    const size_t k3 = 3 * (size_t)p;
-    float nrm[3];
-    pack_slot(sphere, sphere ? d.prim_center + k3 : zero, sphere ? d.prim_radius[p] : 0.0,
-              sphere ? zero : d.prim_a + k3, sphere ? zero : d.prim_e1 + k3, sphere ? zero : d.prim_e2 + k3,
-              sphere ? zero : d.prim_normal + k3, &ps->tri[3 * (size_t)s], &ps->slot64[9 * (size_t)s], nrm);
-    ps->snorm[s] = F4{nrm[0], nrm[1], nrm[2], matbits};
-  }
+  for (int32_t p = 0; p < n && !ps->has_spheres; p++) ps->has_spheres = d.prim_kind[p] == BC_PRIM_SPHERE;
+  parallel_chunks(n, 1 << 16, [&](int64_t lo, int64_t hi) {
+    for (int32_t s = (int32_t)lo; s < (int32_t)hi; s++) {
+      const int32_t p = d.order[s];
+      ps->slot_prim[s] = p;
+      int32_t mat = d.prim_material[p];
+      float matbits;
+      std::memcpy(&matbits, &mat, 4);
+      const bool sphere = d.prim_kind[p] == BC_PRIM_SPHERE;
+      const double zero[3] = {0.0, 0.0, 0.0};
+      const size_t k3 = 3 * (size_t)p;
+      float nrm[3];
+      pack_slot(sphere, sphere ? d.prim_center + k3 : zero, sphere ? d.prim_radius[p] : 0.0,
+                sphere ? zero : d.prim_a + k3, sphere ? zero : d.prim_e1 + k3, sphere ? zero : d.prim_e2 + k3,
+                sphere ? zero : d.prim_normal + k3, &ps->tri[3 * (size_t)s], &ps->slot64[9 * (size_t)s], nrm);
+      ps->snorm[s] = F4{nrm[0], nrm[1], nrm[2], matbits};
+    }
+  });
 }
 
 void quantize_node(Node8& n, const double* boxes, int nk) {
@@ -162,15 +189,44 @@ class WideCollapse {
     merged_.assign(n_, 0);
     start_.assign(n_, 0);
     count_.assign(n_, 0);
-    const int max_leaf = cp.merges(d.n_prims) && cp.max_leaf > 0 && leaves_partition(d) ? std::min(cp.max_leaf, 16) : 0;
-    const double tri_cost = max_leaf > 0 ? cp.tri_cost : 0.0;  // 0: the node-area-only collapse
-    for (int32_t i = n_ - 1; i >= 0; i--) {  // children follow their parent: reverse order is bottom-up
+    max_leaf_ = cp.merges(d.n_prims) && cp.max_leaf > 0 && leaves_partition(d) ? std::min(cp.max_leaf, 16) : 0;
+    tri_cost_ = max_leaf_ > 0 ? cp.tri_cost : 0.0;  // 0: the node-area-only collapse
+    // A node needs only its children's results: the levels of the tree are
+    // solved deepest first, the nodes of a level in parallel (children follow
+    // their parent, so one forward pass gives the depths).
+    std::vector<int32_t> depth(n_, 0);
+    int32_t max_depth = 0;
+    for (int32_t i = 0; i < n_; i++)
+      if (d.node_count[i] == 0) {
+        depth[d.node_left[i]] = depth[d.node_right[i]] = depth[i] + 1;
+        max_depth = std::max(max_depth, depth[i] + 1);
+      }
+    std::vector<int32_t> at((size_t)max_depth + 2, 0), order(n_);
+    for (int32_t i = 0; i < n_; i++) at[depth[i] + 1]++;
+    for (int32_t k = 0; k <= max_depth; k++) at[k + 1] += at[k];
+    {
+      std::vector<int32_t> fill(at.begin(), at.end() - 1);
+      for (int32_t i = 0; i < n_; i++) order[fill[depth[i]]++] = i;
+    }
+    for (int32_t k = max_depth; k >= 0; k--) {
+      const int32_t* lvl = order.data() + at[k];
+      parallel_chunks(at[k + 1] - at[k], 1 << 14, [&](int64_t lo, int64_t hi) {
+        for (int64_t j = lo; j < hi; j++) solve(lvl[j]);
+      });
+    }
+  }
+  // The DP entries of binary node i from its children's.
+  void solve(int32_t i) {
+    const bc_scene_desc& d = d_;
+    const int max_leaf = max_leaf_;
+    const double tri_cost = tri_cost_;
+    {
       if (d.node_count[i] > 0) {
         start_[i] = d.node_start[i];
         count_[i] = d.node_count[i];
         const double c = tri_cost * box_area(d.node_box + 6 * (size_t)i) * d.node_count[i];
         for (int k = 1; k <= 8; k++) cost_[(size_t)i * 9 + k] = c;
-        continue;
+        return;
       }
       const int32_t l = d.node_left[i], r = d.node_right[i];
       // the subtree's slots: one range when the children's ranges abut
@@ -256,6 +312,8 @@ class WideCollapse {
   std::vector<uint8_t> open_;  // [node][k]: k slots open the node (else k - 1 were as good)
   std::vector<uint8_t> merged_; // inner node that is a leaf when it takes one slot
   std::vector<int32_t> start_, count_;  // the subtree's slot range (count 0: not one range)
+  int max_leaf_ = 0;
+  double tri_cost_ = 0.0;
 };
 
 void collapse(const bc_scene_desc& d, const CollapseParams& cp, PackedScene* ps) {

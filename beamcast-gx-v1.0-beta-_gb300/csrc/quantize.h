@@ -3,6 +3,7 @@
 // device geometry update (refit.cu): both paths produce the same bytes.
 #pragma once
 #include <math.h>
+#include <algorithm>
 #include <stdint.h>
 
 #include "layout.h"
@@ -50,7 +51,12 @@ BC_HD void quantize_children(Node8& n, const double* boxes, int nk) {
   for (int a = 0; a < 3; a++) {
     p[a] = nextafterf(rd_f32(lo[a]), -INFINITY);
     const double extent = hi[a] - (double)p[a];
+    // the least e in [-126, 127] with 254 * 2^e >= extent (127 if none); the
+    // host starts the search at ilogb(extent) - 9, which is never above it
     int e = -126;
+#ifndef __CUDA_ARCH__
+    if (extent > 0) e = std::max(-126, std::min(127, ilogb(extent) - 9));
+#endif
     while (e < 127 && ldexp(254.0, e) < extent) e++;
     eb[a] = (uint8_t)(e + 127);
     scale[a] = ldexp(1.0, e);

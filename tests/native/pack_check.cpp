@@ -205,9 +205,57 @@ static int check_light_cdf() {
   return rc;
 }
 
+// A scene large enough for the packer's threads (slot records in chunks of
+// 65,536, tree levels of more than 16,384 nodes): two packs of it are
+// byte-identical, with and without leaf merging.
+static int check_threaded_pack() {
+  std::mt19937_64 rng(99);
+  std::uniform_real_distribution<double> U(0, 1);
+  bc_hscene* s = bc_hscene_create();
+  const double c0[3] = {0.5, 0.5, 0.5}, e0[3] = {0, 0, 0};
+  const int m = bc_hscene_add_material(s, BC_MAT_DIFFUSE, c0, 0, 0, e0);
+  const int n = 300000;
+  std::vector<double> v(9 * (size_t)n);
+  for (int t = 0; t < n; t++) {
+    const double c[3] = {U(rng), U(rng), U(rng)};
+    for (int j = 0; j < 3; j++)
+      for (int a = 0; a < 3; a++) v[9 * (size_t)t + 3 * j + a] = c[a] + (U(rng) - 0.5) * 0.01;
+  }
+  std::vector<int32_t> mats(n, m);
+  bc_hscene_add_triangles(s, n, v.data(), mats.data());
+  bc_hscene_set_bvh(s, "SAH", 32, 4);
+  bc_hscene_build(s);
+  bc_scene_desc d;
+  int rc = bc_hscene_describe(s, &d) != BC_OK;
+  for (int merge = 0; merge <= 1 && !rc; merge++) {
+    CollapseParams cp;
+    cp.merge = merge;
+    PackedScene a, b;
+    std::string err;
+    if (pack_scene(d, &a, &err, cp) != BC_OK || pack_scene(d, &b, &err, cp) != BC_OK) {
+      std::printf("pack failed: %s\n", err.c_str());
+      rc = 1;
+      break;
+    }
+    auto same = [](const auto& x, const auto& y) {
+      return x.size() == y.size() && std::memcmp(x.data(), y.data(), x.size() * sizeof(x[0])) == 0;
+    };
+    if (!same(a.nodes, b.nodes) || !same(a.tri, b.tri) || !same(a.slot64, b.slot64) || !same(a.snorm, b.snorm) ||
+        !same(a.slot_prim, b.slot_prim) || !same(a.kids8, b.kids8) || a.stack_need != b.stack_need) {
+      std::printf("two packs differ (merge %d)\n", merge);
+      rc = 1;
+    }
+  }
+  if (!rc) rc = check_scene(s);
+  if (!rc) std::printf("ok threaded pack\n");
+  bc_hscene_destroy(s);
+  return rc;
+}
+
 int main() {
   std::mt19937_64 rng(12345);
   int rc = check_light_cdf();
+  rc |= check_threaded_pack();
   for (int trial = 0; trial < 6; trial++) {
     bc_hscene* s = bc_hscene_create();
     double c0[3] = {0.5, 0.5, 0.5}, e0[3] = {0, 0, 0};

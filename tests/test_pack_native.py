@@ -20,11 +20,12 @@ def test_quantized_nodes_conservative(tmp_path):
     csrc = os.path.join(PKG_DIR, "csrc")
     cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I" + csrc, "-I" + os.path.join(ROOT, "include"),
            os.path.join(ROOT, "tests", "native", "pack_check.cpp"), os.path.join(csrc, "pack.cpp"),
-           os.path.join(csrc, "host_scene.cpp"), "-o", str(exe)]
+           os.path.join(csrc, "host_scene.cpp"), "-pthread", "-o", str(exe)]
     subprocess.run(cmd, check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
-    assert out.stdout.count("ok nodes=") == 6
-    assert out.stdout.count("ok merged nodes=") == 6
+    assert out.stdout.count("ok nodes=") == 7
+    assert out.stdout.count("ok merged nodes=") == 7
+    assert "ok threaded pack" in out.stdout
     assert "ok light cdf" in out.stdout
-    assert out.stdout.count("ok overlapping leaves unmerged") == 6
+    assert out.stdout.count("ok overlapping leaves unmerged") == 7
